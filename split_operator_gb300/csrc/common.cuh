@@ -1,0 +1,109 @@
+// Shared device-side definitions of the split-operator GB300 library.
+//
+// A wave function lives in GPU memory as interleaved complex values (double2 or
+// float2) in "storage order": row-major over the logical axes permuted by
+// `perm` (storage position p holds logical axis perm[p]); the propagation puts
+// its FFT axis last so radial FFT lanes are contiguous.
+//
+// Work is issued as *passes*.  A pass owns whole lanes along one axis (the
+// sweep axis): every CTA loads a tile of complete lanes into shared memory,
+// runs a short program of ops on it (diagonal multiplies, FFT or lane matrix
+// along the sweep axis, FP64 norm partial sums), stores it back, and the last
+// CTA to finish folds the norm partials in a fixed order (deterministic) and
+// runs the program's scalar bookkeeping (loss accumulation, slot copies).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace so {
+
+constexpr int kMaxDims = 4;
+constexpr int kMaxOps = 24;
+constexpr int kMaxRed = 8;      // norm reductions per pass
+constexpr int kNumSlots = 256;  // FP64 scalar slots per engine
+
+enum OpKind : int32_t {
+  OP_DIAG1D = 0,     // psi *= table[coord(axis)]
+  OP_DIAGND = 1,     // psi *= table[storage index]
+  OP_FFT = 2,        // unitary DFT along the sweep axis, dir = -1 forward, +1 inverse
+  OP_MAT = 3,        // lane <- M lane along the sweep axis (one matrix)
+  OP_MAT_LANE = 4,   // matrix per lane (non-diagonal propagator)
+  OP_MAT_SLICE = 5,  // matrix per index of a dependent axis (state matrix transformation)
+  OP_NORM = 6,       // slot[a] = sum |psi|^2 prod_axis w_axis (FP64)
+  OP_COPY = 7,       // slot[a] = slot[b]
+  OP_LOSS = 8,       // slot[a] += slot[b] - slot[c]
+  OP_SCALE = 9,      // psi *= sqrt(slot[b] / slot[c])
+  OP_SETC = 10,      // slot[a] = value
+  OP_RECORD = 11,    // record[count] = slot[a]
+  OP_DOT = 12        // slot[a] + i slot[b] = sum psi conj(other) prod w  (other = ptr, same layout)
+};
+
+struct DevOp {
+  int32_t kind;
+  int32_t axis;   // logical axis (DIAG1D), dependent axis (MAT_SLICE)
+  int32_t dir;    // FFT direction
+  int32_t a, b, c;
+  int32_t red;    // reduction index inside the pass (NORM, DOT uses red and red+1)
+  int32_t flags;  // bit0: matrix is real
+  int64_t count;  // matrices available (MAT_LANE / MAT_SLICE), record index (RECORD)
+  double value;   // SETC
+  const void* ptr;               // table / matrix base / other wave function
+  const double* w[kMaxDims];     // NORM / DOT weights per logical axis
+};
+
+struct Geometry {
+  int32_t ndim;
+  int32_t perm[kMaxDims];       // storage position -> logical axis
+  int64_t sshape[kMaxDims];     // storage shape
+  int32_t spos;                 // storage position of the sweep axis
+  int32_t sweep_axis;           // logical sweep axis
+  int64_t n;                    // sweep axis extent
+  int64_t inner;                // product of storage dims after spos
+  int64_t outer;                // product of storage dims before spos
+  int32_t lanes_per_tile;       // L
+  int32_t tiles_per_outer;      // inner > 1: inner / L; inner == 1: 1
+  int64_t tiles;                // grid size
+  int32_t vals;                 // V: values a thread holds in FFT/MAT ops
+  int32_t lane_stride;          // padded shared-memory lane stride (complex units)
+};
+
+struct PassParams {
+  Geometry g;
+  void* psi;
+  double* slots;
+  double* partials;             // [kMaxRed][tiles]
+  unsigned int* counter;        // last-block ticket (reset by the last block)
+  const void* twiddle;          // exp(-2 pi i j / n), j < n, in the state precision
+  double* record;
+  int32_t nops;
+  int32_t nred;
+  int32_t repeat;               // resident mode: program repetitions
+  int32_t resident;             // 1: single CTA owns the whole array, scalars are immediate
+  int32_t nonfinite_slot;       // slot set to 1 if a norm is not finite
+  DevOp ops[kMaxOps];
+};
+
+// Host launchers (lane_sweep.cu)
+cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);
+cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s);
+size_t pass_smem_bytes(const Geometry& g, bool fp64);
+int pass_threads(const Geometry& g);
+
+// Auxiliary kernels (aux_kernels.cu)
+cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);
+// dst (storage order, precision of dst) <- src (logical row-major complex128)
+cudaError_t launch_import(void* dst, bool dst_fp64, const double* src, const Geometry& g, cudaStream_t s);
+// dst (logical row-major complex128) <- src (storage order)
+cudaError_t launch_export(double* dst, const void* src, bool src_fp64, const Geometry& g, cudaStream_t s);
+// density |psi|^2 in logical order, and its weighted marginal along one logical axis
+cudaError_t launch_density(double* dst, const void* src, bool fp64, const Geometry& g, cudaStream_t s);
+cudaError_t launch_state_density(double* dst, const void* src, bool fp64, const Geometry& g, int axis,
+                                 const double* const* w, double* partials, cudaStream_t s);
+cudaError_t launch_copy_convert(void* dst, bool dst_fp64, const void* src, bool src_fp64, int64_t n,
+                                cudaStream_t s);
+cudaError_t launch_table_convert(void* dst, bool dst_fp64, const double* src_dev, int64_t count, cudaStream_t s);
+
+void count_launch(uint64_t k = 1);
+uint64_t launch_count();
+
+}  // namespace so

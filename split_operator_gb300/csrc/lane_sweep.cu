@@ -1,0 +1,590 @@
+// Lane-sweep pass kernel: one CTA owns a tile of complete lanes along the pass's
+// sweep axis in shared memory and runs the pass program on it.
+//
+// Replaces, fused into single passes, the reference's per-operator full-array
+// sweeps: OneDimPropagator::apply (one_dim_propagator.rs:37-46),
+// NDimPropagator::apply (n_dim_propagator.rs:32-36), FFTTransformation
+// (fft_transformation.rs:53-88), MatrixTransformation (matrix_transformation.rs:60-75),
+// NonDiagPropagator (non_diagonal_propagator.rs:29-37), StateMatrixTransformation
+// (state_matrix_transformation.rs:48-73) and the norm folds of WaveFunction::norm
+// (wave_function.rs:68-85) used by LossChecker / LeakControl.
+//
+// FFT: Stockham autosort between two shared-memory buffers (radix 8 stages for FP64,
+// radix 16 for FP32, one smaller closing stage), register butterflies, twiddles from
+// an FP64-built table, the 1/sqrt(N) of the reference folded into the last stage.
+// Lanes shorter than 16 or of non power-of-two length use a direct DFT with the same
+// table.  The lane matrix product also writes into the second buffer.
+// Norms: FP64 per-thread sums, fixed-order warp/block trees, per-CTA partials folded
+// by the last CTA in a fixed order, so results do not depend on scheduling.
+#include <cstdio>
+
+#include "common.cuh"
+
+namespace so {
+
+template <typename R>
+struct Cx;
+template <>
+struct Cx<double> {
+  using T = double2;
+};
+template <>
+struct Cx<float> {
+  using T = float2;
+};
+
+template <typename C>
+__device__ __forceinline__ C cmul(C a, C b) {
+  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <typename C>
+__device__ __forceinline__ C cadd(C a, C b) {
+  return {a.x + b.x, a.y + b.y};
+}
+template <typename C>
+__device__ __forceinline__ C csub(C a, C b) {
+  return {a.x - b.x, a.y - b.y};
+}
+// multiply by s*i (s = +1 or -1)
+template <typename C>
+__device__ __forceinline__ C mul_si(C a, int s) {
+  return s > 0 ? C{-a.y, a.x} : C{a.y, -a.x};
+}
+
+__device__ __forceinline__ int sidx(int l, int j, int ls) { return l * ls + j + (j >> 4); }
+
+// ---------------------------------------------------------------- butterflies
+template <typename C>
+__device__ __forceinline__ void dft2(C& a0, C& a1) {
+  C t = a0;
+  a0 = cadd(t, a1);
+  a1 = csub(t, a1);
+}
+
+template <typename C>
+__device__ __forceinline__ void dft4(C& a0, C& a1, C& a2, C& a3, int s) {
+  C e0 = cadd(a0, a2), e1 = csub(a0, a2);
+  C o0 = cadd(a1, a3), o1 = mul_si(csub(a1, a3), s);
+  a0 = cadd(e0, o0);
+  a2 = csub(e0, o0);
+  a1 = cadd(e1, o1);
+  a3 = csub(e1, o1);
+}
+
+template <typename C>
+__device__ __forceinline__ void dft8(C* a, int s) {
+  using R = decltype(a[0].x);
+  const R h = (R)0.70710678118654752440;
+  C e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
+  C o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
+  dft4(e0, e1, e2, e3, s);
+  dft4(o0, o1, o2, o3, s);
+  // o_q *= w8^q, w8 = e^{s 2 pi i / 8}
+  o1 = C{h * (o1.x - s * o1.y), h * (s * o1.x + o1.y)};
+  o2 = mul_si(o2, s);
+  o3 = C{h * (-o3.x - s * o3.y), h * (s * o3.x - o3.y)};
+  a[0] = cadd(e0, o0);
+  a[4] = csub(e0, o0);
+  a[1] = cadd(e1, o1);
+  a[5] = csub(e1, o1);
+  a[2] = cadd(e2, o2);
+  a[6] = csub(e2, o2);
+  a[3] = cadd(e3, o3);
+  a[7] = csub(e3, o3);
+}
+
+template <typename C>
+__device__ __forceinline__ void dft16(C* a, int s) {
+  using R = decltype(a[0].x);
+  C e[8], o[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    e[q] = a[2 * q];
+    o[q] = a[2 * q + 1];
+  }
+  dft8(e, s);
+  dft8(o, s);
+  const R c1 = (R)0.92387953251128675613, c2 = (R)0.70710678118654752440, c3 = (R)0.38268343236508977173;
+  const R cs[8] = {(R)1, c1, c2, c3, (R)0, -c3, -c2, -c1};
+  const R sn[8] = {(R)0, c3, c2, c1, (R)1, c1, c2, c3};
+#pragma unroll
+  for (int q = 1; q < 8; ++q) {
+    C w = C{cs[q], (R)s * sn[q]};
+    o[q] = cmul(o[q], w);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    a[q] = cadd(e[q], o[q]);
+    a[q + 8] = csub(e[q], o[q]);
+  }
+}
+
+template <int RS, typename C>
+__device__ __forceinline__ void dft_r(C* a, int s) {
+  if constexpr (RS == 2) {
+    dft2(a[0], a[1]);
+  } else if constexpr (RS == 4) {
+    dft4(a[0], a[1], a[2], a[3], s);
+  } else if constexpr (RS == 8) {
+    dft8(a, s);
+  } else {
+    dft16(a, s);
+  }
+}
+
+// One Stockham stage of radix RS from src to dst (ping-pong buffers): each
+// thread walks its butterflies one at a time, so it holds RS values at most.
+template <int RS, typename C>
+__device__ __forceinline__ void stockham_stage(const C* __restrict__ src, C* __restrict__ dst, int L, int n, int ls,
+                                               int p, int dir, const C* __restrict__ tw, bool last, double scale) {
+  using R = decltype(src[0].x);
+  const int nb = n / RS;
+  const int total = L * nb;
+  const R sc = (R)scale;
+  const int estride = n / (RS * p);
+  for (int b = threadIdx.x; b < total; b += blockDim.x) {
+    const int l = b / nb, i = b - l * nb;
+    const int k = i & (p - 1);
+    C reg[RS];
+#pragma unroll
+    for (int r = 0; r < RS; ++r) {
+      C x = src[sidx(l, i + r * nb, ls)];
+      if (r > 0 && k > 0) {
+        C w = __ldg(tw + r * k * estride);
+        if (dir > 0) w.y = -w.y;
+        x = cmul(x, w);
+      }
+      reg[r] = x;
+    }
+    dft_r<RS>(reg, dir);
+    const int base = (i - k) * RS + k;
+#pragma unroll
+    for (int q = 0; q < RS; ++q) {
+      C v = reg[q];
+      if (last) v = C{v.x * sc, v.y * sc};
+      dst[sidx(l, base + q * p, ls)] = v;
+    }
+  }
+  __syncthreads();
+}
+
+// Unitary DFT of every lane of the tile (radix RMAX stages, then one smaller
+// stage); the result ends in `alt`, and the two buffer pointers are swapped.
+template <int RMAX, typename C>
+__device__ void fft_stockham(C*& buf, C*& alt, const Geometry& g, int dir, const C* __restrict__ tw) {
+  const int n = (int)g.n, L = g.lanes_per_tile, ls = g.lane_stride;
+  const double scale = 1.0 / sqrt((double)n);
+  int p = 1;
+  while (p < n) {
+    const int rem = n / p;
+    if (rem >= RMAX) {
+      stockham_stage<RMAX>(buf, alt, L, n, ls, p, dir, tw, rem == RMAX, scale);
+      p *= RMAX;
+    } else if (rem == 8) {
+      stockham_stage<8>(buf, alt, L, n, ls, p, dir, tw, true, scale);
+      p *= 8;
+    } else if (rem == 4) {
+      stockham_stage<4>(buf, alt, L, n, ls, p, dir, tw, true, scale);
+      p *= 4;
+    } else {
+      stockham_stage<2>(buf, alt, L, n, ls, p, dir, tw, true, scale);
+      p *= 2;
+    }
+    C* t = buf;
+    buf = alt;
+    alt = t;
+  }
+}
+
+// Direct DFT for short or non power-of-two lanes: out_j = scale sum_k x_k w^{jk}.
+template <typename C>
+__device__ void dft_direct(C*& buf, C*& alt, const Geometry& g, int dir, const C* __restrict__ tw) {
+  using R = decltype(buf[0].x);
+  const int n = (int)g.n, L = g.lanes_per_tile, ls = g.lane_stride;
+  const int total = L * n;
+  const R sc = (R)(1.0 / sqrt((double)n));
+  for (int o = threadIdx.x; o < total; o += blockDim.x) {
+    const int l = o / n, j = o - l * n;
+    C s = C{(R)0, (R)0};
+    for (int k = 0; k < n; ++k) {
+      C w = tw[(int)(((int64_t)j * k) % n)];
+      if (dir > 0) w.y = -w.y;
+      s = cadd(s, cmul(buf[sidx(l, k, ls)], w));
+    }
+    alt[sidx(l, j, ls)] = C{s.x * sc, s.y * sc};
+  }
+  __syncthreads();
+  C* t = buf;
+  buf = alt;
+  alt = t;
+}
+
+// lane <- M lane.  Matrices are stored transposed (MT[k*n + j] = M[j][k]) so that
+// threads with consecutive j read consecutive addresses; real matrices store one
+// real per entry.  `sel` picks the matrix of a lane (-1: leave the lane as it is).
+template <typename C>
+__device__ void mat_apply(C*& buf, C*& alt, const Geometry& g, const DevOp& op, const int* lane_sel) {
+  using R = decltype(buf[0].x);
+  const int n = (int)g.n, L = g.lanes_per_tile, ls = g.lane_stride;
+  const int total = L * n;
+  const bool real = op.flags & 1;
+  for (int o = threadIdx.x; o < total; o += blockDim.x) {
+    const int l = o / n, j = o - l * n;
+    const int sel = lane_sel ? lane_sel[l] : 0;
+    C res;
+    if (sel < 0) {
+      res = buf[sidx(l, j, ls)];
+    } else if (real) {
+      const R* mt = reinterpret_cast<const R*>(op.ptr) + (int64_t)sel * n * n;
+      R sr = 0, si = 0;
+      for (int k = 0; k < n; ++k) {
+        const R m = __ldg(mt + (int64_t)k * n + j);
+        const C x = buf[sidx(l, k, ls)];
+        sr += m * x.x;
+        si += m * x.y;
+      }
+      res = C{sr, si};
+    } else {
+      const C* mt = reinterpret_cast<const C*>(op.ptr) + (int64_t)sel * n * n;
+      C s = C{(R)0, (R)0};
+      for (int k = 0; k < n; ++k) {
+        const C m = mt[(int64_t)k * n + j];
+        s = cadd(s, cmul(m, buf[sidx(l, k, ls)]));
+      }
+      res = s;
+    }
+    alt[sidx(l, j, ls)] = res;
+  }
+  __syncthreads();
+  C* t = buf;
+  buf = alt;
+  alt = t;
+}
+
+// Fixed-order block sum of one double per thread; result valid in thread 0.
+__device__ double block_sum(double v, double* scratch) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) scratch[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int i = 0; i < nw; ++i) r += scratch[i];
+  }
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double ld_slot(const double* s, int i) { return __ldcg(s + i); }
+
+// scalar bookkeeping of one op, run by a single thread
+__device__ void run_scalar(const PassParams& p, const DevOp& op, const double* totals) {
+  double* s = p.slots;
+  switch (op.kind) {
+    case OP_NORM: {
+      const double v = totals[op.red];
+      s[op.a] = v;
+      if (!isfinite(v) && p.nonfinite_slot >= 0) s[p.nonfinite_slot] = 1.0;
+      break;
+    }
+    case OP_DOT:
+      s[op.a] = totals[op.red];
+      s[op.b] = totals[op.red + 1];
+      break;
+    case OP_COPY:
+      s[op.a] = s[op.b];
+      break;
+    case OP_LOSS:
+      s[op.a] += s[op.b] - s[op.c];
+      break;
+    case OP_SETC:
+      s[op.a] = op.value;
+      break;
+    case OP_RECORD:
+      if (p.record) p.record[op.count] = s[op.a];
+      break;
+    default:
+      break;
+  }
+}
+
+template <typename R, int RMAX>
+__global__ void __launch_bounds__(512) pass_kernel(const __grid_constant__ PassParams p) {
+  using C = typename Cx<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Geometry& g = p.g;
+  const int L = g.lanes_per_tile, n = (int)g.n, ls = g.lane_stride;
+  const int T = blockDim.x, tid = threadIdx.x;
+  const size_t tile_bytes = ((size_t)L * ls * sizeof(C) + 15) & ~(size_t)15;
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  C* alt = reinterpret_cast<C*>(smem_raw + tile_bytes);
+  size_t off = 2 * tile_bytes;
+  int64_t* lane_base = reinterpret_cast<int64_t*>(smem_raw + off);
+  off += (size_t)L * sizeof(int64_t);
+  double* lane_w = reinterpret_cast<double*>(smem_raw + off);
+  off += (size_t)L * sizeof(double);
+  int* lane_coord = reinterpret_cast<int*>(smem_raw + off);
+  off += (size_t)L * kMaxDims * sizeof(int);
+  int* lane_sel = reinterpret_cast<int*>(smem_raw + off);
+  off += (size_t)L * sizeof(int);
+  __shared__ double scratch[32];
+  __shared__ double blk_red[kMaxRed];
+  __shared__ double totals[kMaxRed];
+  __shared__ int s_last;
+
+  const int64_t tile = blockIdx.x;
+  const bool pow2 = (n & (n - 1)) == 0;
+  const int lg = pow2 ? __ffs(n) - 1 : 0;
+
+  // lane metadata
+  for (int l = tid; l < L; l += T) {
+    int64_t o, i;
+    bool valid;
+    if (g.inner == 1) {
+      o = tile * L + l;
+      i = 0;
+      valid = o < g.outer;
+    } else {
+      o = tile / g.tiles_per_outer;
+      i = (tile - o * g.tiles_per_outer) * L + l;
+      valid = (o < g.outer) && (i < g.inner);
+    }
+    lane_base[l] = valid ? o * g.n * g.inner + i : -1;
+    int64_t ro = valid ? o : 0, ri = valid ? i : 0;
+    for (int q = g.ndim - 1; q > g.spos; --q) {
+      lane_coord[l * kMaxDims + g.perm[q]] = (int)(ri % g.sshape[q]);
+      ri /= g.sshape[q];
+    }
+    for (int q = g.spos - 1; q >= 0; --q) {
+      lane_coord[l * kMaxDims + g.perm[q]] = (int)(ro % g.sshape[q]);
+      ro /= g.sshape[q];
+    }
+    lane_coord[l * kMaxDims + g.sweep_axis] = 0;
+  }
+  __syncthreads();
+
+  auto split = [&](int pt, int& l, int& x) {
+    if (g.inner == 1) {
+      l = pow2 ? (pt >> lg) : pt / n;
+      x = pt - l * n;
+    } else {
+      x = pt / L;
+      l = pt - x * L;
+    }
+  };
+
+  C* psi = reinterpret_cast<C*>(p.psi);
+  const int total = L * n;
+  for (int pt = tid; pt < total; pt += T) {
+    int l, x;
+    split(pt, l, x);
+    const int64_t b = lane_base[l];
+    buf[sidx(l, x, ls)] = b >= 0 ? psi[b + (int64_t)x * g.inner] : C{(R)0, (R)0};
+  }
+  __syncthreads();
+
+  const C* tw = reinterpret_cast<const C*>(p.twiddle);
+  for (int rep = 0; rep < p.repeat; ++rep) {
+    for (int oi = 0; oi < p.nops; ++oi) {
+      const DevOp& op = p.ops[oi];
+      switch (op.kind) {
+        case OP_DIAG1D: {
+          const C* t = reinterpret_cast<const C*>(op.ptr);
+          const bool along = op.axis == g.sweep_axis;
+          for (int pt = tid; pt < total; pt += T) {
+            const int l = pow2 ? (pt >> lg) : pt / n, x = pt - l * n;
+            const int k = along ? x : lane_coord[l * kMaxDims + op.axis];
+            const int si = sidx(l, x, ls);
+            buf[si] = cmul(buf[si], __ldg(reinterpret_cast<const typename Cx<R>::T*>(t) + k));
+          }
+          __syncthreads();
+          break;
+        }
+        case OP_DIAGND: {
+          const C* t = reinterpret_cast<const C*>(op.ptr);
+          for (int pt = tid; pt < total; pt += T) {
+            int l, x;
+            split(pt, l, x);
+            const int64_t b = lane_base[l];
+            if (b >= 0) {
+              const int si = sidx(l, x, ls);
+              buf[si] = cmul(buf[si], t[b + (int64_t)x * g.inner]);
+            }
+          }
+          __syncthreads();
+          break;
+        }
+        case OP_SCALE: {
+          const double f = sqrt(ld_slot(p.slots, op.b) / ld_slot(p.slots, op.c));
+          const R fr = (R)f;
+          for (int pt = tid; pt < total; pt += T) {
+            const int l = pow2 ? (pt >> lg) : pt / n, x = pt - l * n;
+            const int si = sidx(l, x, ls);
+            buf[si] = C{buf[si].x * fr, buf[si].y * fr};
+          }
+          __syncthreads();
+          break;
+        }
+        case OP_FFT:
+          if (pow2 && n >= 16)
+            fft_stockham<RMAX>(buf, alt, g, op.dir, tw);
+          else
+            dft_direct(buf, alt, g, op.dir, tw);
+          break;
+        case OP_MAT:
+          mat_apply(buf, alt, g, op, nullptr);
+          break;
+        case OP_MAT_LANE:
+        case OP_MAT_SLICE: {
+          for (int l = tid; l < L; l += T) {
+            int64_t idx;
+            if (op.kind == OP_MAT_SLICE) {
+              idx = lane_coord[l * kMaxDims + op.axis];
+            } else {
+              // ndarray lanes_mut order: row-major over the logical axes other than the sweep axis
+              idx = 0;
+              for (int a = 0; a < g.ndim; ++a) {
+                if (a == g.sweep_axis) continue;
+                int64_t ext = 0;
+                for (int q = 0; q < g.ndim; ++q)
+                  if (g.perm[q] == a) ext = g.sshape[q];
+                idx = idx * ext + lane_coord[l * kMaxDims + a];
+              }
+            }
+            lane_sel[l] = (lane_base[l] >= 0 && idx < op.count) ? (int)idx : -1;
+          }
+          __syncthreads();
+          mat_apply(buf, alt, g, op, lane_sel);
+          break;
+        }
+        case OP_NORM:
+        case OP_DOT: {
+          for (int l = tid; l < L; l += T) {
+            double w = 1.0;
+            if (lane_base[l] < 0) {
+              w = 0.0;
+            } else {
+              for (int a = 0; a < g.ndim; ++a)
+                if (a != g.sweep_axis) w *= op.w[a][lane_coord[l * kMaxDims + a]];
+            }
+            lane_w[l] = w;
+          }
+          __syncthreads();
+          const double* wx = op.w[g.sweep_axis];
+          double acc = 0.0, acc_i = 0.0;
+          const C* other = reinterpret_cast<const C*>(op.ptr);
+          for (int pt = tid; pt < total; pt += T) {
+            int l, x;
+            split(pt, l, x);
+            const C v = buf[sidx(l, x, ls)];
+            const double w = lane_w[l] * __ldg(wx + x);
+            if (op.kind == OP_NORM) {
+              acc += ((double)v.x * (double)v.x + (double)v.y * (double)v.y) * w;
+            } else if (lane_base[l] >= 0) {
+              const C o = other[lane_base[l] + (int64_t)x * g.inner];
+              // v * conj(o)
+              acc += ((double)v.x * (double)o.x + (double)v.y * (double)o.y) * w;
+              acc_i += ((double)v.y * (double)o.x - (double)v.x * (double)o.y) * w;
+            }
+          }
+          const double tsum = block_sum(acc, scratch);
+          double tsum_i = 0.0;
+          if (op.kind == OP_DOT) tsum_i = block_sum(acc_i, scratch);
+          if (tid == 0) {
+            if (p.resident) {
+              totals[op.red] = tsum;
+              if (op.kind == OP_DOT) totals[op.red + 1] = tsum_i;
+              run_scalar(p, op, totals);
+            } else {
+              blk_red[op.red] = tsum;
+              if (op.kind == OP_DOT) blk_red[op.red + 1] = tsum_i;
+            }
+          }
+          __syncthreads();
+          break;
+        }
+        default:  // COPY / LOSS / SETC / RECORD
+          if (p.resident) {
+            if (tid == 0) run_scalar(p, op, totals);
+            __syncthreads();
+          }
+          break;
+      }
+    }
+  }
+
+  for (int pt = tid; pt < total; pt += T) {
+    int l, x;
+    split(pt, l, x);
+    const int64_t b = lane_base[l];
+    if (b >= 0) psi[b + (int64_t)x * g.inner] = buf[sidx(l, x, ls)];
+  }
+  if (p.resident) return;
+
+  // ---- deterministic finalize by the last CTA
+  if (p.nred == 0 && p.nops == 0) return;
+  __syncthreads();
+  if (tid == 0) {
+    for (int r = 0; r < p.nred; ++r) p.partials[(int64_t)r * g.tiles + tile] = blk_red[r];
+    __threadfence();
+    const unsigned int ticket = atomicAdd(p.counter, 1u);
+    s_last = ticket == (unsigned int)(g.tiles - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int w = tid >> 5, lane = tid & 31;
+  for (int r = w; r < p.nred; r += (T >> 5)) {
+    double v = 0.0;
+    for (int64_t b = lane; b < g.tiles; b += 32) v += __ldcg(p.partials + (int64_t)r * g.tiles + b);
+#pragma unroll
+    for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_down_sync(0xffffffffu, v, o2);
+    if (lane == 0) totals[r] = v;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int oi = 0; oi < p.nops; ++oi) run_scalar(p, p.ops[oi], totals);
+    __threadfence();
+    *p.counter = 0u;
+  }
+}
+
+size_t pass_smem_bytes(const Geometry& g, bool fp64) {
+  const size_t cs = fp64 ? 16 : 8;
+  size_t b = 2 * (((size_t)g.lanes_per_tile * g.lane_stride * cs + 15) & ~(size_t)15);
+  b += (size_t)g.lanes_per_tile * (sizeof(int64_t) + sizeof(double) + kMaxDims * sizeof(int) + sizeof(int));
+  return b;
+}
+
+int pass_threads(const Geometry& g) {
+  const int64_t pts = (int64_t)g.lanes_per_tile * g.n;
+  int64_t t = (pts + g.vals - 1) / g.vals;
+  t = ((t + 31) / 32) * 32;
+  if (t < 32) t = 32;
+  if (t > 512) t = 512;
+  return (int)t;
+}
+
+template <typename R, int RMAX>
+static cudaError_t launch_impl(const PassParams& p, cudaStream_t s) {
+  const size_t smem = pass_smem_bytes(p.g, sizeof(R) == 8);
+  auto kern = pass_kernel<R, RMAX>;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  const int threads = pass_threads(p.g);
+  kern<<<(unsigned)p.g.tiles, threads, smem, s>>>(p);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s) { return launch_impl<double, 8>(p, s); }
+cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s) { return launch_impl<float, 16>(p, s); }
+
+}  // namespace so

@@ -1,0 +1,1132 @@
+// Engine (device state + pass builder) and the host logic of the operators,
+// written to follow the Rust crate's control flow operator by operator so the
+// norm cache, loss bookkeeping and representation swaps happen exactly where
+// the reference does them; every array touch becomes an emitted device op.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "model.hpp"
+
+namespace so {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw Error(SO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DeviceBuffer::DeviceBuffer(size_t b) : bytes(b) {
+  if (b) cuda_check(cudaMalloc(&ptr, b), "cudaMalloc");
+}
+DeviceBuffer& DeviceBuffer::operator=(DeviceBuffer&& o) noexcept {
+  if (this != &o) {
+    if (ptr) cudaFree(ptr);
+    ptr = o.ptr;
+    bytes = o.bytes;
+    o.ptr = nullptr;
+    o.bytes = 0;
+  }
+  return *this;
+}
+DeviceBuffer::~DeviceBuffer() {
+  if (ptr) cudaFree(ptr);
+}
+
+// ------------------------------------------------------------------ ScalarState
+ScalarState::~ScalarState() {
+  if (home) {
+    auto& v = home->bound;
+    v.erase(std::remove(v.begin(), v.end(), this), v.end());
+    for (int s : slots) home->free_slot(s);
+  }
+}
+
+const std::vector<int>& ScalarState::bind(Engine* e) {
+  if (home == e) return slots;
+  if (home) unbind();
+  slots.clear();
+  for (double v : host) slots.push_back(e->alloc_slot(v));
+  home = e;
+  e->bound.push_back(this);
+  return slots;
+}
+
+void ScalarState::unbind() {
+  if (!home) return;
+  for (size_t i = 0; i < slots.size(); ++i) host[i] = home->read_slot(slots[i]);
+  for (int s : slots) home->free_slot(s);
+  auto& v = home->bound;
+  v.erase(std::remove(v.begin(), v.end(), this), v.end());
+  home = nullptr;
+  slots.clear();
+}
+
+double ScalarState::get(size_t i) { return home ? home->read_slot(slots[i]) : host[i]; }
+
+void ScalarState::set(size_t i, double v) {
+  if (home)
+    home->write_slot(slots[i], v);
+  else
+    host[i] = v;
+}
+
+// ----------------------------------------------------------------------- Engine
+static bool is_scalar_kind(int k) { return k == OP_COPY || k == OP_LOSS || k == OP_SETC || k == OP_RECORD; }
+
+Engine::Engine(const std::vector<size_t>& shp, const std::vector<int>& prm, bool f64)
+    : fp64(f64), shape(shp), perm(prm) {
+  if (shape.empty() || shape.size() > (size_t)kMaxDims)
+    throw Error(SO_ERR_UNSUPPORTED, "wave functions of 1 to 4 dimensions are supported");
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+    cudaGetLastError();
+    throw Error(SO_ERR_CUDA, "no CUDA device available");
+  }
+  psi = DeviceBuffer(points() * elem_bytes());
+  slots_ = DeviceBuffer(kNumSlots * sizeof(double));
+  cuda_check(cudaMemset(slots_.ptr, 0, kNumSlots * sizeof(double)), "cudaMemset");
+  counter_ = DeviceBuffer(sizeof(unsigned int) * 4);
+  cuda_check(cudaMemset(counter_.ptr, 0, sizeof(unsigned int) * 4), "cudaMemset");
+  nonfinite_slot = alloc_slot(0.0);
+  int64_t max_tiles = 1;
+  for (size_t a = 0; a < shape.size(); ++a) {
+    try {
+      Geometry g = geometry((int)a, false);
+      max_tiles = std::max<int64_t>(max_tiles, g.tiles);
+    } catch (const Error&) {
+    }
+  }
+  partials_cap_ = (size_t)max_tiles;
+  partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
+}
+
+Engine::~Engine() {
+  try {
+    std::vector<ScalarState*> b = bound;
+    for (ScalarState* s : b) s->unbind();
+    if (stream) cudaStreamSynchronize(stream);
+    else cudaDeviceSynchronize();
+  } catch (...) {
+  }
+}
+
+size_t Engine::points() const {
+  size_t p = 1;
+  for (size_t s : shape) p *= s;
+  return p;
+}
+
+bool Engine::resident_capable() const {
+  const size_t tile_max = fp64 ? 4096 : 8192;
+  return shape.size() == 1 && points() <= tile_max && points() >= 2;
+}
+
+static int64_t pow2_floor(int64_t v) {
+  int64_t p = 1;
+  while (p * 2 <= v) p *= 2;
+  return p;
+}
+
+Geometry Engine::geometry(int sweep_axis, bool resident) const {
+  Geometry g{};
+  const int nd = (int)shape.size();
+  g.ndim = nd;
+  g.spos = -1;
+  for (int q = 0; q < nd; ++q) {
+    g.perm[q] = perm[q];
+    g.sshape[q] = (int64_t)shape[perm[q]];
+    if (perm[q] == sweep_axis) g.spos = q;
+  }
+  if (g.spos < 0) throw Error(SO_ERR_INVALID, "sweep axis out of range");
+  g.sweep_axis = sweep_axis;
+  g.n = g.sshape[g.spos];
+  g.inner = 1;
+  for (int q = g.spos + 1; q < nd; ++q) g.inner *= g.sshape[q];
+  g.outer = 1;
+  for (int q = 0; q < g.spos; ++q) g.outer *= g.sshape[q];
+  // two tile buffers of at most ~139 KB together
+  const int64_t tile_max = fp64 ? 4096 : 8192;
+  g.vals = 8;
+  if (g.n > tile_max)
+    throw Error(SO_ERR_UNSUPPORTED, "lanes longer than " + std::to_string(tile_max) + " points are not supported");
+  int64_t L;
+  if (resident) {
+    if (g.inner == 1)
+      L = g.outer;
+    else if (g.outer == 1)
+      L = g.inner;
+    else
+      throw Error(SO_ERR_UNSUPPORTED, "resident pass needs a single lane family");
+    if (L * g.n > tile_max) throw Error(SO_ERR_UNSUPPORTED, "array too large for a resident pass");
+    g.tiles_per_outer = 1;
+    g.tiles = 1;
+  } else if (g.inner == 1) {
+    const int64_t lmax = std::max<int64_t>(1, pow2_floor(tile_max / g.n));
+    int64_t want = pow2_floor(std::max<int64_t>(1, g.outer / 304));
+    want = std::max<int64_t>(want, pow2_floor(std::max<int64_t>(1, 1024 / g.n)));
+    L = std::min(want, lmax);
+    g.tiles_per_outer = 1;
+    g.tiles = (g.outer + L - 1) / L;
+  } else {
+    const int64_t lmax = std::max<int64_t>(1, pow2_floor(tile_max / g.n));
+    L = std::min<int64_t>({lmax, fp64 ? 16 : 32, pow2_floor(g.inner)});
+    while (L > 4 && g.outer * ((g.inner + L - 1) / L) < 304) L /= 2;
+    g.tiles_per_outer = (int32_t)((g.inner + L - 1) / L);
+    g.tiles = g.outer * g.tiles_per_outer;
+  }
+  g.lanes_per_tile = (int32_t)L;
+  int64_t ls = g.n + (g.n >> 4);
+  if (ls % 2 == 0) ls += 1;
+  g.lane_stride = (int32_t)ls;
+  return g;
+}
+
+int Engine::alloc_slot(double init) {
+  int s;
+  if (!free_slots_.empty()) {
+    s = free_slots_.back();
+    free_slots_.pop_back();
+  } else {
+    if (next_slot_ >= kNumSlots) throw Error(SO_ERR_UNSUPPORTED, "out of device scalar slots");
+    s = next_slot_++;
+  }
+  write_slot(s, init);
+  return s;
+}
+
+void Engine::free_slot(int s) { free_slots_.push_back(s); }
+
+void Engine::write_slot(int s, double v) {
+  flush();
+  cuda_check(cudaMemcpyAsync(slots() + s, &v, sizeof(double), cudaMemcpyHostToDevice, stream), "slot write");
+}
+
+double Engine::read_slot(int s) {
+  flush();
+  double v = 0.0;
+  cuda_check(cudaMemcpyAsync(&v, slots() + s, sizeof(double), cudaMemcpyDeviceToHost, stream), "slot read");
+  cuda_check(cudaStreamSynchronize(stream), "stream sync");
+  return v;
+}
+
+template <typename T>
+static void upload(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) {
+  const size_t b = v.size() * sizeof(T);
+  if (buf.bytes != b) buf = DeviceBuffer(b);
+  cuda_check(cudaMemcpyAsync(buf.ptr, v.data(), b, cudaMemcpyHostToDevice, s), "table upload");
+  cuda_check(cudaStreamSynchronize(s), "table upload sync");
+}
+
+static void upload_complex(DeviceBuffer& buf, const std::vector<cplx>& t, bool fp64, cudaStream_t s) {
+  if (fp64) {
+    std::vector<double> v(2 * t.size());
+    for (size_t i = 0; i < t.size(); ++i) {
+      v[2 * i] = t[i].real();
+      v[2 * i + 1] = t[i].imag();
+    }
+    upload(buf, v, s);
+  } else {
+    std::vector<float> v(2 * t.size());
+    for (size_t i = 0; i < t.size(); ++i) {
+      v[2 * i] = (float)t[i].real();
+      v[2 * i + 1] = (float)t[i].imag();
+    }
+    upload(buf, v, s);
+  }
+}
+
+const void* Engine::table_1d(const void* key, uint64_t version, const std::vector<cplx>& t) {
+  auto& c = tables_[{key, 0}];
+  if (c.buf.ptr && c.version == version) return c.buf.ptr;
+  flush();
+  upload_complex(c.buf, t, fp64, stream);
+  c.version = version;
+  return c.buf.ptr;
+}
+
+const void* Engine::table_nd(const void* key, uint64_t version, const std::vector<cplx>& t) {
+  auto& c = tables_[{key, 1}];
+  if (c.buf.ptr && c.version == version) return c.buf.ptr;
+  flush();
+  // logical row-major -> storage order
+  const int nd = (int)shape.size();
+  std::vector<cplx> st(t.size());
+  std::vector<size_t> lstride(nd);
+  size_t acc = 1;
+  for (int a = nd - 1; a >= 0; --a) {
+    lstride[a] = acc;
+    acc *= shape[a];
+  }
+  std::vector<size_t> idx(nd, 0);
+  for (size_t s = 0; s < t.size(); ++s) {
+    size_t li = 0, r = s;
+    for (int q = nd - 1; q >= 0; --q) {
+      const size_t ext = shape[perm[q]];
+      li += (r % ext) * lstride[perm[q]];
+      r /= ext;
+    }
+    st[s] = t[li];
+  }
+  upload_complex(c.buf, st, fp64, stream);
+  c.version = version;
+  return c.buf.ptr;
+}
+
+const void* Engine::matrices(const void* key, uint64_t version, const std::vector<cplx>& m, size_t n, size_t count,
+                             bool& real) {
+  auto& c = tables_[{key, 2}];
+  if (c.buf.ptr && c.version == version) {
+    real = c.real;
+    return c.buf.ptr;
+  }
+  flush();
+  real = std::all_of(m.begin(), m.end(), [](const cplx& v) { return v.imag() == 0.0; });
+  std::vector<cplx> mt(m.size());
+  for (size_t b = 0; b < count; ++b)
+    for (size_t j = 0; j < n; ++j)
+      for (size_t k = 0; k < n; ++k) mt[b * n * n + k * n + j] = m[b * n * n + j * n + k];
+  if (real) {
+    if (fp64) {
+      std::vector<double> v(mt.size());
+      for (size_t i = 0; i < mt.size(); ++i) v[i] = mt[i].real();
+      upload(c.buf, v, stream);
+    } else {
+      std::vector<float> v(mt.size());
+      for (size_t i = 0; i < mt.size(); ++i) v[i] = (float)mt[i].real();
+      upload(c.buf, v, stream);
+    }
+  } else {
+    upload_complex(c.buf, mt, fp64, stream);
+  }
+  c.version = version;
+  c.real = real;
+  return c.buf.ptr;
+}
+
+const double* Engine::weights(const Grid& g) {
+  auto it = weights_.find(g.uid);
+  if (it != weights_.end()) return it->second.as<double>();
+  flush();
+  DeviceBuffer b;
+  upload(b, g.weights, stream);
+  const double* p = b.as<double>();
+  weights_.emplace(g.uid, std::move(b));
+  return p;
+}
+
+const void* Engine::twiddle(size_t n) {
+  auto it = twiddles_.find(n);
+  if (it != twiddles_.end()) return it->second.ptr;
+  DeviceBuffer b;
+  upload_complex(b, twiddles(n), fp64, stream);
+  const void* p = b.ptr;
+  twiddles_.emplace(n, std::move(b));
+  return p;
+}
+
+void Engine::submit(const Action& a) {
+  const int k = a.op.kind;
+  if (a.lane_axis >= 0 && cur_axis_ >= 0 && cur_axis_ != a.lane_axis) flush();
+  if (k == OP_SCALE) {
+    for (int w : cur_written_)
+      if (w == a.op.b || w == a.op.c) {
+        flush();
+        break;
+      }
+  }
+  const int need = k == OP_NORM ? 1 : (k == OP_DOT ? 2 : 0);
+  if ((int)cur_.size() >= kMaxOps || cur_red_ + need > kMaxRed) flush();
+  if (a.lane_axis >= 0) cur_axis_ = a.lane_axis;
+  DevOp op = a.op;
+  if (need) {
+    op.red = cur_red_;
+    cur_red_ += need;
+  }
+  if (k == OP_NORM || k == OP_COPY || k == OP_LOSS || k == OP_SETC) cur_written_.push_back(op.a);
+  if (k == OP_DOT) {
+    cur_written_.push_back(op.a);
+    cur_written_.push_back(op.b);
+  }
+  cur_.push_back(op);
+}
+
+void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int repeat) {
+  PassParams p{};
+  p.g = geometry(axis, resident);
+  p.psi = psi.ptr;
+  p.slots = slots();
+  p.partials = partials_.as<double>();
+  p.counter = counter_.as<unsigned int>();
+  p.record = record_dev;
+  p.nops = (int)ops.size();
+  p.repeat = repeat;
+  p.resident = resident ? 1 : 0;
+  p.nonfinite_slot = nonfinite_slot;
+  int nred = 0;
+  bool fft = false;
+  for (size_t i = 0; i < ops.size(); ++i) {
+    p.ops[i] = ops[i];
+    if (ops[i].kind == OP_NORM) nred = std::max(nred, ops[i].red + 1);
+    if (ops[i].kind == OP_DOT) nred = std::max(nred, ops[i].red + 2);
+    if (ops[i].kind == OP_FFT) fft = true;
+  }
+  p.nred = nred;
+  if (fft) p.twiddle = twiddle((size_t)p.g.n);
+  if (!resident && (size_t)p.g.tiles > partials_cap_) {
+    partials_cap_ = (size_t)p.g.tiles;
+    partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
+    p.partials = partials_.as<double>();
+  }
+  cuda_check(fp64 ? launch_pass_f64(p, stream) : launch_pass_f32(p, stream), "pass launch");
+}
+
+void Engine::flush() {
+  if (cur_.empty()) return;
+  std::vector<DevOp> ops;
+  ops.swap(cur_);
+  const int axis = cur_axis_ >= 0 ? cur_axis_ : perm.back();
+  cur_axis_ = -1;
+  cur_red_ = 0;
+  cur_written_.clear();
+  const bool array = std::any_of(ops.begin(), ops.end(), [](const DevOp& o) { return !is_scalar_kind(o.kind); });
+  if (!array) {
+    PassParams p{};
+    p.slots = slots();
+    p.record = record_dev;
+    p.nops = (int)ops.size();
+    for (size_t i = 0; i < ops.size(); ++i) p.ops[i] = ops[i];
+    cuda_check(launch_scalar_program(p, stream), "scalar launch");
+    return;
+  }
+  launch(ops, axis, false, 1);
+}
+
+void Engine::run_resident(const std::vector<Action>& prog, int repeat) {
+  flush();
+  if (prog.empty() || repeat <= 0) return;
+  std::vector<DevOp> ops;
+  int red = 0;
+  for (const Action& a : prog) {
+    DevOp op = a.op;
+    if (op.kind == OP_NORM || op.kind == OP_DOT) op.red = 0;
+    ops.push_back(op);
+    (void)red;
+  }
+  const int axis = perm.back();
+  if ((int)ops.size() <= kMaxOps) {
+    launch(ops, axis, true, repeat);
+    return;
+  }
+  for (int r = 0; r < repeat; ++r)
+    for (size_t s = 0; s < ops.size(); s += kMaxOps) {
+      std::vector<DevOp> chunk(ops.begin() + s, ops.begin() + std::min(ops.size(), s + (size_t)kMaxOps));
+      launch(chunk, axis, true, 1);
+    }
+}
+
+void Engine::sync() {
+  flush();
+  cuda_check(cudaStreamSynchronize(stream), "stream sync");
+}
+
+void Engine::check_nonfinite() {
+  if (read_slot(nonfinite_slot) != 0.0) {
+    write_slot(nonfinite_slot, 0.0);
+    throw Error(SO_ERR_NONFINITE, "a norm of the wave function is not finite");
+  }
+}
+
+static Geometry flat_geometry(const Engine& e) {
+  Geometry g{};
+  g.ndim = (int)e.shape.size();
+  for (int q = 0; q < g.ndim; ++q) {
+    g.perm[q] = e.perm[q];
+    g.sshape[q] = (int64_t)e.shape[e.perm[q]];
+  }
+  return g;
+}
+
+static bool identity_perm(const std::vector<int>& p) {
+  for (size_t i = 0; i < p.size(); ++i)
+    if (p[i] != (int)i) return false;
+  return true;
+}
+
+void Engine::import_host(const double* host) {
+  flush();
+  const size_t b = points() * 16;
+  if (fp64 && identity_perm(perm)) {
+    cuda_check(cudaMemcpyAsync(psi.ptr, host, b, cudaMemcpyHostToDevice, stream), "import copy");
+    return;
+  }
+  if (staging_.bytes < b) staging_ = DeviceBuffer(b);
+  cuda_check(cudaMemcpyAsync(staging_.ptr, host, b, cudaMemcpyHostToDevice, stream), "import copy");
+  cuda_check(launch_import(psi.ptr, fp64, staging_.as<double>(), flat_geometry(*this), stream), "import");
+}
+
+void Engine::export_host(double* host) {
+  flush();
+  const size_t b = points() * 16;
+  if (fp64 && identity_perm(perm)) {
+    cuda_check(cudaMemcpyAsync(host, psi.ptr, b, cudaMemcpyDeviceToHost, stream), "export copy");
+  } else {
+    if (staging_.bytes < b) staging_ = DeviceBuffer(b);
+    cuda_check(launch_export(staging_.as<double>(), psi.ptr, fp64, flat_geometry(*this), stream), "export");
+    cuda_check(cudaMemcpyAsync(host, staging_.ptr, b, cudaMemcpyDeviceToHost, stream), "export copy");
+  }
+  cuda_check(cudaStreamSynchronize(stream), "export sync");
+}
+
+// ----------------------------------------------------------------- WaveFunction
+WaveFunction::WaveFunction(const std::vector<size_t>& shp, const std::vector<Grid>& g, const std::vector<int>& perm,
+                           bool fp64)
+    : shape(shp), grids(g) {
+  if (grids.size() != shape.size()) throw Error(SO_ERR_SHAPE, "one grid per axis is required");
+  for (size_t a = 0; a < shape.size(); ++a)
+    if (grids[a].size() != shape[a]) throw Error(SO_ERR_SHAPE, "grid size differs from the array axis");
+  for (const Grid& gr : grids) last_grid_names.push_back(gr.name);
+  eng = std::make_unique<Engine>(shape, perm, fp64);
+  cache_slot = eng->alloc_slot(1.0);
+}
+
+size_t WaveFunction::points() const { return eng->points(); }
+
+std::vector<const double*> WaveFunction::weight_ptrs() {
+  std::vector<const double*> w;
+  for (const Grid& g : grids) w.push_back(eng->weights(g));
+  return w;
+}
+
+void Emitter::host(std::function<void()> f) {
+  if (rec) {
+    Action a{};
+    a.host_call = (int)calls->size();
+    calls->push_back(std::move(f));
+    rec->push_back(a);
+  } else {
+    eng->flush();
+    f();
+  }
+}
+
+int norm_slot(WaveFunction& wf, Emitter& em) {
+  if (!wf.possible_norm_change) return wf.cache_slot;
+  bool changed = false;
+  for (size_t a = 0; a < wf.grids.size(); ++a)
+    if (wf.last_grid_names[a] != wf.grids[a].name) changed = true;
+  if (changed)
+    for (size_t a = 0; a < wf.grids.size(); ++a) wf.last_grid_names[a] = wf.grids[a].name;
+  Action act{};
+  act.op.kind = OP_NORM;
+  act.op.a = wf.cache_slot;
+  std::vector<const double*> w = wf.weight_ptrs();
+  for (size_t a = 0; a < w.size(); ++a) act.op.w[a] = w[a];
+  em.emit(act);
+  wf.possible_norm_change = false;
+  return wf.cache_slot;
+}
+
+void normalize_to_slot(WaveFunction& wf, Emitter& em, int target) {
+  const int n = norm_slot(wf, em);
+  Action s{};
+  s.op.kind = OP_SCALE;
+  s.op.b = target;
+  s.op.c = n;
+  em.emit(s);
+  if (target != wf.cache_slot) {
+    Action c{};
+    c.op.kind = OP_COPY;
+    c.op.a = wf.cache_slot;
+    c.op.b = target;
+    em.emit(c);
+  }
+  wf.possible_norm_change = false;
+}
+
+static Action scalar_action(int kind, int a, int b = 0, int c = 0, double value = 0.0) {
+  Action act{};
+  act.op.kind = kind;
+  act.op.a = a;
+  act.op.b = b;
+  act.op.c = c;
+  act.op.value = value;
+  return act;
+}
+
+// -------------------------------------------------------------------- LossChecker
+void LossChecker::check_before(WaveFunction& wf, Emitter& em) {
+  const int n = norm_slot(wf, em);
+  const auto& s = st.bind(wf.eng.get());
+  em.emit(scalar_action(OP_COPY, s[1], n));
+}
+
+void LossChecker::check_after(WaveFunction& wf, Emitter& em) {
+  const int n = norm_slot(wf, em);
+  const auto& s = st.bind(wf.eng.get());
+  em.emit(scalar_action(OP_LOSS, s[0], s[1], n));
+  em.emit(scalar_action(OP_COPY, s[1], n));
+}
+
+void LossChecker::reset(Emitter* em) {
+  if (em && st.home == em->eng)
+    em->emit(scalar_action(OP_SETC, st.slots[0], 0, 0, 0.0));
+  else
+    st.set(0, 0.0);
+}
+
+// -------------------------------------------------------------------- propagators
+void OneDimPropagator::apply_unchecked(WaveFunction& wf, Emitter& em) {
+  if (dimension_no >= wf.shape.size() || op.size() != wf.shape[dimension_no])
+    throw Error(SO_ERR_SHAPE, "one-dimensional operator does not match the wave function axis");
+  wf.possible_norm_change = true;
+  Action a{};
+  a.op.kind = OP_DIAG1D;
+  a.op.axis = (int)dimension_no;
+  a.op.ptr = wf.eng->table_1d(this, version, op);
+  em.emit(a);
+}
+
+void OneDimPropagator::apply(WaveFunction& wf, Emitter& em) {
+  if (lc) lc->check_before(wf, em);
+  apply_unchecked(wf, em);
+  if (lc) lc->check_after(wf, em);
+}
+
+void NDimPropagator::apply(WaveFunction& wf, Emitter& em) {
+  if (shape != wf.shape) throw Error(SO_ERR_SHAPE, "n-dimensional operator shape differs from the wave function");
+  if (lc) lc->check_before(wf, em);
+  wf.possible_norm_change = true;
+  Action a{};
+  a.op.kind = OP_DIAGND;
+  a.op.ptr = wf.eng->table_nd(this, version, op);
+  em.emit(a);
+  if (lc) lc->check_after(wf, em);
+}
+
+void NonDiagPropagator::apply(WaveFunction& wf, Emitter& em) {
+  if (dimension_no >= wf.shape.size() || n != wf.shape[dimension_no])
+    throw Error(SO_ERR_SHAPE, "non-diagonal operator size differs from the wave function axis");
+  if (lc) lc->check_before(wf, em);
+  wf.possible_norm_change = true;
+  Action a{};
+  bool real = false;
+  a.op.kind = OP_MAT_LANE;
+  a.op.ptr = wf.eng->matrices(this, version, ops, n, count, real);
+  a.op.flags = real ? 1 : 0;
+  a.op.count = (int64_t)count;
+  a.lane_axis = (int)dimension_no;
+  em.emit(a);
+  if (lc) lc->check_after(wf, em);
+}
+
+// ---------------------------------------------------------------- transformations
+FFTTransformation::FFTTransformation(const Grid& g, const std::string& name)
+    : Operator(OpClass::Transformation, "FFTTransformation"),
+      dimension_no(g.dimension_no),
+      dimension_size(g.size()),
+      grid_trans(fft_momentum_grid(g, name)) {}
+
+static void swap_grid(WaveFunction& wf, size_t dim, Grid& other) {
+  if (dim >= wf.grids.size()) throw Error(SO_ERR_SHAPE, "transformation axis out of range");
+  std::swap(wf.grids[dim], other);
+  wf.possible_norm_change = true;
+}
+
+static void emit_fft(WaveFunction& wf, Emitter& em, size_t dim, size_t n, int dir) {
+  if (dim >= wf.shape.size() || wf.shape[dim] != n) throw Error(SO_ERR_SHAPE, "FFT size differs from the axis");
+  Action a{};
+  a.op.kind = OP_FFT;
+  a.op.dir = dir;
+  a.lane_axis = (int)dim;
+  em.emit(a);
+}
+
+void FFTTransformation::transform(WaveFunction& wf, Emitter& em) {
+  swap_grid(wf, dimension_no, grid_trans);
+  emit_fft(wf, em, dimension_no, dimension_size, -1);
+}
+
+void FFTTransformation::inverse_transform(WaveFunction& wf, Emitter& em) {
+  swap_grid(wf, dimension_no, grid_trans);
+  emit_fft(wf, em, dimension_no, dimension_size, +1);
+}
+
+MatrixTransformation::MatrixTransformation(const Grid& g, const Grid& gt)
+    : Operator(OpClass::Transformation, "MatrixTransformation"),
+      dimension_no(g.dimension_no),
+      dimension_size(g.size()),
+      t(g.size() * g.size(), cplx(0, 0)),
+      tinv(g.size() * g.size(), cplx(0, 0)),
+      grid_trans(gt) {}
+
+static void emit_mat(WaveFunction& wf, Emitter& em, const void* key, uint64_t version, const std::vector<cplx>& m,
+                     size_t dim, size_t n) {
+  if (dim >= wf.shape.size() || wf.shape[dim] != n) throw Error(SO_ERR_SHAPE, "matrix size differs from the axis");
+  Action a{};
+  bool real = false;
+  a.op.kind = OP_MAT;
+  a.op.ptr = wf.eng->matrices(key, version, m, n, 1, real);
+  a.op.flags = real ? 1 : 0;
+  a.lane_axis = (int)dim;
+  em.emit(a);
+}
+
+void MatrixTransformation::transform(WaveFunction& wf, Emitter& em) {
+  swap_grid(wf, dimension_no, grid_trans);
+  emit_mat(wf, em, &t, version, t, dimension_no, dimension_size);
+}
+
+void MatrixTransformation::inverse_transform(WaveFunction& wf, Emitter& em) {
+  swap_grid(wf, dimension_no, grid_trans);
+  emit_mat(wf, em, &tinv, version, tinv, dimension_no, dimension_size);
+}
+
+StateMatrixTransformation::StateMatrixTransformation(size_t dep, const Grid& g, const Grid& gt)
+    : Operator(OpClass::Transformation, "StateMatrixTransformation"),
+      dimension_no(g.dimension_no),
+      dependent(dep),
+      n(g.size()),
+      grid_trans(gt) {
+  if (dep <= g.dimension_no) throw Error(SO_ERR_INVALID, "Dependent dimension should have higher dimension index");
+}
+
+static void emit_state_mat(WaveFunction& wf, Emitter& em, const void* key, uint64_t version,
+                           const std::vector<cplx>& m, size_t count, size_t dim, size_t dep, size_t n) {
+  if (dim >= wf.shape.size() || dep >= wf.shape.size() || wf.shape[dim] != n)
+    throw Error(SO_ERR_SHAPE, "state matrix size differs from the axis");
+  Action a{};
+  bool real = false;
+  a.op.kind = OP_MAT_SLICE;
+  a.op.ptr = count ? wf.eng->matrices(key, version, m, n, count, real) : nullptr;
+  a.op.flags = real ? 1 : 0;
+  a.op.axis = (int)dep;
+  a.op.count = (int64_t)count;
+  a.lane_axis = (int)dim;
+  em.emit(a);
+}
+
+void StateMatrixTransformation::transform(WaveFunction& wf, Emitter& em) {
+  swap_grid(wf, dimension_no, grid_trans);
+  emit_state_mat(wf, em, &ts, version, ts, count, dimension_no, dependent, n);
+}
+
+void StateMatrixTransformation::inverse_transform(WaveFunction& wf, Emitter& em) {
+  swap_grid(wf, dimension_no, grid_trans);
+  emit_state_mat(wf, em, &tinvs, version, tinvs, count, dimension_no, dependent, n);
+}
+
+// ------------------------------------------------------------------------ controls
+void LeakControl::first_half(WaveFunction& wf, Emitter& em) {
+  const int n = norm_slot(wf, em);
+  const auto& s = st.bind(wf.eng.get());
+  em.emit(scalar_action(OP_COPY, s[0], n));
+  if (lc) lc->check_before(wf, em);
+}
+
+void LeakControl::second_half(WaveFunction& wf, Emitter& em) {
+  if (lc) lc->check_after(wf, em);
+  const auto& s = st.bind(wf.eng.get());
+  normalize_to_slot(wf, em, s[0]);
+}
+
+BorderDumping::BorderDumping(const std::vector<cplx>& mask, const Grid& g)
+    : Operator(OpClass::Control, "BorderDumping"), op(mask.size(), g.dimension_no) {
+  op.op = mask;
+}
+
+void BorderDumping::half(WaveFunction& wf, Emitter& em) {
+  if (lc) lc->check_before(wf, em);
+  op.apply(wf, em);
+  if (lc) lc->check_after(wf, em);
+}
+
+// -------------------------------------------------------------------------- savers
+StateSaver::StateSaver(const std::string& name, so_time_grid t, const Grid& a, const Grid* b, size_t frames)
+    : Operator(OpClass::Saver, b ? "WaveFunctionSaver" : "StateSaver"),
+      two_d(b != nullptr),
+      fname(name),
+      time(t),
+      grid_a(a),
+      frames_no(frames) {
+  if (b) grid_b = *b;
+  if (frames_no == 0 || frames_no > time.step_no)
+    throw Error(SO_ERR_INVALID, "frames_no must be between 1 and step_no (the reference divides step_no by it)");
+  points = two_d ? grid_a.size() * grid_b.size() : grid_a.size();
+  data.assign(points * frames_no, 0.0);
+}
+
+void StateSaver::monitor(WaveFunction& wf, Emitter& em) {
+  if (two_d && wf.shape.size() != 2) throw Error(SO_ERR_STATE, "Wave function must be 2d for now");
+  const size_t freq = time.step_no / frames_no;
+  if (current_frame % freq == 0 && current_frame / freq < frames_no) {
+    const size_t frame = current_frame / freq;
+    times.push_back(time.step * ((double)current_frame + 1.0));
+    WaveFunction* w = &wf;
+    em.host([this, w, frame]() { record_frame(*w, frame); });
+  }
+  current_frame += 1;
+}
+
+void StateSaver::record_frame(WaveFunction& wf, size_t frame) {
+  Engine& e = *wf.eng;
+  e.flush();
+  Geometry g{};
+  g.ndim = (int)wf.shape.size();
+  for (int q = 0; q < g.ndim; ++q) {
+    g.perm[q] = e.perm[q];
+    g.sshape[q] = (int64_t)wf.shape[e.perm[q]];
+  }
+  if (two_d || wf.shape.size() == 1) {
+    if (wf.points() != points) throw Error(SO_ERR_SHAPE, "saver grid sizes differ from the wave function");
+    DeviceBuffer d(points * sizeof(double));
+    cuda_check(launch_density(d.as<double>(), e.psi.ptr, e.fp64, g, e.stream), "density");
+    std::vector<double> h(points);
+    cuda_check(cudaMemcpyAsync(h.data(), d.ptr, points * sizeof(double), cudaMemcpyDeviceToHost, e.stream), "copy");
+    cuda_check(cudaStreamSynchronize(e.stream), "sync");
+    for (size_t i = 0; i < points; ++i) data[i * frames_no + frame] = h[i];
+  } else {
+    const size_t axis = grid_a.dimension_no;
+    if (axis >= wf.shape.size() || wf.shape[axis] != points)
+      throw Error(SO_ERR_SHAPE, "state grid differs from the wave function axis");
+    std::vector<const double*> w = wf.weight_ptrs();
+    DeviceBuffer d(points * sizeof(double));
+    cuda_check(launch_state_density(d.as<double>(), e.psi.ptr, e.fp64, g, (int)axis, w.data(), nullptr, e.stream),
+               "state density");
+    std::vector<double> h(points);
+    cuda_check(cudaMemcpyAsync(h.data(), d.ptr, points * sizeof(double), cudaMemcpyDeviceToHost, e.stream), "copy");
+    cuda_check(cudaStreamSynchronize(e.stream), "sync");
+    for (size_t i = 0; i < points; ++i) data[i * frames_no + frame] = h[i];
+  }
+}
+
+void StateSaver::reset() { data.assign(points * frames_no, 0.0); }
+
+// ------------------------------------------------------------------- Propagation
+static std::vector<int> choose_perm(size_t ndim, const OperationStack& st) {
+  int fft_axis = -1;
+  for (const auto& e : st.stack)
+    if (auto* f = dynamic_cast<FFTTransformation*>(e.op.get())) {
+      fft_axis = (int)f->dimension_no;
+      break;
+    }
+  std::vector<int> perm;
+  for (size_t a = 0; a < ndim; ++a)
+    if ((int)a != fft_axis) perm.push_back((int)a);
+  if (fft_axis >= 0 && (size_t)fft_axis < ndim) perm.push_back(fft_axis);
+  return perm;
+}
+
+Propagation::Propagation(WaveFunction& src, so_time_grid time, std::shared_ptr<OperationStack> stack, int prec)
+    : precision(prec), time_(time), stack_(std::move(stack)) {
+  if (prec < SO_PRECISION_FP64 || prec > SO_PRECISION_FP32_SIMT) throw Error(SO_ERR_INVALID, "unknown precision");
+  const bool fp64 = prec == SO_PRECISION_FP64;
+  wf_ = std::make_unique<WaveFunction>(src.shape, src.grids, choose_perm(src.shape.size(), *stack_), fp64);
+  wf_->last_grid_names = src.last_grid_names;
+  wf_->possible_norm_change = src.possible_norm_change;
+  wf_->eng->write_slot(wf_->cache_slot, src.eng->read_slot(src.cache_slot));
+  std::vector<double> host(src.points() * 2);
+  src.eng->export_host(host.data());
+  wf_->eng->import_host(host.data());
+  wf_->eng->sync();
+  for (const auto& e : stack_->stack) keep_.push_back(e.op);
+}
+
+Propagation::~Propagation() {
+  try {
+    if (wf_) wf_->eng->sync();
+  } catch (...) {
+  }
+}
+
+void Propagation::step(Emitter& em) {
+  WaveFunction& wf = *wf_;
+  auto& ops = stack_->stack;
+  for (auto& e : ops) {
+    Operator& op = *e.op;
+    switch (op.cls) {
+      case OpClass::Propagator:
+        op.apply(wf, em);
+        break;
+      case OpClass::Transformation:
+        if (e.flag == SO_ORDER_NORMAL)
+          op.transform(wf, em);
+        else
+          op.inverse_transform(wf, em);
+        break;
+      case OpClass::Saver:
+        if (e.flag & SO_APPLY_FIRST_HALF) op.monitor(wf, em);
+        break;
+      case OpClass::Control:
+        if (e.flag & SO_APPLY_FIRST_HALF) op.first_half(wf, em);
+        break;
+    }
+  }
+  for (size_t i = ops.size(); i-- > 1;) {
+    auto& e = ops[i - 1];
+    Operator& op = *e.op;
+    switch (op.cls) {
+      case OpClass::Propagator:
+        op.apply(wf, em);
+        break;
+      case OpClass::Transformation:
+        if (e.flag == SO_ORDER_NORMAL)
+          op.inverse_transform(wf, em);
+        else
+          op.transform(wf, em);
+        break;
+      case OpClass::Saver:
+        if (e.flag & SO_APPLY_SECOND_HALF) op.monitor(wf, em);
+        break;
+      case OpClass::Control:
+        if (e.flag & SO_APPLY_SECOND_HALF) op.second_half(wf, em);
+        break;
+    }
+  }
+}
+
+static bool same_program(const std::vector<Action>& a, const std::vector<Action>& b) {
+  if (a.size() != b.size()) return false;
+  for (size_t i = 0; i < a.size(); ++i) {
+    if (a[i].lane_axis != b[i].lane_axis || a[i].host_call != b[i].host_call) return false;
+    if (std::memcmp(&a[i].op, &b[i].op, sizeof(DevOp)) != 0) return false;
+  }
+  return true;
+}
+
+void Propagation::steps(uint64_t n) {
+  Engine& e = *wf_->eng;
+  if (!e.resident_capable()) {
+    Emitter em{&e};
+    for (uint64_t i = 0; i < n; ++i) step(em);
+    e.flush();
+    return;
+  }
+  // Whole array in one CTA: consecutive identical steps run as one launch.
+  std::vector<Action> prev;
+  int rep = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    std::vector<Action> rec;
+    std::vector<std::function<void()>> calls;
+    Emitter em{&e, &rec, &calls};
+    step(em);
+    const bool has_host = std::any_of(rec.begin(), rec.end(), [](const Action& a) { return a.host_call >= 0; });
+    if (!has_host && rep > 0 && same_program(rec, prev)) {
+      ++rep;
+      continue;
+    }
+    if (rep > 0) e.run_resident(prev, rep);
+    rep = 0;
+    prev.clear();
+    if (has_host) {
+      std::vector<Action> seg;
+      for (const Action& a : rec) {
+        if (a.host_call >= 0) {
+          e.run_resident(seg, 1);
+          seg.clear();
+          calls[a.host_call]();
+        } else {
+          seg.push_back(a);
+        }
+      }
+      e.run_resident(seg, 1);
+    } else {
+      prev = std::move(rec);
+      rep = 1;
+    }
+  }
+  if (rep > 0) e.run_resident(prev, rep);
+}
+
+double Propagation::mean_energy() {
+  Engine& e = *wf_->eng;
+  Emitter em{&e};
+  if (time_.im_time) {
+    if (stack_->stack.empty() || stack_->stack[0].op->cls != OpClass::Control ||
+        stack_->stack[0].op->name() != "LeakControl")
+      throw Error(SO_ERR_STATE, "For imaginary time propagation first control must be LeakControl.");
+    LossChecker* lc = stack_->stack[0].op->loss_checker();
+    if (!lc) throw Error(SO_ERR_STATE, "Leak control must have loss checker to get mean energy for imaginary time.");
+    lc->reset(&em);
+    steps(1);
+    const int n = norm_slot(*wf_, em);
+    const double norm = e.read_slot(n);
+    const double decay = lc->loss();
+    e.check_nonfinite();
+    return -std::log(norm - decay) / time_.step / 2.0;
+  }
+  e.flush();
+  DeviceBuffer before(e.points() * e.elem_bytes());
+  cuda_check(cudaMemcpyAsync(before.ptr, e.psi.ptr, before.bytes, cudaMemcpyDeviceToDevice, e.stream), "clone");
+  steps(1);
+  const int sre = e.alloc_slot(0.0), sim = e.alloc_slot(0.0);
+  Action a{};
+  a.op.kind = OP_DOT;
+  a.op.a = sre;
+  a.op.b = sim;
+  a.op.ptr = before.ptr;
+  std::vector<const double*> w = wf_->weight_ptrs();
+  for (size_t k = 0; k < w.size(); ++k) a.op.w[k] = w[k];
+  e.submit(a);
+  const double re = e.read_slot(sre), im = e.read_slot(sim);
+  e.free_slot(sre);
+  e.free_slot(sim);
+  e.sync();
+  return -std::atan2(im, re) / time_.step;
+}
+
+std::vector<double> Propagation::losses(bool include_controls) {
+  std::vector<double> out;
+  for (auto& e : stack_->stack) {
+    if (e.op->cls == OpClass::Propagator || (include_controls && e.op->cls == OpClass::Control))
+      if (LossChecker* lc = e.op->loss_checker()) out.push_back(lc->loss());
+  }
+  wf_->eng->check_nonfinite();
+  return out;
+}
+
+void Propagation::reset_losses() {
+  Emitter em{wf_->eng.get()};
+  for (auto& e : stack_->stack)
+    if (e.op->cls == OpClass::Propagator)
+      if (LossChecker* lc = e.op->loss_checker()) lc->reset(&em);
+  wf_->eng->flush();
+}
+
+std::unique_ptr<WaveFunction> Propagation::snapshot() {
+  std::vector<int> ident(wf_->shape.size());
+  std::iota(ident.begin(), ident.end(), 0);
+  auto w = std::make_unique<WaveFunction>(wf_->shape, wf_->grids, ident, true);
+  w->last_grid_names = wf_->last_grid_names;
+  w->possible_norm_change = wf_->possible_norm_change;
+  w->eng->write_slot(w->cache_slot, wf_->eng->read_slot(wf_->cache_slot));
+  std::vector<double> host(wf_->points() * 2);
+  wf_->eng->export_host(host.data());
+  w->eng->import_host(host.data());
+  w->eng->sync();
+  return w;
+}
+
+void Propagation::reset_savers() {
+  for (auto& e : stack_->stack)
+    if (e.op->cls == OpClass::Saver) e.op->reset();
+}
+
+void Propagation::savers_save() {
+  wf_->eng->sync();
+  for (auto& e : stack_->stack)
+    if (auto* s = dynamic_cast<StateSaver*>(e.op.get())) s->save();
+}
+
+void Propagation::get_array(double* out) { wf_->eng->export_host(out); }
+
+void Propagation::set_array(const double* in) {
+  wf_->eng->import_host(in);
+  wf_->possible_norm_change = true;
+}
+
+double Propagation::norm() {
+  Emitter em{wf_->eng.get()};
+  const int s = norm_slot(*wf_, em);
+  const double v = wf_->eng->read_slot(s);
+  wf_->eng->check_nonfinite();
+  return v;
+}
+
+void Propagation::synchronize() {
+  wf_->eng->sync();
+  wf_->eng->check_nonfinite();
+}
+
+static const char* kind_name(int k) {
+  switch (k) {
+    case OP_DIAG1D: return "diag1d";
+    case OP_DIAGND: return "diagnd";
+    case OP_FFT: return "fft";
+    case OP_MAT: return "mat";
+    case OP_MAT_LANE: return "mat_lane";
+    case OP_MAT_SLICE: return "mat_slice";
+    case OP_NORM: return "norm";
+    case OP_COPY: return "copy";
+    case OP_LOSS: return "loss";
+    case OP_SCALE: return "scale";
+    case OP_SETC: return "setc";
+    case OP_RECORD: return "record";
+    case OP_DOT: return "dot";
+  }
+  return "?";
+}
+
+std::string Propagation::describe() {
+  // Record two steps and group them the way Engine::submit would.
+  std::vector<Action> rec;
+  std::vector<std::function<void()>> calls;
+  Emitter em{wf_->eng.get(), &rec, &calls};
+  // describe() must not change observable state: run on a copy of the host-side flags only
+  const bool pnc = wf_->possible_norm_change;
+  const auto names = wf_->last_grid_names;
+  const auto grids = wf_->grids;
+  std::vector<Grid> trans_grids;
+  for (auto& e : stack_->stack)
+    if (Grid* g = e.op->grid_transformation()) trans_grids.push_back(*g);
+  std::vector<size_t> frames;
+  for (auto& e : stack_->stack)
+    if (auto* s = dynamic_cast<StateSaver*>(e.op.get())) frames.push_back(s->current_frame);
+  std::vector<std::vector<double>> times;
+  for (auto& e : stack_->stack)
+    if (auto* s = dynamic_cast<StateSaver*>(e.op.get())) times.push_back(s->times);
+  step(em);
+  step(em);
+  wf_->possible_norm_change = pnc;
+  wf_->last_grid_names = names;
+  wf_->grids = grids;
+  size_t ti = 0, fi = 0, tmi = 0;
+  for (auto& e : stack_->stack)
+    if (Grid* g = e.op->grid_transformation()) *g = trans_grids[ti++];
+  for (auto& e : stack_->stack)
+    if (auto* s = dynamic_cast<StateSaver*>(e.op.get())) {
+      s->current_frame = frames[fi++];
+      s->times = times[tmi++];
+    }
+  std::string out = wf_->eng->resident_capable() ? "resident " : "sweep ";
+  out += "perm=";
+  for (int p : wf_->eng->perm) out += std::to_string(p);
+  out += "\n";
+  int axis = -1;
+  std::vector<int> written;
+  int nops = 0;
+  std::string cur;
+  auto close = [&]() {
+    if (nops) out += "pass axis=" + std::to_string(axis) + ": " + cur + "\n";
+    cur.clear();
+    nops = 0;
+    axis = -1;
+    written.clear();
+  };
+  for (const Action& a : rec) {
+    if (a.host_call >= 0) {
+      close();
+      out += "host\n";
+      continue;
+    }
+    if (!wf_->eng->resident_capable()) {
+      if (a.lane_axis >= 0 && axis >= 0 && axis != a.lane_axis) close();
+      if (a.op.kind == OP_SCALE)
+        for (int w : written)
+          if (w == a.op.b || w == a.op.c) {
+            close();
+            break;
+          }
+    }
+    if (a.lane_axis >= 0) axis = a.lane_axis;
+    if (a.op.kind == OP_NORM || a.op.kind == OP_COPY || a.op.kind == OP_LOSS || a.op.kind == OP_SETC)
+      written.push_back(a.op.a);
+    cur += kind_name(a.op.kind);
+    if (a.lane_axis >= 0) cur += "@" + std::to_string(a.lane_axis);
+    cur += " ";
+    ++nops;
+  }
+  close();
+  return out;
+}
+
+}  // namespace so

@@ -1,0 +1,371 @@
+// Host-side model of the split-operator API (C++), mirroring the Rust crate's
+// types: Grid, WaveFunction (+ ChangeObserver norm cache), the propagators,
+// transformations, controls, savers, LossChecker, OperationStack and
+// Propagation.  The objects hold FP64 host tables; the arrays they act on live
+// in GPU memory inside an Engine, which turns the stream of actions the host
+// logic emits into fused lane-sweep passes.
+#pragma once
+#include <complex>
+#include <functional>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/split_operator.h"
+#include "common.cuh"
+
+namespace so {
+
+using cplx = std::complex<double>;
+
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+void cuda_check(cudaError_t e, const char* what);
+
+// ------------------------------------------------------------------ grid.rs
+struct Grid {
+  std::string name;
+  size_t dimension_no = 0;
+  std::vector<double> nodes, weights;
+  uint64_t uid = 0;  // identifies the weight vector on the device
+  static uint64_t next_uid();
+  static Grid linear_continuos(const std::string&, double, double, size_t, size_t);
+  static Grid linear_countable(const std::string&, double, double, size_t, size_t);
+  static Grid custom(const std::string&, std::vector<double>, std::vector<double>, size_t);
+  size_t size() const { return nodes.size(); }
+};
+
+// factory.cpp
+std::vector<double> momenta_fft_order(const Grid& g);
+Grid fft_momentum_grid(const Grid& g, const std::string& name);
+std::vector<double> kinetic_hamiltonian(const Grid& g, double red_mass);
+std::vector<double> rotational_hamiltonian(const Grid& radial, const Grid& polar, double red_mass, double b);
+std::vector<double> legendre_polynomials(size_t j, double x);
+std::vector<double> associated_legendre_polynomials(size_t j, int64_t m, double x);
+void legendre_matrices(const Grid& polar, int64_t omega, std::vector<cplx>& t, std::vector<cplx>& tinv);
+void gauss_legendre(size_t n, std::vector<double>& x, std::vector<double>& w);
+std::vector<cplx> twiddles(size_t n);
+double pot_dispersion(double r, int n, double cn);
+double pot_lennard_jones(double r, double d6, double r6);
+double pot_harmonic(double r, double r0, double mass, double omega);
+double pot_morse(double r, double d, double a, double re);
+cplx gaussian(double x, double x0, double sigma, double p);
+std::vector<cplx> dumping_end(double width, double end, const Grid& g);
+cplx select_step(int step, const so_time_grid& t);
+std::vector<cplx> phase_table(const double* h, size_t n, cplx dt);
+std::vector<cplx> phase_table_complex(const cplx* h, size_t n, cplx dt);
+
+// ------------------------------------------------------------ device memory
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DeviceBuffer() = default;
+  explicit DeviceBuffer(size_t b);
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+  DeviceBuffer(DeviceBuffer&& o) noexcept : ptr(o.ptr), bytes(o.bytes) { o.ptr = nullptr; o.bytes = 0; }
+  DeviceBuffer& operator=(DeviceBuffer&& o) noexcept;
+  ~DeviceBuffer();
+  template <typename T>
+  T* as() const { return reinterpret_cast<T*>(ptr); }
+};
+
+class Engine;
+
+// Scalars of an operator (loss, current norm, leak norm) that live in device
+// slots while an engine uses them, and on the host otherwise.
+struct ScalarState {
+  std::vector<double> host;
+  Engine* home = nullptr;
+  std::vector<int> slots;
+  explicit ScalarState(size_t n = 0) : host(n, 0.0) {}
+  ScalarState(const ScalarState&) = delete;
+  ~ScalarState();
+  const std::vector<int>& bind(Engine* e);
+  void unbind();  // copies device values back to `host`
+  double get(size_t i);
+  void set(size_t i, double v);
+};
+
+// One emitted unit of work: a device op (with the lane axis it needs, -1 for
+// point-wise and scalar ops) or a host callback (saver frames).
+struct Action {
+  DevOp op{};
+  int lane_axis = -1;
+  int host_call = -1;
+};
+
+class Engine {
+ public:
+  Engine(const std::vector<size_t>& shape, const std::vector<int>& perm, bool fp64);
+  ~Engine();
+
+  bool fp64;
+  std::vector<size_t> shape;  // logical
+  std::vector<int> perm;      // storage position -> logical axis
+  DeviceBuffer psi;
+  cudaStream_t stream = nullptr;
+  int nonfinite_slot = 0;
+
+  size_t points() const;
+  size_t elem_bytes() const { return fp64 ? 16 : 8; }
+  Geometry geometry(int sweep_axis, bool resident) const;
+  bool resident_capable() const;
+
+  // scalar slots
+  int alloc_slot(double init);
+  void free_slot(int s);
+  void write_slot(int s, double v);
+  double read_slot(int s);  // synchronizes
+  double* slots() const { return slots_.as<double>(); }
+
+  // device copies of host tables (state precision), cached by key
+  const void* table_1d(const void* key, uint64_t version, const std::vector<cplx>& t);
+  const void* table_nd(const void* key, uint64_t version, const std::vector<cplx>& t);
+  const void* matrices(const void* key, uint64_t version, const std::vector<cplx>& m, size_t n, size_t count,
+                       bool& real);
+  const double* weights(const Grid& g);
+  const void* twiddle(size_t n);
+
+  // pass building
+  void submit(const Action& a);
+  void flush();
+  void run_resident(const std::vector<Action>& prog, int repeat);
+  void sync();
+  void import_host(const double* host);   // logical complex128 -> storage
+  void export_host(double* host);         // storage -> logical complex128 (synchronizes)
+  void check_nonfinite();
+
+  std::vector<ScalarState*> bound;
+  double* record_dev = nullptr;
+
+ private:
+  void launch(const std::vector<DevOp>& ops, int axis, bool resident, int repeat);
+  DeviceBuffer slots_, partials_, counter_, staging_;
+  size_t partials_cap_ = 0;
+  std::vector<int> free_slots_;
+  int next_slot_ = 1;
+  struct Cached {
+    uint64_t version;
+    DeviceBuffer buf;
+    bool real;
+  };
+  std::map<std::pair<const void*, int>, Cached> tables_;
+  std::map<uint64_t, DeviceBuffer> weights_;
+  std::map<size_t, DeviceBuffer> twiddles_;
+  // open pass
+  std::vector<DevOp> cur_;
+  int cur_axis_ = -1;
+  int cur_red_ = 0;
+  std::vector<int> cur_written_;
+};
+
+// ------------------------------------------------------------ wave function
+struct WaveFunction {
+  std::vector<size_t> shape;
+  std::vector<Grid> grids;
+  std::vector<std::string> last_grid_names;  // change_observer.rs:8
+  bool possible_norm_change = true;          // change_observer.rs:11
+  std::unique_ptr<Engine> eng;
+  int cache_slot = -1;  // change_observer.rs:10 (last_norm), on the device
+
+  WaveFunction(const std::vector<size_t>& shape, const std::vector<Grid>& grids, const std::vector<int>& perm,
+               bool fp64);
+  std::vector<const double*> weight_ptrs();
+  size_t points() const;
+};
+
+// Where the host logic sends its actions: straight to the engine, or recorded.
+struct Emitter {
+  Engine* eng;
+  std::vector<Action>* rec = nullptr;
+  std::vector<std::function<void()>>* calls = nullptr;
+  void emit(const Action& a) {
+    if (rec)
+      rec->push_back(a);
+    else
+      eng->submit(a);
+  }
+  void host(std::function<void()> f);
+};
+
+// wave_function.rs:68-85 on the host side: returns the slot holding the norm,
+// emitting a norm reduction only when the cache is dirty.
+int norm_slot(WaveFunction& wf, Emitter& em);
+void normalize_to_slot(WaveFunction& wf, Emitter& em, int target_slot);
+
+// ------------------------------------------------------------ operators
+struct LossChecker {  // loss_checker.rs:7-69 (LossSaver not reproduced)
+  std::string name;
+  ScalarState st{2};  // 0: loss, 1: current_norm
+  explicit LossChecker(const std::string& n) : name(n) { st.host[1] = 1.0; }
+  void check_before(WaveFunction& wf, Emitter& em);
+  void check_after(WaveFunction& wf, Emitter& em);
+  void reset(Emitter* em);
+  double loss() { return st.get(0); }
+};
+
+enum class OpClass { Propagator, Transformation, Control, Saver };
+
+struct Operator {
+  OpClass cls;
+  std::string type;
+  uint64_t version = 1;
+  explicit Operator(OpClass c, const std::string& t) : cls(c), type(t) {}
+  virtual ~Operator() = default;
+  // Propagator
+  virtual void apply(WaveFunction&, Emitter&) { throw Error(SO_ERR_INVALID, "not a propagator"); }
+  virtual LossChecker* loss_checker() { return nullptr; }
+  // Transformation
+  virtual void transform(WaveFunction&, Emitter&) { throw Error(SO_ERR_INVALID, "not a transformation"); }
+  virtual void inverse_transform(WaveFunction&, Emitter&) { throw Error(SO_ERR_INVALID, "not a transformation"); }
+  virtual Grid* grid_transformation() { return nullptr; }
+  // Control
+  virtual std::string name() const { return type; }
+  virtual void first_half(WaveFunction&, Emitter&) { throw Error(SO_ERR_INVALID, "not a control"); }
+  virtual void second_half(WaveFunction&, Emitter&) { throw Error(SO_ERR_INVALID, "not a control"); }
+  // Saver
+  virtual void monitor(WaveFunction&, Emitter&) { throw Error(SO_ERR_INVALID, "not a saver"); }
+  virtual void reset() {}
+};
+
+struct OneDimPropagator : Operator {
+  size_t dimension_no;
+  std::vector<cplx> op;
+  std::unique_ptr<LossChecker> lc;
+  OneDimPropagator(size_t shape, size_t dim)
+      : Operator(OpClass::Propagator, "OneDimPropagator"), dimension_no(dim), op(shape, cplx(1, 0)) {}
+  void apply_unchecked(WaveFunction& wf, Emitter& em);
+  void apply(WaveFunction& wf, Emitter& em) override;
+  LossChecker* loss_checker() override { return lc.get(); }
+};
+
+struct NDimPropagator : Operator {
+  std::vector<size_t> shape{1};
+  std::vector<cplx> op{cplx(0, 0)};
+  std::unique_ptr<LossChecker> lc;
+  NDimPropagator() : Operator(OpClass::Propagator, "NDimPropagator") {}
+  void apply(WaveFunction& wf, Emitter& em) override;
+  LossChecker* loss_checker() override { return lc.get(); }
+};
+
+struct NonDiagPropagator : Operator {
+  size_t dimension_no;
+  size_t n = 0, count = 0;
+  std::vector<cplx> ops;  // count x n x n
+  std::unique_ptr<LossChecker> lc;
+  explicit NonDiagPropagator(size_t dim) : Operator(OpClass::Propagator, "NonDiagPropagator"), dimension_no(dim) {}
+  void apply(WaveFunction& wf, Emitter& em) override;
+  LossChecker* loss_checker() override { return lc.get(); }
+};
+
+struct FFTTransformation : Operator {
+  size_t dimension_no, dimension_size;
+  Grid grid_trans;
+  FFTTransformation(const Grid& g, const std::string& name);
+  void transform(WaveFunction& wf, Emitter& em) override;
+  void inverse_transform(WaveFunction& wf, Emitter& em) override;
+  Grid* grid_transformation() override { return &grid_trans; }
+};
+
+struct MatrixTransformation : Operator {
+  size_t dimension_no, dimension_size;
+  std::vector<cplx> t, tinv;
+  Grid grid_trans;
+  MatrixTransformation(const Grid& g, const Grid& gt);
+  void transform(WaveFunction& wf, Emitter& em) override;
+  void inverse_transform(WaveFunction& wf, Emitter& em) override;
+  Grid* grid_transformation() override { return &grid_trans; }
+};
+
+struct StateMatrixTransformation : Operator {
+  size_t dimension_no, dependent, n, count = 0;
+  std::vector<cplx> ts, tinvs;
+  Grid grid_trans;
+  StateMatrixTransformation(size_t dep, const Grid& g, const Grid& gt);
+  void transform(WaveFunction& wf, Emitter& em) override;
+  void inverse_transform(WaveFunction& wf, Emitter& em) override;
+  Grid* grid_transformation() override { return &grid_trans; }
+};
+
+struct LeakControl : Operator {  // leak_control.rs
+  ScalarState st{1};
+  std::unique_ptr<LossChecker> lc;
+  LeakControl() : Operator(OpClass::Control, "LeakControl") {}
+  std::string name() const override { return "LeakControl"; }
+  void first_half(WaveFunction& wf, Emitter& em) override;
+  void second_half(WaveFunction& wf, Emitter& em) override;
+  LossChecker* loss_checker() override { return lc.get(); }
+};
+
+struct BorderDumping : Operator {  // border_dumping.rs:36-93
+  OneDimPropagator op;
+  std::unique_ptr<LossChecker> lc;
+  BorderDumping(const std::vector<cplx>& mask, const Grid& g);
+  std::string name() const override { return "BorderDumping"; }
+  void half(WaveFunction& wf, Emitter& em);
+  void first_half(WaveFunction& wf, Emitter& em) override { half(wf, em); }
+  void second_half(WaveFunction& wf, Emitter& em) override { half(wf, em); }
+  LossChecker* loss_checker() override { return lc.get(); }
+};
+
+struct StateSaver : Operator {  // wave_function_saver.rs:101-183 (StateSaver) and :6-98 (2-D saver)
+  bool two_d;
+  std::string fname;
+  so_time_grid time;
+  Grid grid_a, grid_b;  // state grid (or x grid), y grid
+  size_t frames_no, current_frame = 0, points;
+  std::vector<double> data;  // (points, frames_no) row-major
+  std::vector<double> times;
+  StateSaver(const std::string& name, so_time_grid t, const Grid& a, const Grid* b, size_t frames);
+  void monitor(WaveFunction& wf, Emitter& em) override;
+  void reset() override;
+  void record_frame(WaveFunction& wf, size_t frame);
+  void save() const;
+};
+
+// ------------------------------------------------------------ stack + propagation
+struct StackEntry {
+  std::shared_ptr<Operator> op;
+  int flag;  // Order or Apply bits
+};
+
+struct OperationStack {
+  std::vector<StackEntry> stack;
+};
+
+class Propagation {
+ public:
+  Propagation(WaveFunction& wf, so_time_grid time, std::shared_ptr<OperationStack> stack, int precision);
+  ~Propagation();
+  void steps(uint64_t n);
+  void propagate() { steps(time_.step_no); }
+  void reset_savers();
+  void savers_save();
+  double mean_energy();
+  std::vector<double> losses(bool include_controls);
+  void reset_losses();
+  std::unique_ptr<WaveFunction> snapshot();
+  void get_array(double* out);
+  void set_array(const double* in);
+  double norm();
+  std::string describe();
+  void set_stream(cudaStream_t s) { wf_->eng->stream = s; }
+  void synchronize();
+
+  int precision;
+
+ private:
+  void step(Emitter& em);
+  std::unique_ptr<WaveFunction> wf_;
+  so_time_grid time_;
+  std::shared_ptr<OperationStack> stack_;
+  std::vector<std::shared_ptr<Operator>> keep_;
+};
+
+}  // namespace so

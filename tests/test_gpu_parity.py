@@ -1,0 +1,163 @@
+"""GPU parity of the split-operator path against the FP64 oracle and the
+reference's golden outputs, through the C ABI (ctypes)."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import scenarios as S
+from oracle import split_operator_oracle as O
+from tests.gpu_common import ensure_built, load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def so():
+    ensure_built()
+    import split_operator_gb300 as so
+    return so
+
+
+# ----------------------------------------------------------------- known answers
+def test_fft_known_answer_exact(so):
+    """tests/fft_tests.rs:11-78: forward result and bitwise round trip."""
+    import os
+    ka = np.load(os.path.join(os.path.dirname(__file__), "golden", "fft_known_answer.npz"))
+    g1 = so.Grid.new_linear_countable("a", 0.0, 1.0, 4, 0)
+    g2 = so.Grid.new_linear_countable("b", 0.0, 1.0, 4, 1)
+    wf = so.WaveFunction(ka["input"], [g1, g2])
+    fft = so.FFTTransformation(g1, "a_fft")
+    n1 = wf.norm()
+    fft.transform(wf)
+    np.testing.assert_array_equal(wf.array, ka["forward"])
+    assert wf.grid(0).name == "a_fft"
+    n2 = wf.norm()
+    fft.inverse_transform(wf)
+    np.testing.assert_array_equal(wf.array, ka["input"])
+    n3 = wf.norm()
+    assert n1 == n3
+    assert wf.grid(0).name == "a"
+    assert n2 > 0
+
+
+@pytest.mark.parametrize("n", [8, 16, 64, 256, 1024, 4096])
+def test_fft_lane_matches_numpy(so, n):
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
+    g = so.Grid.new_linear_continuos("x", 0.0, 1.0, n, 0)
+    g2 = so.Grid.new_linear_countable("y", 0.0, 2.0, 3, 1)
+    wf = so.WaveFunction(a, [g, g2])
+    f = so.FFTTransformation(g, "k")
+    f.transform(wf)
+    assert rel_l2(wf.array, np.fft.fft(a, axis=0, norm="ortho")) < 1e-14
+    f.inverse_transform(wf)
+    assert rel_l2(wf.array, a) < 1e-14
+
+
+@pytest.mark.parametrize("n", [3, 5, 12, 100])
+def test_fft_non_power_of_two(so, n):
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    g = so.Grid.new_linear_continuos("x", 0.0, 1.0, n, 0)
+    wf = so.WaveFunction(a, [g])
+    so.FFTTransformation(g, "k").transform(wf)
+    assert rel_l2(wf.array, np.fft.fft(a, norm="ortho")) < 1e-13
+
+
+# ------------------------------------------------------------ reference goldens
+def _harmonic_trap(so, im_time):
+    grid = so.Grid.new_linear_continuos("space", -4.0, 4.0, 256, 0)
+    wf = so.WaveFunction(so.gaussian_distribution(grid.nodes, 2.0, 0.2, 0.0), [grid])
+    wf.normalize(1.0)
+    tg = so.TimeGrid(3.0, 1000, im_time)
+    mu = O.MU_LI6_LI7
+    v = so.harmonic(grid.nodes, 0.0, mu, 0.001)
+    saver = so.StateSaver("harmonic", tg, grid, 50)
+    st = so.OperationStack()
+    st.add_saver(saver, so.FIRST_HALF)
+    st.add_control(so.LeakControl(), so.FIRST_HALF | so.SECOND_HALF)
+    st.add_propagator(so.one_dim_into_propagator(v, grid, tg, so.HALF))
+    st.add_transformation(so.FFTTransformation(grid, "momentum"), so.NORMAL)
+    st.add_propagator(so.one_dim_into_propagator(so.kinetic_hamiltonian(grid, mu), grid, tg, so.FULL))
+    return so.Propagation(wf, tg, st, "fp64"), saver
+
+
+@pytest.mark.parametrize("im_time,name", [(False, "harmonic"), (True, "harmonic_imaginary")])
+def test_harmonic_trap_matches_reference_golden(so, im_time, name):
+    prop, saver = _harmonic_trap(so, im_time)
+    prop.propagate()
+    assert rel_l2(saver.data, load_golden(f"{name}.npy")) < 1e-12
+    np.testing.assert_array_equal(saver.times, load_golden(f"{name}_time.npy"))
+
+
+def test_lj_ground_state_matches_reference_golden_and_energy(so):
+    grid = so.Grid.new_linear_continuos("space", 8.0, 20.0, 512, 0)
+    mu = O.MU_LI6_LI7
+    mom = math.sqrt(2.0 * mu * 1e-7 * O.KELVIN_TO_AU)
+    wf = so.WaveFunction(so.gaussian_distribution(grid.nodes, 14.0, 2.0, mom), [grid])
+    wf.normalize(1.0)
+    tg = so.TimeGrid(50.0, 1000, True)
+    leak = so.LeakControl()
+    leak.add_loss_checker("leak control")
+    saver = so.StateSaver("lj", tg, grid, 120)
+    st = so.OperationStack()
+    st.add_control(leak, so.FIRST_HALF | so.SECOND_HALF)
+    st.add_saver(saver, so.FIRST_HALF)
+    st.add_propagator(so.one_dim_into_propagator(so.lennard_jones(grid.nodes, 0.0003, 9.7), grid, tg, so.HALF))
+    st.add_transformation(so.FFTTransformation(grid, "momentum"), so.NORMAL)
+    st.add_propagator(so.one_dim_into_propagator(so.kinetic_hamiltonian(grid, mu), grid, tg, so.FULL))
+    prop = so.Propagation(wf, tg, st, "fp64")
+    prop.propagate()
+    assert rel_l2(saver.data, load_golden("lj_ground_space.npy")) < 1e-12
+    e_gpu = prop.mean_energy()
+    oprop, _ = S.lj_ground_state()
+    oprop.propagate()
+    e_ref = oprop.mean_energy()
+    assert abs(e_gpu - e_ref) <= 1e-12 * abs(e_ref)
+
+
+# ------------------------------------------------------------ 1-D workload
+def test_harmonic_1d_fp64_matches_oracle_and_ehrenfest(so):
+    from split_operator_gb300 import workloads as W
+    prop, _ = W.harmonic_1d(step_no=1000)
+    oprop = S.harmonic_1d(step_no=1000)
+    x = np.linspace(-20.0, 20.0, 1024)
+    dx = x[1] - x[0]
+    for k in range(10):
+        prop.steps(100)
+        oprop.propagate(100)
+        a = prop.get_array()
+        assert rel_l2(a, oprop.wave_function.array) < 1e-11 * (k + 1)
+        t = 0.01 * 100 * (k + 1)
+        d = np.abs(a) ** 2
+        xm = np.sum(x * d) / np.sum(d)
+        # Ehrenfest: <x>(t) = x0 cos(omega t) for any Gaussian in a harmonic trap
+        assert abs(xm - 2.0 * math.cos(t)) < 2e-4
+    assert abs(prop.norm() - 1.0) < 1e-12
+
+
+def test_harmonic_1d_real_time_energy(so):
+    from split_operator_gb300 import workloads as W
+    prop, _ = W.harmonic_1d(step_no=10)
+    oprop = S.harmonic_1d(step_no=10)
+    e = prop.mean_energy()
+    eo = oprop.mean_energy()
+    assert abs(e - eo) < 1e-10 * abs(eo)
+
+
+# ------------------------------------------------------------ 2-D workload
+@pytest.mark.parametrize("nr,nth,steps", [(256, 16, 40), (512, 32, 20)])
+def test_radial_angular_fp64_per_step_parity(so, nr, nth, steps):
+    from split_operator_gb300 import workloads as W
+    prop, h = W.radial_angular_2d(nr=nr, nth=nth, step_no=steps, r0=25.0)
+    oprop, odamp = S.radial_angular_2d(nr=nr, nth=nth, step_no=steps, r0=25.0)
+    for k in range(steps):
+        prop.steps(1)
+        oprop.step()
+        err = rel_l2(prop.get_array(), oprop.wave_function.array)
+        assert err < 1e-12 * (k + 1), (k, err)
+    lo = odamp.loss().loss()
+    lg = h["damp"].loss()
+    assert abs(lg - lo) <= 1e-12 + 1e-9 * abs(lo)
+    assert prop.all_losses() == [lg]
