@@ -260,6 +260,12 @@ int so_propagation_set_stream(so_propagation p, void* stream);
 int so_propagation_synchronize(so_propagation p);
 /* Human-readable description of the fused device passes of one step (for tests and profiling). */
 int so_propagation_describe(so_propagation p, char* buf, size_t cap);
+/* Per-pass device timing (no reference counterpart): when enabled, every pass launch is
+ * bracketed by CUDA events on the propagation's stream.  so_propagation_kernel_times
+ * synchronizes, writes one line per pass kind "name<TAB>launches<TAB>total_ms<TAB>algorithmic_bytes"
+ * and clears the record. */
+int so_propagation_set_timing(so_propagation p, int enabled);
+int so_propagation_kernel_times(so_propagation p, char* buf, size_t cap);
 void so_propagation_free(so_propagation p);
 
 #if defined(__GNUC__)

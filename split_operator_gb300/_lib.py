@@ -127,6 +127,8 @@ SIGNATURES = {
     "so_propagation_set_stream": [_P, _P],
     "so_propagation_synchronize": [_P],
     "so_propagation_describe": [_P, C.c_char_p, _S],
+    "so_propagation_set_timing": [_P, _I],
+    "so_propagation_kernel_times": [_P, C.c_char_p, _S],
 }
 VOID = {
     "so_grid_free": [_P],

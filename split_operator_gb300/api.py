@@ -613,6 +613,13 @@ class Propagation(_Handle):
         a = _c128(a)
         call("so_propagation_set_array", self._h, _dp(a.view(np.float64)))
 
+    def set_array_ptr(self, host_ptr: int):
+        """Replace the state from a host buffer (complex128, logical order) given by address."""
+        call("so_propagation_set_array", self._h, C.cast(C.c_void_p(host_ptr), C.POINTER(C.c_double)))
+
+    def get_array_ptr(self, host_ptr: int):
+        call("so_propagation_get_array", self._h, C.cast(C.c_void_p(host_ptr), C.POINTER(C.c_double)))
+
     def wave_function_shape(self):
         if not hasattr(self, "_shape"):
             self._shape = self.wave_function().shape
@@ -633,6 +640,19 @@ class Propagation(_Handle):
         buf = C.create_string_buffer(1 << 16)
         call("so_propagation_describe", self._h, buf, 1 << 16)
         return buf.value.decode()
+
+    def set_timing(self, enabled: bool):
+        call("so_propagation_set_timing", self._h, 1 if enabled else 0)
+
+    def kernel_times(self):
+        """[(pass name, launches, total_ms, algorithmic bytes)] since the last call."""
+        buf = C.create_string_buffer(1 << 16)
+        call("so_propagation_kernel_times", self._h, buf, 1 << 16)
+        out = []
+        for line in buf.value.decode().splitlines():
+            name, n, ms, b = line.split("\t")
+            out.append((name, int(n), float(ms), float(b)))
+        return out
 
 
 def launch_count() -> int:

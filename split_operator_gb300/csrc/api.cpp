@@ -905,6 +905,18 @@ int so_propagation_describe(so_propagation p, char* buf, size_t cap) {
     std::snprintf(buf, cap, "%s", p->p->describe().c_str());
   });
 }
+int so_propagation_set_timing(so_propagation p, int enabled) {
+  return guard([&] {
+    need(p, "null argument");
+    p->p->set_timing(enabled != 0);
+  });
+}
+int so_propagation_kernel_times(so_propagation p, char* buf, size_t cap) {
+  return guard([&] {
+    need(p && buf && cap > 0, "null argument");
+    std::snprintf(buf, cap, "%s", p->p->kernel_times().c_str());
+  });
+}
 void so_propagation_free(so_propagation p) { delete p; }
 
 }  // extern "C"

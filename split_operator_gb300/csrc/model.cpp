@@ -71,6 +71,7 @@ void ScalarState::set(size_t i, double v) {
 }
 
 // ----------------------------------------------------------------------- Engine
+const char* op_kind_name(int k);
 static bool is_scalar_kind(int k) { return k == OP_COPY || k == OP_LOSS || k == OP_SETC || k == OP_RECORD; }
 
 Engine::Engine(const std::vector<size_t>& shp, const std::vector<int>& prm, bool f64)
@@ -377,7 +378,73 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
     p.partials = partials_.as<double>();
   }
+  if (timing) {
+    std::string name = std::string(fp64 ? "f64" : "f32") + (resident ? " resident" : " sweep") + " axis" +
+                       std::to_string(axis) + ":";
+    for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
+    timed_begin(name);
+    timed_.back().bytes = pass_bytes(ops, p.g);
+  }
   cuda_check(fp64 ? launch_pass_f64(p, stream) : launch_pass_f32(p, stream), "pass launch");
+  if (timing) timed_end();
+}
+
+cudaEvent_t Engine::take_event() {
+  if (!event_pool_.empty()) {
+    cudaEvent_t e = event_pool_.back();
+    event_pool_.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cuda_check(cudaEventCreate(&e), "event create");
+  return e;
+}
+
+void Engine::timed_begin(const std::string& name) {
+  TimedLaunch t{name, take_event(), take_event(), 0.0};
+  cuda_check(cudaEventRecord(t.a, stream), "event record");
+  timed_.push_back(t);
+}
+
+void Engine::timed_end() { cuda_check(cudaEventRecord(timed_.back().b, stream), "event record"); }
+
+double Engine::pass_bytes(const std::vector<DevOp>& ops, const Geometry& g) const {
+  // algorithmic bytes: read + write of the state, plus every full-size table streamed
+  double pts = 1.0;
+  for (int q = 0; q < g.ndim; ++q) pts *= (double)g.sshape[q];
+  double b = 2.0 * pts * (double)elem_bytes();
+  for (const DevOp& o : ops)
+    if (o.kind == OP_DIAGND || o.kind == OP_DOT) b += pts * (double)elem_bytes();
+  return b;
+}
+
+std::string Engine::collect_timing() {
+  flush();
+  cuda_check(cudaStreamSynchronize(stream), "stream sync");
+  struct Acc {
+    int n = 0;
+    double ms = 0.0, bytes = 0.0;
+  };
+  std::map<std::string, Acc> acc;
+  std::vector<std::string> order;
+  for (TimedLaunch& t : timed_) {
+    float ms = 0.f;
+    cuda_check(cudaEventElapsedTime(&ms, t.a, t.b), "event elapsed");
+    if (!acc.count(t.name)) order.push_back(t.name);
+    Acc& a = acc[t.name];
+    a.n += 1;
+    a.ms += ms;
+    a.bytes += t.bytes;
+    event_pool_.push_back(t.a);
+    event_pool_.push_back(t.b);
+  }
+  timed_.clear();
+  std::string out;
+  for (const std::string& k : order) {
+    const Acc& a = acc[k];
+    out += k + "\t" + std::to_string(a.n) + "\t" + std::to_string(a.ms) + "\t" + std::to_string(a.bytes) + "\n";
+  }
+  return out;
 }
 
 void Engine::flush() {
@@ -1037,7 +1104,7 @@ void Propagation::synchronize() {
   wf_->eng->check_nonfinite();
 }
 
-static const char* kind_name(int k) {
+const char* op_kind_name(int k) {
   switch (k) {
     case OP_DIAG1D: return "diag1d";
     case OP_DIAGND: return "diagnd";
@@ -1120,7 +1187,7 @@ std::string Propagation::describe() {
     if (a.lane_axis >= 0) axis = a.lane_axis;
     if (a.op.kind == OP_NORM || a.op.kind == OP_COPY || a.op.kind == OP_LOSS || a.op.kind == OP_SETC)
       written.push_back(a.op.a);
-    cur += kind_name(a.op.kind);
+    cur += op_kind_name(a.op.kind);
     if (a.lane_axis >= 0) cur += "@" + std::to_string(a.lane_axis);
     cur += " ";
     ++nops;

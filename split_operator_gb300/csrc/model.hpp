@@ -144,8 +144,23 @@ class Engine {
   std::vector<ScalarState*> bound;
   double* record_dev = nullptr;
 
+  // Per-pass device timing with CUDA events on the engine stream.
+  bool timing = false;
+  void timed_begin(const std::string& name);
+  void timed_end();
+  std::string collect_timing();  // "name\tlaunches\ttotal_ms\tbytes\n" lines; synchronizes and resets
+
  private:
   void launch(const std::vector<DevOp>& ops, int axis, bool resident, int repeat);
+  struct TimedLaunch {
+    std::string name;
+    cudaEvent_t a, b;
+    double bytes;
+  };
+  std::vector<TimedLaunch> timed_;
+  std::vector<cudaEvent_t> event_pool_;
+  cudaEvent_t take_event();
+  double pass_bytes(const std::vector<DevOp>& ops, const Geometry& g) const;
   DeviceBuffer slots_, partials_, counter_, staging_;
   size_t partials_cap_ = 0;
   std::vector<int> free_slots_;
@@ -357,6 +372,8 @@ class Propagation {
   std::string describe();
   void set_stream(cudaStream_t s) { wf_->eng->stream = s; }
   void synchronize();
+  void set_timing(bool on) { wf_->eng->timing = on; }
+  std::string kernel_times() { return wf_->eng->collect_timing(); }
 
   int precision;
 
