@@ -13,6 +13,8 @@
 // runs the program's scalar bookkeeping (loss accumulation, slot copies).
 #pragma once
 #include <cstdint>
+#include <cstring>
+#include <vector>
 #include <cuda_runtime.h>
 
 namespace so {
@@ -88,6 +90,14 @@ cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);
 cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s);
 size_t pass_smem_bytes(const Geometry& g, bool fp64);
 int pass_threads(const Geometry& g);
+
+// Tensor-core angular sweep (angular_tc.cu): FP32 state, real lane matrices as 3xTF32.
+constexpr int kTcColumns = 64;  // complex columns of the inner axis per CTA tile
+bool angular_tc_eligible(const Geometry& g);
+size_t angular_tc_smem_bytes(int n);
+void angular_tc_images(const double* m, int n, std::vector<float>& out);
+cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
+                              int error_slot, cudaStream_t s);
 
 // Auxiliary kernels (aux_kernels.cu)
 cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);

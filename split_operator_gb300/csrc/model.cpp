@@ -89,6 +89,7 @@ Engine::Engine(const std::vector<size_t>& shp, const std::vector<int>& prm, bool
   counter_ = DeviceBuffer(sizeof(unsigned int) * 4);
   cuda_check(cudaMemset(counter_.ptr, 0, sizeof(unsigned int) * 4), "cudaMemset");
   nonfinite_slot = alloc_slot(0.0);
+  timeout_slot = alloc_slot(0.0);
   int64_t max_tiles = 1;
   for (size_t a = 0; a < shape.size(); ++a) {
     try {
@@ -301,7 +302,52 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
   }
   c.version = version;
   c.real = real;
+  if (!fp64 && tc_tf32 && real && count == 1 && (n == 32 || n == 64 || n == 128)) {
+    std::vector<double> md(n * n);
+    for (size_t i = 0; i < n * n; ++i) md[i] = m[i].real();
+    std::vector<float> img;
+    angular_tc_images(md.data(), (int)n, img);
+    upload(c.tc_images, img, stream);
+    tc_images_by_matrix_[c.buf.ptr] = c.tc_images.as<float>();
+  }
   return c.buf.ptr;
+}
+
+bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& p) {
+  Geometry g = geometry(axis, false);
+  if (!angular_tc_eligible(g)) return false;
+  int mats[2], nmat = 0;
+  const float* images[2] = {nullptr, nullptr};
+  for (size_t i = 0; i < ops.size(); ++i) {
+    const int k = ops[i].kind;
+    if (k == OP_FFT || k == OP_MAT_LANE || k == OP_MAT_SLICE || k == OP_DOT) return false;
+    if (k == OP_MAT) {
+      if (nmat == 2 || !(ops[i].flags & 1)) return false;
+      auto it = tc_images_by_matrix_.find(ops[i].ptr);
+      if (it == tc_images_by_matrix_.end()) return false;
+      images[nmat] = it->second;
+      mats[nmat++] = (int)i;
+    }
+  }
+  if (nmat == 0) return false;
+  g.lanes_per_tile = kTcColumns;
+  g.tiles_per_outer = (int32_t)(g.inner / kTcColumns);
+  g.tiles = g.outer * g.tiles_per_outer;
+  p.g = g;
+  if ((size_t)g.tiles > partials_cap_) {
+    partials_cap_ = (size_t)g.tiles;
+    partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
+    p.partials = partials_.as<double>();
+  }
+  if (timing) {
+    std::string name = "f32 tc3xtf32 axis" + std::to_string(axis) + ":";
+    for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
+    timed_begin(name);
+    timed_.back().bytes = pass_bytes(ops, g);
+  }
+  cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, stream), "tensor-core pass launch");
+  if (timing) timed_end();
+  return true;
 }
 
 const double* Engine::weights(const Grid& g) {
@@ -373,6 +419,7 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   }
   p.nred = nred;
   if (fft) p.twiddle = twiddle((size_t)p.g.n);
+  if (!fp64 && tc_tf32 && !resident && try_launch_tc(ops, axis, p)) return;
   if (!resident && (size_t)p.g.tiles > partials_cap_) {
     partials_cap_ = (size_t)p.g.tiles;
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
@@ -497,6 +544,10 @@ void Engine::sync() {
 }
 
 void Engine::check_nonfinite() {
+  if (read_slot(timeout_slot) != 0.0) {
+    write_slot(timeout_slot, 0.0);
+    throw Error(SO_ERR_TIMEOUT, "a bounded device-side wait gave up (tensor-core pass)");
+  }
   if (read_slot(nonfinite_slot) != 0.0) {
     write_slot(nonfinite_slot, 0.0);
     throw Error(SO_ERR_NONFINITE, "a norm of the wave function is not finite");
@@ -869,17 +920,24 @@ void StateSaver::record_frame(WaveFunction& wf, size_t frame) {
 void StateSaver::reset() { data.assign(points * frames_no, 0.0); }
 
 // ------------------------------------------------------------------- Propagation
+// Storage order of a propagation's state: the FFT axis innermost (contiguous FFT
+// lanes); without an FFT, a lane-matrix axis outermost (strided lanes make the
+// matrix product a GEMM over contiguous columns).
 static std::vector<int> choose_perm(size_t ndim, const OperationStack& st) {
-  int fft_axis = -1;
-  for (const auto& e : st.stack)
-    if (auto* f = dynamic_cast<FFTTransformation*>(e.op.get())) {
-      fft_axis = (int)f->dimension_no;
-      break;
-    }
+  int fft_axis = -1, mat_axis = -1;
+  for (const auto& e : st.stack) {
+    if (auto* f = dynamic_cast<FFTTransformation*>(e.op.get()))
+      if (fft_axis < 0) fft_axis = (int)f->dimension_no;
+    if (auto* m = dynamic_cast<MatrixTransformation*>(e.op.get()))
+      if (mat_axis < 0) mat_axis = (int)m->dimension_no;
+  }
+  if (fft_axis >= (int)ndim) fft_axis = -1;
+  if (mat_axis >= (int)ndim || mat_axis == fft_axis) mat_axis = -1;
   std::vector<int> perm;
+  if (fft_axis < 0 && mat_axis >= 0) perm.push_back(mat_axis);
   for (size_t a = 0; a < ndim; ++a)
-    if ((int)a != fft_axis) perm.push_back((int)a);
-  if (fft_axis >= 0 && (size_t)fft_axis < ndim) perm.push_back(fft_axis);
+    if ((int)a != fft_axis && !(fft_axis < 0 && (int)a == mat_axis)) perm.push_back((int)a);
+  if (fft_axis >= 0) perm.push_back(fft_axis);
   return perm;
 }
 
@@ -888,6 +946,7 @@ Propagation::Propagation(WaveFunction& src, so_time_grid time, std::shared_ptr<O
   if (prec < SO_PRECISION_FP64 || prec > SO_PRECISION_FP32_SIMT) throw Error(SO_ERR_INVALID, "unknown precision");
   const bool fp64 = prec == SO_PRECISION_FP64;
   wf_ = std::make_unique<WaveFunction>(src.shape, src.grids, choose_perm(src.shape.size(), *stack_), fp64);
+  wf_->eng->tc_tf32 = prec == SO_PRECISION_FP32_TF32X3;
   wf_->last_grid_names = src.last_grid_names;
   wf_->possible_norm_change = src.possible_norm_change;
   wf_->eng->write_slot(wf_->cache_slot, src.eng->read_slot(src.cache_slot));

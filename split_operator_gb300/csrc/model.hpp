@@ -111,6 +111,8 @@ class Engine {
   DeviceBuffer psi;
   cudaStream_t stream = nullptr;
   int nonfinite_slot = 0;
+  int timeout_slot = 0;
+  bool tc_tf32 = false;  // real lane matrices on the tensor cores (3xTF32); FP32 state only
 
   size_t points() const;
   size_t elem_bytes() const { return fp64 ? 16 : 8; }
@@ -169,8 +171,11 @@ class Engine {
     uint64_t version;
     DeviceBuffer buf;
     bool real;
+    DeviceBuffer tc_images;  // 3xTF32 A-operand chunk images (tensor-core passes)
   };
   std::map<std::pair<const void*, int>, Cached> tables_;
+  std::map<const void*, const float*> tc_images_by_matrix_;
+  bool try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& p);
   std::map<uint64_t, DeviceBuffer> weights_;
   std::map<size_t, DeviceBuffer> twiddles_;
   // open pass
