@@ -37,7 +37,7 @@ constexpr int kChunkK = 32;         // K per A chunk
 constexpr int kChunkBytes = kM * kChunkK * 4;  // one of hi / lo
 constexpr int kLboB = 144;          // B: core matrices along K (16 B padding vs 128)
 constexpr int kStageRow = 132;      // output staging row stride in floats (528 B)
-constexpr uint32_t kWaitLimit = 1u << 26;
+constexpr uint64_t kWaitLimit = 2000000000ull;  // 2 s per wait
 constexpr int kThreads = 128;
 
 struct TcSmemLayout {
@@ -212,10 +212,8 @@ __global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_co
     if (total_chunks > 1) issue_chunk(1);
   }
 
-  // op segments: [0, mat0) pre, (mat0, mat1) mid, (mat1, nops) post
+  // ops before the first matrix run in the prologue, the others in the epilogue that follows their matrix
   const int seg_end0 = tp.mat_op[0];
-  const int seg_beg1 = tp.mat_op[0] + 1, seg_end1 = tp.nmat > 1 ? tp.mat_op[1] : p.nops;
-  const int seg_beg2 = tp.nmat > 1 ? tp.mat_op[1] + 1 : p.nops;
   double acc[kMaxRed];
 #pragma unroll
   for (int r = 0; r < kMaxRed; ++r) acc[r] = 0.0;
@@ -289,7 +287,8 @@ __global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_co
     }
     tc_fence_after();
     const bool last = m + 1 == tp.nmat;
-    const int sb = last ? seg_beg2 : seg_beg1, se = last ? p.nops : seg_end1;
+    // ops between this matrix and the next one (or the end of the program)
+    const int sb = tp.mat_op[m] + 1, se = last ? p.nops : tp.mat_op[m + 1];
     const int j = tid;  // row = TMEM lane
     const bool row_ok = j < n;
     float* stg = bhi;  // output staging reuses the B_hi area once the last GEMM is done

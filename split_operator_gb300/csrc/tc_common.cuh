@@ -36,11 +36,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
   return ok != 0;
 }
 
-// Bounded wait: false when `limit` polls passed without the phase completing.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit) {
-  for (uint32_t i = 0; i < limit; ++i)
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: false when `limit_ns` nanoseconds passed without the phase completing.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint64_t limit_ns) {
+  if (mbar_try_wait(bar, phase)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  while (true) {
     if (mbar_try_wait(bar, phase)) return true;
-  return false;
+    if (globaltimer_ns() - t0 > limit_ns) return false;
+  }
 }
 
 // 1-D bulk copy global -> shared completing on `bar` (byte count multiple of 16, both 16-byte aligned)
