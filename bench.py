@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--nth", type=int, default=128)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="timed region only (no e2e, accuracy or CPU legs): the case profiled under ncu")
     return ap.parse_args()
 
 
@@ -252,6 +254,11 @@ def run_ours(a):
                 "algorithmic_bytes_per_launch": b / n, "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
                 "share_of_step": tms / ms if ms > 0 else None}
 
+    if a.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms_max / a.steps,
+                              "quick": True, "passes": [list(t) for t in kt]}), flush=True)
+        return
     # end to end through the C ABI: pinned host input -> device, one step, device -> pinned host
     host_in = torch.empty(points * 2, dtype=torch.float64).pin_memory()
     host_out = torch.empty(points * 2, dtype=torch.float64).pin_memory()
