@@ -266,6 +266,26 @@ int so_propagation_describe(so_propagation p, char* buf, size_t cap);
  * and clears the record. */
 int so_propagation_set_timing(so_propagation p, int enabled);
 int so_propagation_kernel_times(so_propagation p, char* buf, size_t cap);
+
+/* ---- Allocation-free lane FFT + norm (no counterpart in the reference) ----
+ * For callers that must not allocate GPU memory, or let a library allocate it, while
+ * they run: code inside a strict device memory pool, or a host framework that hands
+ * over only pre-sized buffers.  Every pointer is the caller's device memory.
+ * In place on psi (complex128, `lanes` contiguous lanes of `n` points, row-major):
+ * the unitary DFT of every lane (direction -1 = FFTTransformation::transform, +1 =
+ * inverse_transform, fft_transformation.rs:53-88), then, when `weights` is given,
+ * *norm_out = sum |psi|^2 lane_weights[l] weights[x] (WaveFunction::norm with the
+ * grids' weights, wave_function.rs:68-85); `lane_weights`, `weights`, `norm_out` are
+ * all given or all NULL.  Issued on `stream` (cudaStream_t; NULL = legacy stream).
+ * Limits: n <= 4096 and at most 65536 CTAs of lanes (SO_ERR_UNSUPPORTED beyond).
+ * The kernel's scratch (norm partials, a ticket counter) and the twiddle table are
+ * fixed file-scope device arrays (about 0.6 MiB, held by every GPU that loads the
+ * library until exit); no cudaMalloc / cudaFree is called.  The first call on a
+ * device looks up those arrays' device addresses: make it before any stream
+ * capture.  All calls share the arrays, which keep the last call's contents: calls
+ * that overlap on the GPU (other streams, other threads) race. */
+int so_fft_norm_noalloc(double* psi, size_t lanes, size_t n, int direction, const double* lane_weights,
+                        const double* weights, double* norm_out, void* stream);
 void so_propagation_free(so_propagation p);
 
 #if defined(__GNUC__)

@@ -129,6 +129,7 @@ SIGNATURES = {
     "so_propagation_describe": [_P, C.c_char_p, _S],
     "so_propagation_set_timing": [_P, _I],
     "so_propagation_kernel_times": [_P, C.c_char_p, _S],
+    "so_fft_norm_noalloc": [_P, _S, _S, _I, _P, _P, _P, _P],
 }
 VOID = {
     "so_grid_free": [_P],

@@ -89,6 +89,10 @@ T* as(so_operator o) {
 
 }  // namespace
 
+namespace so {
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace so
+
 extern "C" {
 
 const char* so_last_error(void) { return g_err.c_str(); }
