@@ -409,7 +409,11 @@ void angular_tc_images(const double* m, int n, std::vector<float>& out) {
         b = (b + 0x1000u) & 0xFFFFE000u;
         float h;
         std::memcpy(&h, &b, 4);
-        const float l = (float)(v - (double)h);
+        // remainder rounded to tf32 as well (the tensor core would truncate it)
+        float l = (float)(v - (double)h);
+        std::memcpy(&b, &l, 4);
+        b = (b + 0x1000u) & 0xFFFFE000u;
+        std::memcpy(&l, &b, 4);
         const size_t off = (size_t)(r >> 3) * 256 + (size_t)(kk >> 2) * 32 + (size_t)(r & 7) * 4 + (kk & 3);
         hi[off] = h;
         lo[off] = l;

@@ -121,11 +121,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// fp32 -> (tf32-exact hi, fp32 remainder lo), hi rounded to nearest
+__device__ __forceinline__ float round_tf32(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+// fp32 -> hi + lo with both parts exact in tf32 (each rounded to nearest).  The
+// tensor core reads only the top 19 bits of an fp32 operand; an unrounded
+// remainder would be truncated there, which biases every product toward zero.
 __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
-  const uint32_t b = __float_as_uint(x);
-  hi = __uint_as_float((b + 0x1000u) & 0xFFFFE000u);
-  lo = x - hi;
+  hi = round_tf32(x);
+  lo = round_tf32(x - hi);
 }
 
 }  // namespace tc

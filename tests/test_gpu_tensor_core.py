@@ -38,6 +38,29 @@ def test_real_lane_matrix_3xtf32_matches_fp64(so, n, nr):
     assert err2 < 4e-6, err2
 
 
+@pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_simt"])
+def test_orthogonal_lane_matrix_keeps_the_norm(so, precision):
+    """200 applications of an orthogonal matrix: the norm may random-walk at the FP32
+    level but must not drift systematically (a biased split would shrink it)."""
+    n, nr = 128, 512
+    rng = np.random.default_rng(7)
+    q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    psi = rng.standard_normal((nr, n)) + 1j * rng.standard_normal((nr, n))
+    psi /= np.linalg.norm(psi)
+    g0 = so.Grid.new_linear_countable("r", 0.0, float(nr - 1), nr, 0)
+    g1 = so.Grid.new_linear_countable("th", 0.0, float(n - 1), n, 1)
+    wf = so.WaveFunction(psi, [g0, g1])
+    mt = so.MatrixTransformation(g1, so.Grid.new_linear_countable("l", 0.0, float(n - 1), n, 1))
+    mt.set_diagonalization_matrix(q.astype(np.complex128), q.T.astype(np.complex128))
+    st = so.OperationStack()
+    st.add_transformation(mt, so.NORMAL)
+    prop = so.Propagation(wf, so.TimeGrid(1.0, 200), st, precision)
+    prop.steps(200)
+    a = prop.get_array()
+    drift = abs(np.linalg.norm(a) ** 2 - 1.0)
+    assert drift < 2e-5, drift
+
+
 def test_tensor_core_pass_is_used(so):
     from split_operator_gb300 import workloads as W
     prop, _ = W.radial_angular_2d(nr=256, nth=32, step_no=4, r0=25.0, precision="fp32_tf32x3")
