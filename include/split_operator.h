@@ -267,6 +267,24 @@ int so_propagation_describe(so_propagation p, char* buf, size_t cap);
 int so_propagation_set_timing(so_propagation p, int enabled);
 int so_propagation_kernel_times(so_propagation p, char* buf, size_t cap);
 
+/* ---- Batched propagation (no counterpart in the reference, which runs one
+ * Propagation at a time) ----
+ * Steps many independent propagations together: each pass of the steady-state step
+ * becomes one launch per kernel / shape class covering every instance's tiles, and
+ * the repeated part is replayed from a captured CUDA graph.  The propagations keep
+ * their own state (so_propagation_get_array, losses, norms stay valid) and must share
+ * the step's pass structure (same operator stack kinds); savers are not allowed.
+ * Work is issued on the first propagation's stream. */
+typedef struct so_batch_t* so_batch;
+int so_batch_new(const so_propagation* props, size_t count, so_batch* out);
+/* `steps` steps of every propagation (Propagation::step, propagation.rs:134-182) */
+int so_batch_steps(so_batch b, uint64_t steps);
+int so_batch_set_timing(so_batch b, int enabled);
+int so_batch_kernel_times(so_batch b, char* buf, size_t cap);
+/* launches of the repeated part of one step (after the first) */
+int so_batch_launches_per_step(so_batch b, size_t* out);
+void so_batch_free(so_batch b);
+
 /* ---- Allocation-free lane FFT + norm (no counterpart in the reference) ----
  * For callers that must not allocate GPU memory, or let a library allocate it, while
  * they run: code inside a strict device memory pool, or a host framework that hands

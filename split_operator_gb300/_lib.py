@@ -130,6 +130,11 @@ SIGNATURES = {
     "so_propagation_set_timing": [_P, _I],
     "so_propagation_kernel_times": [_P, C.c_char_p, _S],
     "so_fft_norm_noalloc": [_P, _S, _S, _I, _P, _P, _P, _P],
+    "so_batch_new": [_PP, _S, _PP],
+    "so_batch_steps": [_P, C.c_uint64],
+    "so_batch_set_timing": [_P, _I],
+    "so_batch_kernel_times": [_P, C.c_char_p, _S],
+    "so_batch_launches_per_step": [_P, _SP],
 }
 VOID = {
     "so_grid_free": [_P],
@@ -137,6 +142,7 @@ VOID = {
     "so_operator_free": [_P],
     "so_operation_stack_free": [_P],
     "so_propagation_free": [_P],
+    "so_batch_free": [_P],
 }
 OTHER = {"so_last_error": ([], C.c_char_p)}
 

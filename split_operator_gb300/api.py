@@ -655,6 +655,37 @@ class Propagation(_Handle):
         return out
 
 
+class Batch(_Handle):
+    """Many independent propagations stepped together (batched launches, CUDA graph)."""
+
+    _free = "so_batch_free"
+
+    def __init__(self, propagations: Sequence[Propagation]):
+        arr = (C.c_void_p * len(propagations))(*[p.handle for p in propagations])
+        super().__init__(_new("so_batch_new", C.cast(arr, C.POINTER(C.c_void_p)), len(propagations)))
+        self._props = list(propagations)
+
+    def steps(self, n: int):
+        call("so_batch_steps", self._h, n)
+
+    def set_timing(self, enabled: bool):
+        call("so_batch_set_timing", self._h, 1 if enabled else 0)
+
+    def kernel_times(self):
+        buf = C.create_string_buffer(1 << 18)
+        call("so_batch_kernel_times", self._h, buf, 1 << 18)
+        out = []
+        for line in buf.value.decode().splitlines():
+            name, n, ms, b = line.split("\t")
+            out.append((name, int(n), float(ms), float(b)))
+        return out
+
+    def launches_per_step(self) -> int:
+        v = C.c_size_t()
+        call("so_batch_launches_per_step", self._h, C.byref(v))
+        return v.value
+
+
 def launch_count() -> int:
     v = C.c_uint64()
     call("so_launch_count", C.byref(v))

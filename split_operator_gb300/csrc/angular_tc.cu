@@ -150,7 +150,7 @@ struct TcParams {
   int32_t error_slot;
 };
 
-__global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_constant__ TcParams tp) {
+__device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) {
   using namespace tc;
   const PassParams& p = tp.p;
   const Geometry& g = p.g;
@@ -175,7 +175,6 @@ __global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_co
   const int nk = (n + kChunkK - 1) / kChunkK;
   const int total_chunks = nk * tp.nmat;
 
-  const int64_t tile = blockIdx.x;
   const int64_t o = tile / g.tiles_per_outer;
   const int64_t i0 = (tile - o * g.tiles_per_outer) * kBN;
   const int64_t base = o * g.n * g.inner + i0;  // element (row 0, column 0) of the tile
@@ -382,8 +381,60 @@ __global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_co
   if (warp == 0) tmem_dealloc(tmem, 256);
 }
 
+__global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_constant__ TcParams tp) {
+  tc_tile(tp, blockIdx.x);
+}
+
+// Many propagations' lane-matrix passes in one launch: block b runs tile
+// (b - offsets[i]) of params[i], offsets[i] <= b < offsets[i + 1].
+__global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel_batched(const TcParams* __restrict__ params,
+                                                                        const int64_t* __restrict__ offsets,
+                                                                        int count) {
+  const int64_t b = blockIdx.x;
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (offsets[mid] <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  tc_tile(params[lo], b - offsets[lo]);
+}
+
 // ------------------------------------------------------------------ host side
 size_t angular_tc_smem_bytes(int n) { return tc_layout(n).total; }
+
+size_t tc_params_bytes() { return sizeof(TcParams); }
+
+void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
+                    void* out) {
+  TcParams tp{};
+  tp.p = p;
+  tp.nmat = nmat;
+  for (int i = 0; i < nmat; ++i) {
+    tp.mat_op[i] = mat_op[i];
+    tp.images[i] = images[i];
+  }
+  tp.error_slot = error_slot;
+  std::memcpy(out, &tp, sizeof(TcParams));
+}
+
+cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,
+                                      size_t smem, cudaStream_t s) {
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e =
+        cudaFuncSetAttribute(angular_tc_kernel_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  if (smem > 220 * 1024) return cudaErrorInvalidValue;
+  angular_tc_kernel_batched<<<(unsigned)blocks, kThreads, smem, s>>>(reinterpret_cast<const TcParams*>(params_dev),
+                                                                     offsets_dev, count);
+  count_launch();
+  return cudaGetLastError();
+}
 
 bool angular_tc_eligible(const Geometry& g) {
   return (g.n == 32 || g.n == 64 || g.n == 128) && g.inner >= kBN && g.inner % kBN == 0;

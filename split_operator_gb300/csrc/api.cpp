@@ -24,6 +24,9 @@ struct so_operation_stack_t {
 struct so_propagation_t {
   std::unique_ptr<so::Propagation> p;
 };
+struct so_batch_t {
+  std::unique_ptr<so::Batch> b;
+};
 
 namespace {
 thread_local std::string g_err;
@@ -922,5 +925,42 @@ int so_propagation_kernel_times(so_propagation p, char* buf, size_t cap) {
   });
 }
 void so_propagation_free(so_propagation p) { delete p; }
+
+int so_batch_new(const so_propagation* props, size_t count, so_batch* out) {
+  return guard([&] {
+    need(props && out && count > 0, "null argument");
+    std::vector<so::Propagation*> ps;
+    for (size_t i = 0; i < count; ++i) {
+      need(props[i] != nullptr, "null propagation");
+      ps.push_back(props[i]->p.get());
+    }
+    *out = new so_batch_t{std::make_unique<so::Batch>(ps)};
+  });
+}
+int so_batch_steps(so_batch b, uint64_t steps) {
+  return guard([&] {
+    need(b, "null argument");
+    b->b->steps(steps);
+  });
+}
+int so_batch_set_timing(so_batch b, int enabled) {
+  return guard([&] {
+    need(b, "null argument");
+    b->b->set_timing(enabled != 0);
+  });
+}
+int so_batch_kernel_times(so_batch b, char* buf, size_t cap) {
+  return guard([&] {
+    need(b && buf && cap > 0, "null argument");
+    std::snprintf(buf, cap, "%s", b->b->kernel_times().c_str());
+  });
+}
+int so_batch_launches_per_step(so_batch b, size_t* out) {
+  return guard([&] {
+    need(b && out, "null argument");
+    *out = b->b->launches_per_step();
+  });
+}
+void so_batch_free(so_batch b) { delete b; }
 
 }  // extern "C"

@@ -99,6 +99,15 @@ void angular_tc_images(const double* m, int n, std::vector<float>& out);
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
                               int error_slot, cudaStream_t s);
 
+// Batched launches over many propagations' passes (block -> (instance, tile) by offsets)
+cudaError_t launch_pass_batched(bool fp64, const PassParams* params_dev, const int64_t* offsets_dev, int count,
+                                int64_t blocks, int threads, size_t smem, cudaStream_t s);
+size_t tc_params_bytes();
+void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
+                    void* out);
+cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,
+                                      size_t smem, cudaStream_t s);
+
 // Auxiliary kernels (aux_kernels.cu)
 cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);
 // dst (storage order, precision of dst) <- src (logical row-major complex128)

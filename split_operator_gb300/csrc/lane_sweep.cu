@@ -311,7 +311,7 @@ __device__ void run_scalar(const PassParams& p, const DevOp& op, const double* t
 }
 
 template <typename R, int RMAX>
-__global__ void __launch_bounds__(512) pass_kernel(const __grid_constant__ PassParams p) {
+__device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t tile) {
   using C = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Geometry& g = p.g;
@@ -334,7 +334,6 @@ __global__ void __launch_bounds__(512) pass_kernel(const __grid_constant__ PassP
   __shared__ double totals[kMaxRed];
   __shared__ int s_last;
 
-  const int64_t tile = blockIdx.x;
   const bool pow2 = (n & (n - 1)) == 0;
   const int lg = pow2 ? __ffs(n) - 1 : 0;
 
@@ -549,6 +548,50 @@ __global__ void __launch_bounds__(512) pass_kernel(const __grid_constant__ PassP
     __threadfence();
     *p.counter = 0u;
   }
+}
+
+template <typename R, int RMAX>
+__global__ void __launch_bounds__(512) pass_kernel(const __grid_constant__ PassParams p) {
+  pass_tile<R, RMAX>(p, blockIdx.x);
+}
+
+// Many propagations' passes in one launch: block b runs tile (b - offsets[i]) of
+// params[i], offsets[i] <= b < offsets[i + 1].
+template <typename R, int RMAX>
+__global__ void __launch_bounds__(512) pass_kernel_batched(const PassParams* __restrict__ params,
+                                                           const int64_t* __restrict__ offsets, int count) {
+  const int64_t b = blockIdx.x;
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (offsets[mid] <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  pass_tile<R, RMAX>(params[lo], b - offsets[lo]);
+}
+
+template <typename R, int RMAX>
+static cudaError_t launch_batched_impl(const PassParams* params_dev, const int64_t* offsets_dev, int count,
+                                       int64_t blocks, int threads, size_t smem, cudaStream_t s) {
+  auto kern = pass_kernel_batched<R, RMAX>;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  if (smem > 200 * 1024 || threads > 512) return cudaErrorInvalidValue;
+  kern<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pass_batched(bool fp64, const PassParams* params_dev, const int64_t* offsets_dev, int count,
+                                int64_t blocks, int threads, size_t smem, cudaStream_t s) {
+  return fp64 ? launch_batched_impl<double, 8>(params_dev, offsets_dev, count, blocks, threads, smem, s)
+              : launch_batched_impl<float, 16>(params_dev, offsets_dev, count, blocks, threads, smem, s);
 }
 
 size_t pass_smem_bytes(const Geometry& g, bool fp64) {

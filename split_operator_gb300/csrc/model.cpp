@@ -339,9 +339,16 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
     p.partials = partials_.as<double>();
   }
+  std::string name = "f32 tc3xtf32 axis" + std::to_string(axis) + ":";
+  for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
+  if (recording) {
+    RecordedPass r{RecordedPass::TensorCore, false, p, std::vector<unsigned char>(tc_params_bytes()), 128,
+                   angular_tc_smem_bytes((int)g.n), name, pass_bytes(ops, g)};
+    make_tc_params(p, mats, nmat, images, timeout_slot, r.tcp.data());
+    recording->push_back(std::move(r));
+    return true;
+  }
   if (timing) {
-    std::string name = "f32 tc3xtf32 axis" + std::to_string(axis) + ":";
-    for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
     timed_begin(name);
     timed_.back().bytes = pass_bytes(ops, g);
   }
@@ -383,6 +390,12 @@ void Engine::submit(const Action& a) {
   }
   const int need = k == OP_NORM ? 1 : (k == OP_DOT ? 2 : 0);
   if ((int)cur_.size() >= kMaxOps || cur_red_ + need > kMaxRed) flush();
+  if (k == OP_MAT && tc_tf32) {
+    // the tensor-core pass holds at most two lane-matrix products
+    int mats = 0;
+    for (const DevOp& o : cur_) mats += o.kind == OP_MAT;
+    if (mats >= 2) flush();
+  }
   if (a.lane_axis >= 0) cur_axis_ = a.lane_axis;
   DevOp op = a.op;
   if (need) {
@@ -425,10 +438,16 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
     p.partials = partials_.as<double>();
   }
+  std::string name = std::string(fp64 ? "f64" : "f32") + (resident ? " resident" : " sweep") + " axis" +
+                     std::to_string(axis) + ":";
+  for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
+  if (recording) {
+    RecordedPass r{resident ? RecordedPass::Resident : RecordedPass::Generic, fp64, p, {},
+                   pass_threads(p.g), pass_smem_bytes(p.g, fp64), name, pass_bytes(ops, p.g)};
+    recording->push_back(std::move(r));
+    return;
+  }
   if (timing) {
-    std::string name = std::string(fp64 ? "f64" : "f32") + (resident ? " resident" : " sweep") + " axis" +
-                       std::to_string(axis) + ":";
-    for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
     timed_begin(name);
     timed_.back().bytes = pass_bytes(ops, p.g);
   }
@@ -509,6 +528,10 @@ void Engine::flush() {
     p.record = record_dev;
     p.nops = (int)ops.size();
     for (size_t i = 0; i < ops.size(); ++i) p.ops[i] = ops[i];
+    if (recording) {
+      recording->push_back(RecordedPass{RecordedPass::Scalar, fp64, p, {}, 32, 0, "scalar", 0.0});
+      return;
+    }
     cuda_check(launch_scalar_program(p, stream), "scalar launch");
     return;
   }
@@ -1161,6 +1184,198 @@ double Propagation::norm() {
 void Propagation::synchronize() {
   wf_->eng->sync();
   wf_->eng->check_nonfinite();
+}
+
+bool Propagation::has_savers() const {
+  for (const auto& e : stack_->stack)
+    if (e.op->cls == OpClass::Saver) return true;
+  return false;
+}
+
+std::vector<RecordedPass> Propagation::record_steps(uint64_t n) {
+  Engine& e = *wf_->eng;
+  e.flush();
+  std::vector<RecordedPass> out;
+  e.recording = &out;
+  try {
+    Emitter em{&e};
+    for (uint64_t i = 0; i < n; ++i) step(em);
+    e.flush();
+  } catch (...) {
+    e.recording = nullptr;
+    throw;
+  }
+  e.recording = nullptr;
+  return out;
+}
+
+// ------------------------------------------------------------------------ Batch
+static bool same_params(const RecordedPass& a, const RecordedPass& b) {
+  if (a.kind != b.kind) return false;
+  if (a.kind == RecordedPass::TensorCore) return a.tcp == b.tcp;
+  return std::memcmp(&a.p, &b.p, sizeof(PassParams)) == 0;
+}
+
+Batch::Batch(std::vector<Propagation*> props) : props_(std::move(props)) {
+  if (props_.empty()) throw Error(SO_ERR_INVALID, "empty batch");
+  for (Propagation* p : props_) {
+    if (p->has_savers()) throw Error(SO_ERR_UNSUPPORTED, "batched propagations cannot carry savers");
+    if (p->engine().resident_capable())
+      throw Error(SO_ERR_UNSUPPORTED, "batched propagations need multi-lane (2-D or larger) states");
+  }
+  stream_ = props_[0]->engine().stream;
+}
+
+Batch::~Batch() {
+  for (Timed& t : timed_) {
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+  }
+}
+
+std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<RecordedPass>>& rec, size_t pos) {
+  // group key: kind, precision, threads, shared memory
+  std::map<std::tuple<int, int, int, size_t>, std::vector<const RecordedPass*>> by;
+  for (const auto& r : rec) {
+    const RecordedPass& rp = r[pos];
+    if (rp.kind == RecordedPass::Scalar || rp.kind == RecordedPass::Resident)
+      throw Error(SO_ERR_UNSUPPORTED, "pass kind cannot be batched");
+    by[{(int)rp.kind, rp.fp64 ? 1 : 0, rp.threads, rp.smem}].push_back(&rp);
+  }
+  std::vector<Group> out;
+  for (auto& kv : by) {
+    const auto& v = kv.second;
+    Group g{};
+    g.kind = v[0]->kind;
+    g.fp64 = v[0]->fp64;
+    g.threads = v[0]->threads;
+    g.smem = v[0]->smem;
+    g.count = (int)v.size();
+    g.name = "batched " + std::to_string(v.size()) + "x " + v[0]->name;
+    std::vector<int64_t> off(v.size() + 1, 0);
+    const size_t pb = g.kind == RecordedPass::TensorCore ? tc_params_bytes() : sizeof(PassParams);
+    std::vector<unsigned char> params(pb * v.size());
+    g.bytes = 0.0;
+    for (size_t i = 0; i < v.size(); ++i) {
+      off[i + 1] = off[i] + v[i]->p.g.tiles;
+      if (g.kind == RecordedPass::TensorCore)
+        std::memcpy(params.data() + i * pb, v[i]->tcp.data(), pb);
+      else
+        std::memcpy(params.data() + i * pb, &v[i]->p, pb);
+      g.bytes += v[i]->bytes;
+    }
+    g.blocks = off.back();
+    g.params = DeviceBuffer(params.size());
+    g.offsets = DeviceBuffer(off.size() * sizeof(int64_t));
+    cuda_check(cudaMemcpy(g.params.ptr, params.data(), params.size(), cudaMemcpyHostToDevice), "batch params");
+    cuda_check(cudaMemcpy(g.offsets.ptr, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice),
+               "batch offsets");
+    out.push_back(std::move(g));
+  }
+  return out;
+}
+
+void Batch::run_groups(std::vector<Group>& gs) {
+  for (Group& g : gs) {
+    Timed t{};
+    if (timing_) {
+      t.name = g.name;
+      t.bytes = g.bytes;
+      cuda_check(cudaEventCreate(&t.a), "event");
+      cuda_check(cudaEventCreate(&t.b), "event");
+      cuda_check(cudaEventRecord(t.a, stream_), "event record");
+    }
+    if (g.kind == RecordedPass::TensorCore)
+      cuda_check(launch_angular_tc_batched(g.params.ptr, g.offsets.as<int64_t>(), g.count, g.blocks, g.smem, stream_),
+                 "batched tensor-core pass");
+    else
+      cuda_check(launch_pass_batched(g.fp64, g.params.as<PassParams>(), g.offsets.as<int64_t>(), g.count, g.blocks,
+                                     g.threads, g.smem, stream_),
+                 "batched pass");
+    if (timing_) {
+      cuda_check(cudaEventRecord(t.b, stream_), "event record");
+      timed_.push_back(t);
+    }
+  }
+}
+
+void Batch::steps(uint64_t n) {
+  if (n == 0) return;
+  for (Propagation* p : props_) p->engine().sync();
+  // Host logic of two steps per propagation: passes [head, period..., tail] where the
+  // period (the middle passes) repeats for every further step.
+  std::vector<std::vector<RecordedPass>> rec;
+  for (Propagation* p : props_) rec.push_back(p->record_steps(2));
+  const size_t np = rec[0].size();
+  for (const auto& r : rec)
+    if (r.size() != np || np < 2)
+      throw Error(SO_ERR_UNSUPPORTED, "propagations of a batch must share the pass structure of the step");
+  // Two recorded steps give either
+  //   odd  np = 2m + 1: [head] [period: m passes] [tail: m passes], the last period pass being the
+  //        one where a step's end and the next step's start share a pass; tail == period except
+  //        for that last pass.  n steps = head, period x (n - 1), tail.
+  //   even np = 2m: [step 1: m passes] [step 2: m passes]; n steps = step 1, step 2 x (n - 1).
+  const bool merged = np % 2 == 1;
+  const size_t m = merged ? (np - 1) / 2 : np / 2;
+  const size_t per0 = merged ? 1 : m;  // first pass of the repeated period
+  for (const auto& r : rec)
+    for (size_t i = (merged ? 1 : 1); i < m; ++i)
+      if (!same_params(r[merged ? i : i], r[merged ? m + i : m + i]))
+        throw Error(SO_ERR_UNSUPPORTED, "step program is not periodic; run these propagations one by one");
+  std::vector<std::vector<Group>> pos(np);
+  for (size_t i = 0; i < np; ++i) pos[i] = build_groups(rec, i);
+  launches_per_step_ = 0;
+  for (size_t i = per0; i < per0 + m; ++i) launches_per_step_ += pos[i].size();
+  // first step (head)
+  for (size_t i = 0; i < (merged ? 1 : m); ++i) run_groups(pos[i]);
+  // the period once per further step, captured once as a CUDA graph when timing is off
+  const uint64_t reps = n - 1;
+  if (reps > 0) {
+    if (!timing_ && reps >= 4) {
+      cudaGraph_t graph;
+      cudaGraphExec_t exec;
+      cuda_check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
+      for (size_t i = per0; i < per0 + m; ++i) run_groups(pos[i]);
+      cuda_check(cudaStreamEndCapture(stream_, &graph), "end capture");
+      cuda_check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
+      for (uint64_t r = 0; r < reps; ++r) cuda_check(cudaGraphLaunch(exec, stream_), "graph launch");
+      count_launch(launches_per_step_ * (reps - 1));  // the capture counted the period once
+      cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(graph);
+    } else {
+      for (uint64_t r = 0; r < reps; ++r)
+        for (size_t i = per0; i < per0 + m; ++i) run_groups(pos[i]);
+    }
+  }
+  // tail: the last step's closing passes (merged form only)
+  if (merged)
+    for (size_t i = m + 1; i < np; ++i) run_groups(pos[i]);
+  cuda_check(cudaStreamSynchronize(stream_), "batch sync");
+}
+
+std::string Batch::kernel_times() {
+  cuda_check(cudaStreamSynchronize(stream_), "batch sync");
+  std::map<std::string, std::tuple<int, double, double>> acc;
+  std::vector<std::string> order;
+  for (Timed& t : timed_) {
+    float ms = 0.f;
+    cuda_check(cudaEventElapsedTime(&ms, t.a, t.b), "event elapsed");
+    if (!acc.count(t.name)) order.push_back(t.name);
+    auto& a = acc[t.name];
+    std::get<0>(a) += 1;
+    std::get<1>(a) += ms;
+    std::get<2>(a) += t.bytes;
+    cudaEventDestroy(t.a);
+    cudaEventDestroy(t.b);
+  }
+  timed_.clear();
+  std::string out;
+  for (const std::string& k : order) {
+    const auto& a = acc[k];
+    out += k + "\t" + std::to_string(std::get<0>(a)) + "\t" + std::to_string(std::get<1>(a)) + "\t" +
+           std::to_string(std::get<2>(a)) + "\n";
+  }
+  return out;
 }
 
 const char* op_kind_name(int k) {

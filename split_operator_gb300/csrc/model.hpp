@@ -100,6 +100,18 @@ struct Action {
   int host_call = -1;
 };
 
+// A pass captured instead of launched (batched execution of many propagations).
+struct RecordedPass {
+  enum Kind { Generic, TensorCore, Scalar, Resident } kind;
+  bool fp64;
+  PassParams p;
+  std::vector<unsigned char> tcp;  // TcParams bytes (TensorCore)
+  int threads;
+  size_t smem;
+  std::string name;
+  double bytes;
+};
+
 class Engine {
  public:
   Engine(const std::vector<size_t>& shape, const std::vector<int>& perm, bool fp64);
@@ -145,6 +157,9 @@ class Engine {
 
   std::vector<ScalarState*> bound;
   double* record_dev = nullptr;
+
+  // When set, passes are appended here instead of being launched.
+  std::vector<RecordedPass>* recording = nullptr;
 
   // Per-pass device timing with CUDA events on the engine stream.
   bool timing = false;
@@ -379,6 +394,10 @@ class Propagation {
   void synchronize();
   void set_timing(bool on) { wf_->eng->timing = on; }
   std::string kernel_times() { return wf_->eng->collect_timing(); }
+  Engine& engine() { return *wf_->eng; }
+  // Run the host logic of `n` steps, capturing the passes instead of launching them.
+  std::vector<RecordedPass> record_steps(uint64_t n);
+  bool has_savers() const;
 
   int precision;
 
@@ -388,6 +407,44 @@ class Propagation {
   so_time_grid time_;
   std::shared_ptr<OperationStack> stack_;
   std::vector<std::shared_ptr<Operator>> keep_;
+};
+
+// Many independent propagations stepped together: every pass position of the
+// steady-state step becomes a few batched launches (one per kernel / shape class)
+// covering all instances; the periodic part is captured once as a CUDA graph.
+class Batch {
+ public:
+  explicit Batch(std::vector<Propagation*> props);
+  ~Batch();
+  void steps(uint64_t n);
+  void set_timing(bool on) { timing_ = on; }
+  std::string kernel_times();
+  size_t launches_per_step() const { return launches_per_step_; }
+
+ private:
+  struct Group {
+    RecordedPass::Kind kind;
+    bool fp64;
+    int threads;
+    size_t smem;
+    int64_t blocks;
+    int count;
+    DeviceBuffer params, offsets;
+    std::string name;
+    double bytes;
+  };
+  std::vector<Group> build_groups(const std::vector<std::vector<RecordedPass>>& rec, size_t pos);
+  void run_groups(std::vector<Group>& gs);
+  std::vector<Propagation*> props_;
+  cudaStream_t stream_ = nullptr;
+  bool timing_ = false;
+  size_t launches_per_step_ = 0;
+  struct Timed {
+    std::string name;
+    cudaEvent_t a, b;
+    double bytes;
+  };
+  std::vector<Timed> timed_;
 };
 
 }  // namespace so

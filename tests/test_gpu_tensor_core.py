@@ -39,6 +39,41 @@ def test_real_lane_matrix_3xtf32_matches_fp64(so, n, nr):
 
 
 @pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_simt"])
+@pytest.mark.parametrize("n", [128, 64])
+def test_two_lane_matrices_in_one_pass(so, precision, n):
+    """Stack [T-transformation, diagonal D]: a step is T, D, T2 (the inverse slot holds T2),
+    so the pass carries two matrix products with a table multiply between them."""
+    nr = 256
+    rng = np.random.default_rng(n)
+    t1 = rng.standard_normal((n, n)) / np.sqrt(n)
+    t2 = rng.standard_normal((n, n)) / np.sqrt(n)
+    d = np.exp(1j * rng.uniform(0, 6.28, (nr, n)))
+    psi = rng.standard_normal((nr, n)) + 1j * rng.standard_normal((nr, n))
+    g0 = so.Grid.new_linear_countable("r", 0.0, float(nr - 1), nr, 0)
+    g1 = so.Grid.new_linear_countable("th", 0.0, float(n - 1), n, 1)
+    wf = so.WaveFunction(psi, [g0, g1])
+    mt = so.MatrixTransformation(g1, so.Grid.new_linear_countable("l", 0.0, float(n - 1), n, 1))
+    mt.set_diagonalization_matrix(t1.astype(np.complex128), t2.astype(np.complex128))
+    dp = so.NDimPropagator()
+    dp.set_operator(d)
+    st = so.OperationStack()
+    st.add_transformation(mt, so.NORMAL)
+    st.add_propagator(dp)
+    prop = so.Propagation(wf, so.TimeGrid(1.0, 10), st, precision)
+    ref = psi.copy()
+    for k in range(3):
+        prop.steps(1)
+        ref = ((d * (ref @ t1.T)) @ t2.T)
+        err = rel_l2(prop.get_array(), ref)
+        assert err < 5e-6, (k, err)
+    prop.steps(3)  # passes merge across step boundaries: T2 then T in one pass
+    for _ in range(3):
+        ref = ((d * (ref @ t1.T)) @ t2.T)
+    err = rel_l2(prop.get_array(), ref)
+    assert err < 1e-5, err
+
+
+@pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_simt"])
 def test_orthogonal_lane_matrix_keeps_the_norm(so, precision):
     """200 applications of an orthogonal matrix: the norm may random-walk at the FP32
     level but must not drift systematically (a biased split would shrink it)."""
