@@ -7,13 +7,17 @@
 // and around them (n_dim_propagator.rs:32-36, one_dim_propagator.rs:37-46,
 // border_dumping.rs:57-93, wave_function.rs:68-85).
 //
-// Layout: the state is stored [outer][n][inner] (n = lane axis, e.g. theta, 32..128;
-// inner = radial points).  A CTA owns a tile of kBN = 64 complex columns of the inner
-// axis for all n rows.  Treating (re, im) as two real columns, each lane matrix
-// product is a real GEMM D[128 x 128] = A[128 x n] . B[n x 128] with A the (zero-
-// padded) matrix and B the tile.  3xTF32: A = A_hi + A_lo (split once from the FP64
-// matrix on the host), B = B_hi + B_lo (split on the fly), D = A_hi B_hi + A_hi B_lo
-// + A_lo B_hi accumulated in FP32 in tensor memory.
+// Layout: the state is stored [outer][n][inner] (n = lane axis, e.g. theta; inner =
+// radial points).  A CTA owns a tile of BN complex columns of the inner axis for all
+// n rows.  Treating (re, im) as two real columns, a lane-matrix product is the real
+// GEMM D[M x 2BN] = A[M x n] . B[n x 2BN], A the (zero-padded) matrix, B the tile:
+//   n <= 128: M = 128, BN = 64 (N = 128), A chunks of K = 32
+//   n = 256 : M = 256 as two 128-row halves, BN = 32 (N = 64), A chunks of K = 16
+// 3xTF32: A = A_hi + A_lo (split once from the FP64 matrix on the host), B = B_hi +
+// B_lo (split on the fly), both parts tf32-exact, D = A_hi B_hi + A_hi B_lo + A_lo B_hi.
+// The tensor core's FP32 accumulation truncates; to keep that bias small each K chunk
+// group accumulates in its own TMEM region (up to 4) and the epilogue adds them with
+// round-to-nearest FP32 adds.
 //
 //   prologue  (thread = column): load tile, pre-ops, split -> B_hi/B_lo (smem)
 //   GEMM 1    (one thread issues tcgen05.mma; A chunks stream in by bulk TMA)
@@ -21,8 +25,10 @@
 //   GEMM 2
 //   epilogue 2: post-ops -> staging -> coalesced store
 //   FP64 norm partials folded by the last CTA in a fixed order (as lane_sweep.cu).
-// Every mbarrier wait is bounded; on a timeout the CTA records an error in a slot,
-// waits (bounded) for its own copies, frees its tensor memory and returns.
+// Point-wise ops run on batches of 8-16 values per thread so each thread keeps that
+// many table / state loads in flight.
+// Every mbarrier wait is bounded (2 s); on a timeout the CTA records an error in a
+// slot, waits (bounded) for its own copies, frees its tensor memory and returns.
 #include "common.cuh"
 #include "tc_common.cuh"
 
@@ -30,24 +36,46 @@ namespace so {
 
 namespace {
 
-constexpr int kBN = 64;             // complex columns per tile
-constexpr int kNC = 2 * kBN;        // fp32 columns = MMA N
-constexpr int kM = 128;             // MMA M (matrix rows, zero padded)
-constexpr int kChunkK = 32;         // K per A chunk
-constexpr int kChunkBytes = kM * kChunkK * 4;  // one of hi / lo
+constexpr int kChunkBytes = 16384;  // one of hi / lo: 128 rows x 32 K or 256 rows x 16 K
 constexpr int kLboB = 144;          // B: core matrices along K (16 B padding vs 128)
-constexpr int kStageRow = 132;      // output staging row stride in floats (528 B)
 constexpr uint64_t kWaitLimit = 2000000000ull;  // 2 s per wait
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;
+
+struct TcShape {
+  int mh;        // 128-row halves of M
+  int bn;        // complex columns per tile
+  int nc;        // fp32 columns = MMA N
+  int chunk_k;   // K per A chunk
+  int nk;        // chunks per matrix
+  int nacc;      // TMEM accumulators per GEMM
+  int sbo_a;     // A: row-group stride (bytes)
+  int stage_row; // output staging row stride (floats)
+  int groups;    // threads per column: 256 / bn
+};
+
+__host__ __device__ inline TcShape tc_shape(int n) {
+  TcShape s{};
+  s.mh = n == 256 ? 2 : 1;
+  s.bn = 64 / s.mh;
+  s.nc = 2 * s.bn;
+  s.chunk_k = 32 / s.mh;
+  s.nk = n / s.chunk_k;
+  s.nacc = s.nk < 4 ? s.nk : 4;
+  s.sbo_a = (s.chunk_k / 4) * 128;
+  s.stage_row = s.nc + 4;
+  s.groups = kThreads / s.bn;
+  return s;
+}
 
 struct TcSmemLayout {
   uint32_t stage0, stage1, bhi, blo, bars, sbo_b, bbytes, total;
 };
 
 __host__ __device__ inline TcSmemLayout tc_layout(int n) {
+  const TcShape s = tc_shape(n);
   TcSmemLayout L{};
-  L.sbo_b = (uint32_t)((n + 3) / 4) * kLboB + 16;
-  L.bbytes = 16u * L.sbo_b;  // 16 groups of 8 columns
+  L.sbo_b = (uint32_t)(n / 4) * kLboB + 16;
+  L.bbytes = (uint32_t)(s.nc / 8) * L.sbo_b;
   L.bbytes = (L.bbytes + 127u) & ~127u;
   const uint32_t stage_bytes = 2u * kChunkBytes;
   L.stage0 = 0;
@@ -65,13 +93,14 @@ __device__ __forceinline__ uint32_t boff(int q, int k, uint32_t sbo) {
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
 
-__device__ double block_sum128(double v, double* scratch) {
+__device__ double block_sum256(double v, double* scratch) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
   if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
   __syncthreads();
   double r = 0.0;
-  if (threadIdx.x == 0) r = scratch[0] + scratch[1] + scratch[2] + scratch[3];
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kThreads / 32; ++w) r += scratch[w];
   __syncthreads();
   return r;
 }
@@ -93,31 +122,58 @@ __device__ __forceinline__ int64_t coord_of(const Geometry& g, int a, int64_t o,
   return 0;
 }
 
-// One point-wise op on the complex value at (row j, outer o, inner i); global index idx.
-__device__ __forceinline__ float2 point_op(const PassParams& p, const DevOp& op, int oi, float2 v, int j, int64_t o,
-                                           int64_t i, int64_t idx, double* acc, const double* sc) {
+// Point-wise ops [ob, oe) on NB values: value u sits at lane-axis row jr[u], inner
+// column ic[u], storage index ix[u].  Each op touches all NB values before the next
+// op, so table loads of one op are independent of each other.
+template <int NB>
+__device__ __forceinline__ void apply_ops(const PassParams& p, int ob, int oe, float2 (&v)[NB], const int (&jr)[NB],
+                                          const int64_t (&ic)[NB], const int64_t (&ix)[NB], int64_t o, double* acc,
+                                          const double* sc) {
   const Geometry& g = p.g;
-  switch (op.kind) {
-    case OP_DIAG1D: {
-      const float2* t = reinterpret_cast<const float2*>(op.ptr);
-      const int64_t k = op.axis == g.sweep_axis ? j : coord_of(g, op.axis, o, i);
-      return cmulf(v, __ldg(t + k));
+  for (int oi = ob; oi < oe; ++oi) {
+    const DevOp& op = p.ops[oi];
+    switch (op.kind) {
+      case OP_DIAG1D: {
+        const float2* t = reinterpret_cast<const float2*>(op.ptr);
+        if (op.axis == g.sweep_axis) {
+#pragma unroll
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], __ldg(t + jr[u]));
+        } else {
+#pragma unroll
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], __ldg(t + coord_of(g, op.axis, o, ic[u])));
+        }
+        break;
+      }
+      case OP_DIAGND: {
+        const float2* t = reinterpret_cast<const float2*>(op.ptr);
+        float2 tv[NB];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) tv[u] = __ldg(t + ix[u]);
+#pragma unroll
+        for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tv[u]);
+        break;
+      }
+      case OP_SCALE: {
+        const float f = (float)sc[oi];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) v[u] = {v[u].x * f, v[u].y * f};
+        break;
+      }
+      case OP_NORM: {
+        double s = 0.0;
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+          double w = op.w[g.sweep_axis][jr[u]];
+          for (int a = 0; a < g.ndim; ++a)
+            if (a != g.sweep_axis) w *= op.w[a][coord_of(g, a, o, ic[u])];
+          s += ((double)v[u].x * v[u].x + (double)v[u].y * v[u].y) * w;
+        }
+        acc[op.red] += s;
+        break;
+      }
+      default:
+        break;
     }
-    case OP_DIAGND:
-      return cmulf(v, __ldg(reinterpret_cast<const float2*>(op.ptr) + idx));
-    case OP_SCALE: {
-      const float f = (float)sc[oi];
-      return {v.x * f, v.y * f};
-    }
-    case OP_NORM: {
-      double w = op.w[g.sweep_axis][j];
-      for (int a = 0; a < g.ndim; ++a)
-        if (a != g.sweep_axis) w *= op.w[a][coord_of(g, a, o, i)];
-      acc[op.red] += ((double)v.x * v.x + (double)v.y * v.y) * w;
-      return v;
-    }
-    default:
-      return v;
   }
 }
 
@@ -146,7 +202,7 @@ struct TcParams {
   PassParams p;
   int32_t mat_op[2];      // op indices of the (one or two) lane matrices
   int32_t nmat;
-  const float* images[2]; // A chunk images per matrix: nchunks x (hi 16 KB, lo 16 KB)
+  const float* images[2]; // A chunk images per matrix: nk x (hi 16 KB, lo 16 KB)
   int32_t error_slot;
 };
 
@@ -156,13 +212,14 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
   const Geometry& g = p.g;
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint32_t tmem_base_s;
-  __shared__ double scratch[4];
+  __shared__ double scratch[kThreads / 32];
   __shared__ double blk_red[kMaxRed];
   __shared__ double totals[kMaxRed];
   __shared__ double scale_v[kMaxOps];
   __shared__ int s_last, s_fail;
 
   const int n = (int)g.n;
+  const TcShape S = tc_shape(n);
   const TcSmemLayout L = tc_layout(n);
   unsigned char* stage[2] = {sm + L.stage0, sm + L.stage1};
   float* bhi = reinterpret_cast<float*>(sm + L.bhi);
@@ -171,12 +228,12 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
   uint64_t* full = bars;       // [2]
   uint64_t* empty = bars + 2;  // [2]
   uint64_t* dbar = bars + 4;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int nk = (n + kChunkK - 1) / kChunkK;
-  const int total_chunks = nk * tp.nmat;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int total_chunks = S.nk * tp.nmat;
+  const uint32_t tmem_cols = (uint32_t)S.nacc * 128u;
 
   const int64_t o = tile / g.tiles_per_outer;
-  const int64_t i0 = (tile - o * g.tiles_per_outer) * kBN;
+  const int64_t i0 = (tile - o * g.tiles_per_outer) * S.bn;
   const int64_t base = o * g.n * g.inner + i0;  // element (row 0, column 0) of the tile
   float2* psi = reinterpret_cast<float2*>(p.psi);
 
@@ -193,7 +250,7 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
     const DevOp& op = p.ops[tid < p.nops ? tid : 0];
     scale_v[tid] = (tid < p.nops && op.kind == OP_SCALE) ? sqrt(__ldcg(p.slots + op.b) / __ldcg(p.slots + op.c)) : 0.0;
   }
-  if (warp == 0) tmem_alloc(&tmem_base_s, 256);
+  if (warp == 0) tmem_alloc(&tmem_base_s, tmem_cols);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -201,7 +258,7 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
 
   // A producer (thread 0): chunk c of the whole sequence -> stage c & 1
   auto issue_chunk = [&](int c) {
-    const int m = c / nk, q = c - m * nk;
+    const int m = c / S.nk, q = c - m * S.nk;
     const int s = c & 1;
     mbar_expect_tx(&full[s], 2u * kChunkBytes);
     bulk_g2s(stage[s], tp.images[m] + (size_t)q * 2 * (kChunkBytes / 4), 2u * kChunkBytes, &full[s]);
@@ -211,52 +268,65 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
     if (total_chunks > 1) issue_chunk(1);
   }
 
-  // ops before the first matrix run in the prologue, the others in the epilogue that follows their matrix
-  const int seg_end0 = tp.mat_op[0];
   double acc[kMaxRed];
 #pragma unroll
   for (int r = 0; r < kMaxRed; ++r) acc[r] = 0.0;
 
-  // ---- prologue: thread = complex column c, rows of parity h
+  // ---- prologue: thread = complex column c, rows h, h + G, ... (G = groups)
   {
-    const int c = tid & (kBN - 1), h = tid >> 6;
+    const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
     const int64_t i = i0 + c;
-    for (int k = h; k < n; k += 2) {
-      const int64_t idx = base + (int64_t)k * g.inner + c;
-      float2 v = psi[idx];
-      for (int oi = 0; oi < seg_end0; ++oi) v = point_op(p, p.ops[oi], oi, v, k, o, i, idx, acc, scale_v);
-      float rh, rl, ih, il;
-      split_tf32(v.x, rh, rl);
-      split_tf32(v.y, ih, il);
-      const uint32_t a0 = boff(2 * c, k, L.sbo_b) >> 2, a1 = boff(2 * c + 1, k, L.sbo_b) >> 2;
-      bhi[a0] = rh;
-      blo[a0] = rl;
-      bhi[a1] = ih;
-      blo[a1] = il;
+    for (int kb = h; kb < n; kb += 8 * G) {
+      float2 v[8];
+      int jr[8];
+      int64_t ic[8], ix[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        jr[u] = kb + u * G;
+        ic[u] = i;
+        ix[u] = base + (int64_t)jr[u] * g.inner + c;
+        v[u] = psi[ix[u]];
+      }
+      apply_ops<8>(p, 0, tp.mat_op[0], v, jr, ic, ix, o, acc, scale_v);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        float rh, rl, ih, il;
+        split_tf32(v[u].x, rh, rl);
+        split_tf32(v[u].y, ih, il);
+        const uint32_t a0 = boff(2 * c, jr[u], L.sbo_b) >> 2, a1 = boff(2 * c + 1, jr[u], L.sbo_b) >> 2;
+        bhi[a0] = rh;
+        blo[a0] = rl;
+        bhi[a1] = ih;
+        blo[a1] = il;
+      }
     }
-    // rows n..(K rounded to 8) stay zero in the K remainder (n is a multiple of 32 here)
   }
   fence_proxy_async();
   __syncthreads();
 
-  const uint32_t idesc = idesc_tf32(kM, kNC);
-  // MMA issue for matrix m into TMEM columns [m * 128, m * 128 + 128)
+  const uint32_t idesc = idesc_tf32(128, (uint32_t)S.nc);
+  // MMA issue for matrix m: chunk q accumulates into TMEM region (q * nacc / nk) * 128
   auto run_gemm = [&](int m) -> bool {
-    const uint32_t d = tmem + (uint32_t)(m * kNC);
-    for (int q = 0; q < nk; ++q) {
-      const int c = m * nk + q, s = c & 1;
+    for (int q = 0; q < S.nk; ++q) {
+      const int c = m * S.nk + q, s = c & 1;
+      const int a = q * S.nacc / S.nk;
+      const bool first_of_acc = (q * S.nacc) % S.nk == 0;
       if (!mbar_wait(&full[s], (uint32_t)((c >> 1) & 1), kWaitLimit)) return false;
       tc_fence_after();
-      const int ksteps = min(kChunkK, n - q * kChunkK) / 8;
+      const int ksteps = S.chunk_k / 8;
       for (int ks = 0; ks < ksteps; ++ks) {
-        const int kg = q * kChunkK + ks * 8;
-        const uint64_t ahi = smem_desc(stage[s] + ks * 256, 128, 1024);
-        const uint64_t alo = smem_desc(stage[s] + kChunkBytes + ks * 256, 128, 1024);
+        const int kg = q * S.chunk_k + ks * 8;
         const uint64_t bh = smem_desc(reinterpret_cast<unsigned char*>(bhi) + (kg >> 2) * kLboB, kLboB, L.sbo_b);
         const uint64_t bl = smem_desc(reinterpret_cast<unsigned char*>(blo) + (kg >> 2) * kLboB, kLboB, L.sbo_b);
-        mma_tf32(d, ahi, bh, idesc, (q > 0 || ks > 0) ? 1u : 0u);
-        mma_tf32(d, ahi, bl, idesc, 1u);
-        mma_tf32(d, alo, bh, idesc, 1u);
+        for (int hh = 0; hh < S.mh; ++hh) {
+          const uint32_t d = tmem + (uint32_t)(a * 128 + hh * 64);
+          const int aoff = hh * 16 * S.sbo_a + ks * 256;
+          const uint64_t ahi = smem_desc(stage[s] + aoff, 128, (uint32_t)S.sbo_a);
+          const uint64_t alo = smem_desc(stage[s] + kChunkBytes + aoff, 128, (uint32_t)S.sbo_a);
+          mma_tf32(d, ahi, bh, idesc, (first_of_acc && ks == 0) ? 0u : 1u);
+          mma_tf32(d, ahi, bl, idesc, 1u);
+          mma_tf32(d, alo, bh, idesc, 1u);
+        }
       }
       mma_commit(&empty[s]);
       // refill the stage of the previous chunk with chunk c + 1 (its MMAs were issued earlier)
@@ -270,7 +340,14 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
     return true;
   };
 
-  // ---- GEMMs and epilogues
+  // epilogue mapping: warp w reads TMEM lanes 32 (w & 3) .. +31; upper warps take the
+  // second column half (n <= 128) or the second 128-row half (n = 256)
+  const int lg = warp & 3, up = warp >> 2;
+  const int j = (S.mh == 2 ? 128 * up : 0) + 32 * lg + lane;  // lane-axis row
+  const bool row_ok = j < n;
+  const int cbase = S.mh == 2 ? 0 : 32 * up;  // first complex column of this thread
+  float* stg = bhi;  // output staging reuses the B_hi area once the last GEMM is done
+
   for (int m = 0; m < tp.nmat; ++m) {
     if (tid == 0 && !s_fail) {
       if (!run_gemm(m)) s_fail = 1;
@@ -288,38 +365,45 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
     const bool last = m + 1 == tp.nmat;
     // ops between this matrix and the next one (or the end of the program)
     const int sb = tp.mat_op[m] + 1, se = last ? p.nops : tp.mat_op[m + 1];
-    const int j = tid;  // row = TMEM lane
-    const bool row_ok = j < n;
-    float* stg = bhi;  // output staging reuses the B_hi area once the last GEMM is done
-    for (int cc = 0; cc < kNC / 32; ++cc) {
+    for (int cc = 0; cc < 2; ++cc) {
       float v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(m * kNC + cc * 32), v);
-      if (row_ok) {
+      const uint32_t col = (uint32_t)(64 * up + 32 * cc);
+      tmem_ld32(tmem + ((uint32_t)(lg * 32) << 16) + col, v);
+      for (int a = 1; a < S.nacc; ++a) {
+        float w2[32];
+        tmem_ld32(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(a * 128) + col, w2);
 #pragma unroll
-        for (int pp = 0; pp < 16; pp += 2) {
-          float2 x0 = {v[2 * pp], v[2 * pp + 1]}, x1 = {v[2 * pp + 2], v[2 * pp + 3]};
-          const int c0 = cc * 16 + pp;
-          const int64_t idx0 = base + (int64_t)j * g.inner + c0;
-          for (int oi = sb; oi < se; ++oi) {
-            x0 = point_op(p, p.ops[oi], oi, x0, j, o, i0 + c0, idx0, acc, scale_v);
-            x1 = point_op(p, p.ops[oi], oi, x1, j, o, i0 + c0 + 1, idx0 + 1, acc, scale_v);
-          }
-          if (last) {
-            *reinterpret_cast<float4*>(stg + j * kStageRow + 2 * c0) = make_float4(x0.x, x0.y, x1.x, x1.y);
-          } else {
+        for (int e = 0; e < 32; ++e) v[e] += w2[e];
+      }
+      if (row_ok) {
+        const int c0 = cbase + 16 * cc;  // complex column of v[0..1]
+        float2 x[16];
+        int jr[16];
+        int64_t ic[16], ix[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          x[u] = {v[2 * u], v[2 * u + 1]};
+          jr[u] = j;
+          ic[u] = i0 + c0 + u;
+          ix[u] = base + (int64_t)j * g.inner + c0 + u;
+        }
+        apply_ops<16>(p, sb, se, x, jr, ic, ix, o, acc, scale_v);
+        if (last) {
+#pragma unroll
+          for (int u = 0; u < 16; u += 2)
+            *reinterpret_cast<float4*>(stg + j * S.stage_row + 2 * (c0 + u)) =
+                make_float4(x[u].x, x[u].y, x[u + 1].x, x[u + 1].y);
+        } else {
+#pragma unroll
+          for (int u = 0; u < 16; ++u) {
             float h0, l0;
-            split_tf32(x0.x, h0, l0);
-            bhi[boff(2 * c0, j, L.sbo_b) >> 2] = h0;
-            blo[boff(2 * c0, j, L.sbo_b) >> 2] = l0;
-            split_tf32(x0.y, h0, l0);
-            bhi[boff(2 * c0 + 1, j, L.sbo_b) >> 2] = h0;
-            blo[boff(2 * c0 + 1, j, L.sbo_b) >> 2] = l0;
-            split_tf32(x1.x, h0, l0);
-            bhi[boff(2 * c0 + 2, j, L.sbo_b) >> 2] = h0;
-            blo[boff(2 * c0 + 2, j, L.sbo_b) >> 2] = l0;
-            split_tf32(x1.y, h0, l0);
-            bhi[boff(2 * c0 + 3, j, L.sbo_b) >> 2] = h0;
-            blo[boff(2 * c0 + 3, j, L.sbo_b) >> 2] = l0;
+            const int q = 2 * (c0 + u);
+            split_tf32(x[u].x, h0, l0);
+            bhi[boff(q, j, L.sbo_b) >> 2] = h0;
+            blo[boff(q, j, L.sbo_b) >> 2] = l0;
+            split_tf32(x[u].y, h0, l0);
+            bhi[boff(q + 1, j, L.sbo_b) >> 2] = h0;
+            blo[boff(q + 1, j, L.sbo_b) >> 2] = l0;
           }
         }
       }
@@ -331,16 +415,19 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
 
   if (!s_fail) {
     // coalesced store of the staged tile: thread = complex column
-    const int c = tid & (kBN - 1), h = tid >> 6;
-    for (int k = h; k < n; k += 2) {
-      const float2 v = *reinterpret_cast<const float2*>(bhi + k * kStageRow + 2 * c);
-      psi[base + (int64_t)k * g.inner + c] = v;
+    const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
+    for (int kb = h; kb < n; kb += 8 * G) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = kb + u * G;
+        psi[base + (int64_t)k * g.inner + c] = *reinterpret_cast<const float2*>(stg + k * S.stage_row + 2 * c);
+      }
     }
   }
 
   // ---- norm partials (fixed order) and last-CTA finalize
   for (int r = 0; r < p.nred; ++r) {
-    const double t = block_sum128(acc[r], scratch);
+    const double t = block_sum256(acc[r], scratch);
     if (tid == 0) blk_red[r] = t;
   }
   __syncthreads();
@@ -354,8 +441,7 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
   __syncthreads();
   if (s_last) {
     __threadfence();
-    const int lane = tid & 31;
-    for (int r = warp; r < p.nred; r += 4) {
+    for (int r = warp; r < p.nred; r += kThreads / 32) {
       double v = 0.0;
       for (int64_t b = lane; b < g.tiles; b += 32) v += __ldcg(p.partials + (int64_t)r * g.tiles + b);
 #pragma unroll
@@ -372,13 +458,12 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
 
   // ---- teardown: outstanding copies (on failure), then tensor memory
   if (tid == 0 && s_fail) {
-    // the producer may have copies in flight: wait (bounded) for both stages
     mbar_wait(&full[0], 0u, kWaitLimit);
     mbar_wait(&full[1], 0u, kWaitLimit);
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, 256);
+  if (warp == 0) tmem_dealloc(tmem, tmem_cols);
 }
 
 __global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_constant__ TcParams tp) {
@@ -405,6 +490,8 @@ __global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel_batched(const T
 // ------------------------------------------------------------------ host side
 size_t angular_tc_smem_bytes(int n) { return tc_layout(n).total; }
 
+int angular_tc_columns(int n) { return tc_shape(n).bn; }
+
 size_t tc_params_bytes() { return sizeof(TcParams); }
 
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
@@ -420,15 +507,18 @@ void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const floa
   std::memcpy(out, &tp, sizeof(TcParams));
 }
 
+static bool configure_once(const void* kern, bool& flag) {
+  if (flag) return true;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess)
+    return false;
+  flag = true;
+  return true;
+}
+
 cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,
                                       size_t smem, cudaStream_t s) {
   static bool configured = false;
-  if (!configured) {
-    cudaError_t e =
-        cudaFuncSetAttribute(angular_tc_kernel_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  if (!configure_once((const void*)angular_tc_kernel_batched, configured)) return cudaGetLastError();
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
   angular_tc_kernel_batched<<<(unsigned)blocks, kThreads, smem, s>>>(reinterpret_cast<const TcParams*>(params_dev),
                                                                      offsets_dev, count);
@@ -437,35 +527,36 @@ cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* off
 }
 
 bool angular_tc_eligible(const Geometry& g) {
-  return (g.n == 32 || g.n == 64 || g.n == 128) && g.inner >= kBN && g.inner % kBN == 0;
+  if (!(g.n == 32 || g.n == 64 || g.n == 128 || g.n == 256)) return false;
+  const int bn = tc_shape((int)g.n).bn;
+  return g.inner >= bn && g.inner % bn == 0;
 }
 
-// Chunk images of one real n x n matrix (row-major FP64) for the 3xTF32 A operand:
-// per K chunk of 32, 16 KB of tf32-exact high parts then 16 KB of FP32 remainders,
-// each in the K-major core-matrix order (row group stride 1024 B, K core stride 128 B).
+// Chunk images of one real n x n matrix (row-major FP64) for the 3xTF32 A operand: per
+// K chunk, 16 KB of tf32-exact high parts then 16 KB of tf32-exact remainders, each in
+// the K-major core-matrix order (row-group stride sbo_a, K core-matrix stride 128 B).
 void angular_tc_images(const double* m, int n, std::vector<float>& out) {
-  const int nk = (n + kChunkK - 1) / kChunkK;
-  out.assign((size_t)nk * 2 * (kChunkBytes / 4), 0.0f);
-  for (int q = 0; q < nk; ++q) {
+  const TcShape S = tc_shape(n);
+  const int rows = 128 * S.mh;
+  out.assign((size_t)S.nk * 2 * (kChunkBytes / 4), 0.0f);
+  auto tf32 = [](float x) {
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    b = (b + 0x1000u) & 0xFFFFE000u;
+    float r;
+    std::memcpy(&r, &b, 4);
+    return r;
+  };
+  for (int q = 0; q < S.nk; ++q) {
     float* hi = out.data() + (size_t)q * 2 * (kChunkBytes / 4);
     float* lo = hi + kChunkBytes / 4;
-    for (int r = 0; r < kM; ++r)
-      for (int kk = 0; kk < kChunkK; ++kk) {
-        const int k = q * kChunkK + kk;
-        double v = (r < n && k < n) ? m[(size_t)r * n + k] : 0.0;
-        // nearest tf32 (10 explicit mantissa bits) of the FP64 value, then the FP32 remainder
-        float f = (float)v;
-        uint32_t b;
-        std::memcpy(&b, &f, 4);
-        b = (b + 0x1000u) & 0xFFFFE000u;
-        float h;
-        std::memcpy(&h, &b, 4);
-        // remainder rounded to tf32 as well (the tensor core would truncate it)
-        float l = (float)(v - (double)h);
-        std::memcpy(&b, &l, 4);
-        b = (b + 0x1000u) & 0xFFFFE000u;
-        std::memcpy(&l, &b, 4);
-        const size_t off = (size_t)(r >> 3) * 256 + (size_t)(kk >> 2) * 32 + (size_t)(r & 7) * 4 + (kk & 3);
+    for (int r = 0; r < rows; ++r)
+      for (int kk = 0; kk < S.chunk_k; ++kk) {
+        const int k = q * S.chunk_k + kk;
+        const double v = (r < n && k < n) ? m[(size_t)r * n + k] : 0.0;
+        const float h = tf32((float)v);
+        const float l = tf32((float)(v - (double)h));  // the tensor core would truncate an unrounded remainder
+        const size_t off = (size_t)(r >> 3) * (S.sbo_a / 4) + (size_t)(kk >> 2) * 32 + (size_t)(r & 7) * 4 + (kk & 3);
         hi[off] = h;
         lo[off] = l;
       }
@@ -484,11 +575,7 @@ cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, 
   tp.error_slot = error_slot;
   const size_t smem = angular_tc_smem_bytes((int)p.g.n);
   static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(angular_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  if (!configure_once((const void*)angular_tc_kernel, configured)) return cudaGetLastError();
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
   angular_tc_kernel<<<(unsigned)p.g.tiles, kThreads, smem, s>>>(tp);
   count_launch();

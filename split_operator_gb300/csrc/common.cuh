@@ -92,7 +92,7 @@ size_t pass_smem_bytes(const Geometry& g, bool fp64);
 int pass_threads(const Geometry& g);
 
 // Tensor-core angular sweep (angular_tc.cu): FP32 state, real lane matrices as 3xTF32.
-constexpr int kTcColumns = 64;  // complex columns of the inner axis per CTA tile
+int angular_tc_columns(int n);  // complex columns of the inner axis per CTA tile
 bool angular_tc_eligible(const Geometry& g);
 size_t angular_tc_smem_bytes(int n);
 void angular_tc_images(const double* m, int n, std::vector<float>& out);

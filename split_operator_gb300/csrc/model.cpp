@@ -302,7 +302,7 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
   }
   c.version = version;
   c.real = real;
-  if (!fp64 && tc_tf32 && real && count == 1 && (n == 32 || n == 64 || n == 128)) {
+  if (!fp64 && tc_tf32 && real && count == 1 && (n == 32 || n == 64 || n == 128 || n == 256)) {
     std::vector<double> md(n * n);
     for (size_t i = 0; i < n * n; ++i) md[i] = m[i].real();
     std::vector<float> img;
@@ -330,8 +330,9 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     }
   }
   if (nmat == 0) return false;
-  g.lanes_per_tile = kTcColumns;
-  g.tiles_per_outer = (int32_t)(g.inner / kTcColumns);
+  const int bn = angular_tc_columns((int)g.n);
+  g.lanes_per_tile = bn;
+  g.tiles_per_outer = (int32_t)(g.inner / bn);
   g.tiles = g.outer * g.tiles_per_outer;
   p.g = g;
   if ((size_t)g.tiles > partials_cap_) {

@@ -15,7 +15,7 @@ def so():
     return so
 
 
-@pytest.mark.parametrize("n,nr", [(128, 256), (64, 128), (32, 64), (128, 4096)])
+@pytest.mark.parametrize("n,nr", [(128, 256), (64, 128), (32, 64), (128, 4096), (256, 256), (256, 1024)])
 def test_real_lane_matrix_3xtf32_matches_fp64(so, n, nr):
     rng = np.random.default_rng(n + nr)
     psi = rng.standard_normal((nr, n)) + 1j * rng.standard_normal((nr, n))
@@ -39,7 +39,7 @@ def test_real_lane_matrix_3xtf32_matches_fp64(so, n, nr):
 
 
 @pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_simt"])
-@pytest.mark.parametrize("n", [128, 64])
+@pytest.mark.parametrize("n", [128, 64, 256])
 def test_two_lane_matrices_in_one_pass(so, precision, n):
     """Stack [T-transformation, diagonal D]: a step is T, D, T2 (the inverse slot holds T2),
     so the pass carries two matrix products with a table multiply between them."""
@@ -105,7 +105,7 @@ def test_tensor_core_pass_is_used(so):
     assert any("tc3xtf32" in k for k in names), names
 
 
-@pytest.mark.parametrize("nr,nth", [(256, 32), (512, 64), (1024, 128)])
+@pytest.mark.parametrize("nr,nth", [(256, 32), (512, 64), (1024, 128), (512, 256)])
 def test_radial_angular_tf32x3_close_to_oracle(so, nr, nth):
     from split_operator_gb300 import workloads as W
     steps = 20
