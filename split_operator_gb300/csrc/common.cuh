@@ -88,7 +88,7 @@ struct PassParams {
 // Host launchers (lane_sweep.cu)
 cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);
 cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s);
-size_t pass_smem_bytes(const Geometry& g, bool fp64);
+size_t pass_smem_bytes(const Geometry& g, bool fp64, bool fft);
 int pass_threads(const Geometry& g);
 
 // Tensor-core angular sweep (angular_tc.cu): FP32 state, real lane matrices as 3xTF32.

@@ -150,7 +150,7 @@ __device__ __forceinline__ void stockham_stage(const C* __restrict__ src, C* __r
     for (int r = 0; r < RS; ++r) {
       C x = src[sidx(l, i + r * nb, ls)];
       if (r > 0 && k > 0) {
-        C w = __ldg(tw + r * k * estride);
+        C w = tw[r * k * estride];  // shared-memory copy of the table
         if (dir > 0) w.y = -w.y;
         x = cmul(x, w);
       }
@@ -329,6 +329,8 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
   off += (size_t)L * kMaxDims * sizeof(int);
   int* lane_sel = reinterpret_cast<int*>(smem_raw + off);
   off += (size_t)L * sizeof(int);
+  off = (off + 15) & ~(size_t)15;
+  C* tw_s = reinterpret_cast<C*>(smem_raw + off);  // the lane's twiddles (passes with an FFT)
   __shared__ double scratch[32];
   __shared__ double blk_red[kMaxRed];
   __shared__ double totals[kMaxRed];
@@ -382,9 +384,13 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
     const int64_t b = lane_base[l];
     buf[sidx(l, x, ls)] = b >= 0 ? psi[b + (int64_t)x * g.inner] : C{(R)0, (R)0};
   }
-  __syncthreads();
-
+  // twiddles in shared memory: the butterflies read them at scattered indices
   const C* tw = reinterpret_cast<const C*>(p.twiddle);
+  if (tw) {
+    for (int k = tid; k < n; k += T) tw_s[k] = tw[k];
+    tw = tw_s;
+  }
+  __syncthreads();
   for (int rep = 0; rep < p.repeat; ++rep) {
     for (int oi = 0; oi < p.nops; ++oi) {
       const DevOp& op = p.ops[oi];
@@ -578,11 +584,11 @@ static cudaError_t launch_batched_impl(const PassParams* params_dev, const int64
   auto kern = pass_kernel_batched<R, RMAX>;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  if (smem > 200 * 1024 || threads > 512) return cudaErrorInvalidValue;
+  if (smem > 220 * 1024 || threads > 512) return cudaErrorInvalidValue;
   kern<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
   count_launch();
   return cudaGetLastError();
@@ -594,10 +600,12 @@ cudaError_t launch_pass_batched(bool fp64, const PassParams* params_dev, const i
               : launch_batched_impl<float, 16>(params_dev, offsets_dev, count, blocks, threads, smem, s);
 }
 
-size_t pass_smem_bytes(const Geometry& g, bool fp64) {
+size_t pass_smem_bytes(const Geometry& g, bool fp64, bool fft) {
   const size_t cs = fp64 ? 16 : 8;
   size_t b = 2 * (((size_t)g.lanes_per_tile * g.lane_stride * cs + 15) & ~(size_t)15);
   b += (size_t)g.lanes_per_tile * (sizeof(int64_t) + sizeof(double) + kMaxDims * sizeof(int) + sizeof(int));
+  b = (b + 15) & ~(size_t)15;
+  if (fft) b += (size_t)g.n * cs;
   return b;
 }
 
@@ -612,15 +620,15 @@ int pass_threads(const Geometry& g) {
 
 template <typename R, int RMAX>
 static cudaError_t launch_impl(const PassParams& p, cudaStream_t s) {
-  const size_t smem = pass_smem_bytes(p.g, sizeof(R) == 8);
+  const size_t smem = pass_smem_bytes(p.g, sizeof(R) == 8, p.twiddle != nullptr);
   auto kern = pass_kernel<R, RMAX>;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  if (smem > 220 * 1024) return cudaErrorInvalidValue;
   const int threads = pass_threads(p.g);
   kern<<<(unsigned)p.g.tiles, threads, smem, s>>>(p);
   count_launch();

@@ -444,7 +444,7 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
     RecordedPass r{resident ? RecordedPass::Resident : RecordedPass::Generic, fp64, p, {},
-                   pass_threads(p.g), pass_smem_bytes(p.g, fp64), name, pass_bytes(ops, p.g)};
+                   pass_threads(p.g), pass_smem_bytes(p.g, fp64, p.twiddle != nullptr), name, pass_bytes(ops, p.g)};
     recording->push_back(std::move(r));
     return;
   }
@@ -1320,9 +1320,18 @@ void Batch::steps(uint64_t n) {
   const size_t m = merged ? (np - 1) / 2 : np / 2;
   const size_t per0 = merged ? 1 : m;  // first pass of the repeated period
   for (const auto& r : rec)
-    for (size_t i = (merged ? 1 : 1); i < m; ++i)
-      if (!same_params(r[merged ? i : i], r[merged ? m + i : m + i]))
-        throw Error(SO_ERR_UNSUPPORTED, "step program is not periodic; run these propagations one by one");
+    for (size_t i = 1; i < m; ++i)
+      if (!same_params(r[i], r[m + i])) {
+        // name the first differing byte of the pass parameters (diagnostic)
+        const unsigned char* a = reinterpret_cast<const unsigned char*>(&r[i].p);
+        const unsigned char* b = reinterpret_cast<const unsigned char*>(&r[m + i].p);
+        size_t off = 0;
+        while (off < sizeof(PassParams) && a[off] == b[off]) ++off;
+        throw Error(SO_ERR_UNSUPPORTED, "step program is not periodic (pass " + std::to_string(i) + " '" +
+                                            r[i].name + "' vs '" + r[m + i].name + "', byte " +
+                                            std::to_string(off) + " of " + std::to_string(np) +
+                                            " passes); run these propagations one by one");
+      }
   std::vector<std::vector<Group>> pos(np);
   for (size_t i = 0; i < np; ++i) pos[i] = build_groups(rec, i);
   launches_per_step_ = 0;
