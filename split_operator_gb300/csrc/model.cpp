@@ -192,7 +192,8 @@ int Engine::alloc_slot(double init) {
     if (next_slot_ >= kNumSlots) throw Error(SO_ERR_UNSUPPORTED, "out of device scalar slots");
     s = next_slot_++;
   }
-  write_slot(s, init);
+  // a fresh slot is not referenced by the open pass: initialise it in stream order without closing the pass
+  cuda_check(cudaMemcpyAsync(slots() + s, &init, sizeof(double), cudaMemcpyHostToDevice, stream), "slot init");
   return s;
 }
 
@@ -240,7 +241,7 @@ static void upload_complex(DeviceBuffer& buf, const std::vector<cplx>& t, bool f
 const void* Engine::table_1d(const void* key, uint64_t version, const std::vector<cplx>& t) {
   auto& c = tables_[{key, 0}];
   if (c.buf.ptr && c.version == version) return c.buf.ptr;
-  flush();
+  if (c.buf.ptr) flush();  // replacing a table the open pass may reference (a first upload needs no flush)
   upload_complex(c.buf, t, fp64, stream);
   c.version = version;
   return c.buf.ptr;
@@ -249,7 +250,7 @@ const void* Engine::table_1d(const void* key, uint64_t version, const std::vecto
 const void* Engine::table_nd(const void* key, uint64_t version, const std::vector<cplx>& t) {
   auto& c = tables_[{key, 1}];
   if (c.buf.ptr && c.version == version) return c.buf.ptr;
-  flush();
+  if (c.buf.ptr) flush();
   // logical row-major -> storage order
   const int nd = (int)shape.size();
   std::vector<cplx> st(t.size());
@@ -281,7 +282,7 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
     real = c.real;
     return c.buf.ptr;
   }
-  flush();
+  if (c.buf.ptr) flush();
   real = std::all_of(m.begin(), m.end(), [](const cplx& v) { return v.imag() == 0.0; });
   std::vector<cplx> mt(m.size());
   for (size_t b = 0; b < count; ++b)
@@ -361,7 +362,6 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
 const double* Engine::weights(const Grid& g) {
   auto it = weights_.find(g.uid);
   if (it != weights_.end()) return it->second.as<double>();
-  flush();
   DeviceBuffer b;
   upload(b, g.weights, stream);
   const double* p = b.as<double>();

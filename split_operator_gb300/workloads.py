@@ -59,6 +59,35 @@ def radial_angular_inputs(nr=4096, nth=128, seed=2026, d=0.1, a=1.0, re=3.0, bet
     return dict(r=r, x=x, w=w, v=v, psi=psi, mass=mass, r_min=r_min, r_max=r_max)
 
 
+NR_CHOICES = (512, 1024, 2048, 4096, 8192)
+NTH_CHOICES = (32, 64, 128, 256)
+
+
+def batched_instance_params(count=512, seed_base=1000):
+    """Seeded per-instance sizes and Morse parameters of the batched workload:
+    Nr uniform over {512..8192}, Ntheta over {32..256}, D in [0.05, 0.2], a in [0.6, 1.4],
+    re in [2, 4], beta in [0, 0.05] (instance i draws from default_rng(seed_base + i))."""
+    out = []
+    for i in range(count):
+        rng = np.random.default_rng(seed_base + i)
+        nr = int(rng.choice(NR_CHOICES))
+        nth = int(rng.choice(NTH_CHOICES))
+        out.append(dict(nr=nr, nth=nth, d=float(rng.uniform(0.05, 0.2)), a=float(rng.uniform(0.6, 1.4)),
+                        re=float(rng.uniform(2.0, 4.0)), beta=float(rng.uniform(0.0, 0.05)), seed=seed_base + i))
+    return out
+
+
+def batched_radial_angular(count=512, seed_base=1000, precision="fp32_tf32x3", dt=0.5, step_no=2000):
+    """The batched workload: `count` independent radial x angular propagations of uneven
+    sizes, each with its own seeded potential and initial state (mass 1000)."""
+    props = []
+    for prm in batched_instance_params(count, seed_base):
+        p, _ = radial_angular_2d(nr=prm["nr"], nth=prm["nth"], dt=dt, step_no=step_no, seed=prm["seed"],
+                                 precision=precision, d=prm["d"], a=prm["a"], re=prm["re"], beta=prm["beta"])
+        props.append(p)
+    return props
+
+
 def radial_angular_2d(nr=4096, nth=128, dt=0.5, step_no=10000, seed=2026, precision="fp64", with_loss=True,
                       im_time=False, **kw):
     inp = radial_angular_inputs(nr, nth, seed, **kw)
