@@ -1,20 +1,23 @@
 #!/usr/bin/env python
 """Benchmark of the split-operator propagation step on GB300.
 
-Workload (default): the 2-D radial x angular problem -- 4096 radial points on
-r in [0.5, 60] x 128 Gauss-Legendre angular points (Legendre transform to
-l_max = 127), Morse + beta e^{-r/2} P2(cos th), mass 1000, dt = 0.5, border
-damping with a loss checker, stack [Damp, V/2, Legendre, Rot/2, FFT, K].
-One bench step = one split-operator time step of that problem, timed with CUDA
-events on the library's stream; the L2 is flushed (256 MiB write) before every
-timed step, so each step reads its state and tables from HBM.
+Default workload (``--workload batch``): 512 independent 2-D radial x angular
+propagations of uneven sizes -- Nr drawn from {512..8192}, Ntheta from
+{32, 64, 128, 256} (Gauss-Legendre, Legendre transform to l_max = Ntheta - 1),
+Morse D(1-e^{-a(r-re)})^2 + beta e^{-r/2} P2(cos th) with D, a, re, beta seeded per
+instance, mass 1000, dt = 0.5, border damping with a loss checker, stack
+[Damp, V/2, Legendre, Rot/2, FFT, K] -- stepped together by the batched executor
+(FP32 state, 3xTF32 tensor-core Legendre transforms, FP64 norms and loss).  The
+states and tables (~4.2 GB) are far larger than L2, so no flush is needed.
+One bench step = one split-operator time step of all 512 instances.
 
-Prints ONE JSON line (rank 0).  ``--impl reference`` times the reference's CPU
-algorithm instead (the C++ FP64 restatement in oracle/, all host threads).
+``--workload single`` is the single 4096 x 128 problem (L2 flushed before every
+timed step).  ``--impl reference`` times the reference's CPU algorithm instead (the
+C++ FP64 restatement in oracle/, all host threads) on the same workload.
+Prints ONE JSON line (rank 0).
 """
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
@@ -31,10 +34,12 @@ UNIT = "grid-pt·steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp32_simt", choices=["fp64", "fp32_tf32x3", "fp32_bf16x3", "fp32_simt"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "single"])
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--precision", default="fp32_tf32x3", choices=["fp64", "fp32_tf32x3", "fp32_simt"])
     ap.add_argument("--nr", type=int, default=4096)
     ap.add_argument("--nth", type=int, default=128)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -45,6 +50,10 @@ def parse():
 
 
 def workload_name(a):
+    if a.workload == "batch":
+        return (f"batched radial x angular: {a.instances} instances, Nr in {{512..8192}}, Ntheta in {{32,64,128,256}} "
+                "(GL), Morse D~U[0.05,0.2] a~U[0.6,1.4] re~U[2,4] + beta~U[0,0.05] e^(-r/2) P2, mass 1000, dt=0.5, "
+                "damping+loss, stack [Damp,V/2,L,Rot/2,F,K], seeds default_rng(1000+i)")
     return (f"radial_angular_2d Nr={a.nr} x Ntheta={a.nth} (GL), Morse D=0.1 a=1 re=3 + 0.02 e^(-r/2) P2, "
             f"mass 1000, dt=0.5, damping+loss, stack [Damp,V/2,L,Rot/2,F,K]")
 
@@ -109,7 +118,7 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes per launch of each pass kind from the committed ncu summary (or {})."""
+    """DRAM bytes per launch of each kernel family from the committed ncu summary (or {})."""
     p = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.txt")
     out = {}
     if os.path.exists(p):
@@ -120,31 +129,14 @@ def ncu_traffic():
     return out
 
 
-def cpu_baseline(a, seconds):
-    """The C++ FP64 restatement of the reference algorithm on all host threads, bounded sample."""
-    from oracle import cpu_port as P
-    port = P.RadialAngular(a.nr, a.nth)
-    threads = os.cpu_count() or 1
-    port.run(1, threads=threads)  # warm-up (also builds the library)
-    t0 = time.perf_counter()
-    port.run(1, threads=threads)
-    one = time.perf_counter() - t0
-    n = max(1, min(200, int(seconds / max(one, 1e-6))))
-    t0 = time.perf_counter()
-    port.run(n, threads=threads)
-    dt = time.perf_counter() - t0
-    return {"value": a.nr * a.nth * n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} steps of the {a.nr}x{a.nth} problem, FP64, C++ restatement of the reference passes"}
-
-
-def dist_setup(n):
+def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("nccl" if os.environ.get("SO_BENCH_GLOO") is None else "gloo")
+        dist.init_process_group("gloo" if os.environ.get("SO_BENCH_GLOO") else "nccl")
     return world, rank, local
 
 
@@ -164,156 +156,249 @@ def allmax(world, v):
     return float(t.item())
 
 
+def rel_l2(x, y):
+    import numpy as np
+    return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+
+
+# ------------------------------------------------------------------ CPU legs
+def cpu_sample(a):
+    """Instances the CPU legs time: the single problem, or a size-stratified sample of the batch."""
+    if a.workload == "single":
+        return [dict(nr=a.nr, nth=a.nth, seed=2026, d=0.1, a=1.0, re=3.0, beta=0.02)]
+    from split_operator_gb300 import workloads as W
+    params = W.batched_instance_params(a.instances)
+    # two instances of every (Nr, Ntheta) class present, in instance order
+    seen, out = {}, []
+    for p in params:
+        k = (p["nr"], p["nth"])
+        if seen.get(k, 0) < 2:
+            seen[k] = seen.get(k, 0) + 1
+            out.append(p)
+    return out
+
+
+def cpu_rate(a, seconds, steps=None):
+    """pt*steps/s of the C++ FP64 restatement of the reference passes on all host threads."""
+    from oracle import cpu_port as P
+    threads = os.cpu_count() or 1
+    sample = cpu_sample(a)
+    ports = [P.RadialAngular(s["nr"], s["nth"], seed=s["seed"], d=s["d"], a=s["a"], re=s["re"], beta=s["beta"])
+             for s in sample]
+    for pt in ports:
+        pt.run(1, threads=threads)  # warm-up
+    if steps is None:
+        t0 = time.perf_counter()
+        for pt in ports:
+            pt.run(1, threads=threads)
+        one = time.perf_counter() - t0
+        steps = max(1, min(200, int(seconds / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for pt in ports:
+        pt.run(steps, threads=threads)
+    dt = time.perf_counter() - t0
+    pts = sum(s["nr"] * s["nth"] for s in sample)
+    desc = (f"{steps} steps of {len(sample)} instances ({pts} grid points: two of every Nr x Ntheta class of the "
+            "batch)" if a.workload == "batch" else f"{steps} steps of the {a.nr}x{a.nth} problem")
+    return pts * steps / dt, threads, desc + ", FP64, C++ restatement of the reference passes (oracle/cpu_port.cpp)"
+
+
 def run_reference(a):
-    world, rank, _ = dist_setup(a.gpus)
+    world, rank, _ = dist_setup()
     if rank != 0:
         return
-    from oracle import cpu_port as P
-    port = P.RadialAngular(a.nr, a.nth)
-    threads = os.cpu_count() or 1
-    port.run(a.warmup, threads=threads)
-    t0 = time.perf_counter()
-    port.run(a.steps, threads=threads)
-    dt = time.perf_counter() - t0
-    v = a.nr * a.nth * a.steps / dt
+    v, threads, desc = cpu_rate(a, a.cpu_seconds, steps=max(1, a.steps // 10))
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-            "ms_per_step": dt / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload_name(a), "precision": "fp64 (reference algorithm, CPU)"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{a.steps} timed steps of the {a.nr}x{a.nth} problem (C++ FP64 restatement "
-                                       "of the reference's passes; the Rust crate cannot be built here)"},
+            "config": {"workload": workload_name(a), "precision": "fp64 (reference algorithm, CPU)",
+                       "note": "the Rust crate cannot be built here; its algorithm runs as a C++ restatement"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def rel_l2(x, y):
-    import numpy as np
-    return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+# ------------------------------------------------------------------ GPU leg
+def build_props(a, precision, count=None):
+    from split_operator_gb300 import workloads as W
+    if a.workload == "single":
+        return [W.radial_angular_2d(nr=a.nr, nth=a.nth, step_no=10 ** 6, precision=precision)[0]]
+    return W.batched_radial_angular(count or a.instances, precision=precision, step_no=10 ** 6)
+
+
+def roofline_from(times, total_ms):
+    hbm, _, peak_kind = measured_peaks()
+    if not times:
+        return None
+    name, n, tms, b = max(times, key=lambda t: t[2])
+    ach = (b / n) / (tms / n / 1e3) / 1e9
+    fam = "angular_tc" if "tc3xtf32" in name else "pass_kernel"
+    return {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+            "traffic": ncu_traffic().get(fam), "kernel": name, "launches": n, "avg_us": tms / n * 1e3,
+            "algorithmic_bytes_per_launch": b / n, "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
+            "share_of_timed": tms / total_ms if total_ms > 0 else None}
 
 
 def run_ours(a):
     import numpy as np
     import torch
 
-    world, rank, local = dist_setup(a.gpus)
+    world, rank, local = dist_setup()
     torch.cuda.set_device(local)
     import split_operator_gb300 as so
-    from split_operator_gb300 import workloads as W
 
     stream = torch.cuda.Stream()
-    prop, h = W.radial_angular_2d(nr=a.nr, nth=a.nth, step_no=10 ** 6, precision=a.precision)
-    prop.set_stream(stream.cuda_stream)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    points = a.nr * a.nth
+    props = build_props(a, a.precision)
+    for p in props:
+        p.set_stream(stream.cuda_stream)
+    points = sum(int(np.prod(p.wave_function_shape())) for p in props)
+    single = a.workload == "single"
+    batch = None if single else so.Batch(props)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda") if single else None
 
-    def step_timed(ev0, ev1):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        ev0.record(stream)
-        prop.steps(1)
-        ev1.record(stream)
+    def run_steps(k, timing):
+        if single:
+            props[0].set_timing(timing)
+            evs = []
+            for _ in range(k):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                props[0].steps(1)
+                e1.record(stream)
+                evs.append((e0, e1))
+            props[0].synchronize()
+            torch.cuda.synchronize()
+            kt = props[0].kernel_times() if timing else []
+            props[0].set_timing(False)
+            return sum(x.elapsed_time(y) for x, y in evs), kt
+        batch.set_timing(timing)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.steps(k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        kt = batch.kernel_times() if timing else []
+        batch.set_timing(False)
+        return e0.elapsed_time(e1), kt
 
-    for _ in range(a.warmup):
-        step_timed(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-    prop.synchronize()
-
+    run_steps(a.warmup, False)
     clocks = Clocks(local)
     clocks.start()
     time.sleep(0.3)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
-    prop.set_timing(True)
     n0 = so.launch_count()
     barrier(world)
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
-    for e0, e1 in evs:
-        step_timed(e0, e1)
-    prop.synchronize()
-    torch.cuda.synchronize()
+    ms, kt = run_steps(a.steps, single)  # batch: production path (CUDA graph); single: per-pass events
     wall = time.perf_counter() - wall0
     barrier(world)
     launches = so.launch_count() - n0
-    kt = prop.kernel_times()
-    prop.set_timing(False)
     clocks.stop()
-    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
     ms_max = allmax(world, ms)
     value = points * a.steps * world / (ms_max / 1e3)
-
-    # roofline of the dominant pass kind (live CUDA events on the library's stream)
-    hbm, _, peak_kind = measured_peaks()
-    dom = max(kt, key=lambda t: t[2]) if kt else None
-    roof = None
-    if dom:
-        name, n, tms, b = dom
-        ach = (b / n) / (tms / n / 1e3) / 1e9
-        traffic = ncu_traffic().get(name)
-        roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                "traffic": traffic, "kernel": name, "launches": n, "avg_us": tms / n * 1e3,
-                "algorithmic_bytes_per_launch": b / n, "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
-                "share_of_step": tms / ms if ms > 0 else None}
+    if not single:
+        # per-launch breakdown of the same K steps with CUDA events on every batched launch
+        ms_t, kt = run_steps(a.steps, True)
+    roof = roofline_from(kt, ms if single else ms_t)
 
     if a.quick:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms_max / a.steps,
-                              "quick": True, "passes": [list(t) for t in kt]}), flush=True)
+                              "quick": True, "passes": [list(t) for t in kt], "roofline": roof}), flush=True)
         return
-    # end to end through the C ABI: pinned host input -> device, one step, device -> pinned host
-    host_in = torch.empty(points * 2, dtype=torch.float64).pin_memory()
-    host_out = torch.empty(points * 2, dtype=torch.float64).pin_memory()
-    host_in.numpy()[:] = prop.get_array().view(np.float64).ravel()
-    e2e_steps = max(3, min(a.steps, 20))
-    prop.synchronize()
+
+    # end to end through the C ABI: pinned FP64 host state in, one step, state out
+    e2e_steps = 3
+    hosts = [torch.empty(int(np.prod(p.wave_function_shape())) * 2, dtype=torch.float64).pin_memory()
+             for p in props]
+    outs = [torch.empty_like(h).pin_memory() for h in hosts]
+    for p, h in zip(props, hosts):
+        h.numpy()[:] = p.get_array().view(np.float64).ravel()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        prop.set_array_ptr(host_in.data_ptr())
-        prop.steps(1)
-        prop.get_array_ptr(host_out.data_ptr())
+        for p, h in zip(props, hosts):
+            p.set_array_ptr(h.data_ptr())
+        if single:
+            props[0].steps(1)
+        else:
+            batch.steps(1)
+        for p, o in zip(props, outs):
+            p.get_array_ptr(o.data_ptr())
     e2e_s = allmax(world, time.perf_counter() - t0)
     e2e = {"value": points * e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": points * 16,
            "d2h_bytes_per_step": points * 16, "steps": e2e_steps,
-           "note": "so_propagation_set_array (pinned FP64 host) + so_propagation_steps(1) + so_propagation_get_array"}
+           "note": "every step: so_propagation_set_array from pinned FP64 host buffers for all instances, one step, "
+                   "so_propagation_get_array into pinned host buffers"}
 
-    # accuracy of this precision against the plain FP64 GPU path on the same inputs
     acc = {}
     if rank == 0:
+        # accuracy against the plain FP64 GPU path on identical inputs (a few instances, 100 steps)
+        from split_operator_gb300 import workloads as W
         nchk = 100
-        p64, _ = W.radial_angular_2d(nr=a.nr, nth=a.nth, step_no=nchk, precision="fp64")
-        pfx, hf = W.radial_angular_2d(nr=a.nr, nth=a.nth, step_no=nchk, precision=a.precision)
-        p64.steps(nchk)
-        pfx.steps(nchk)
-        acc = {"steps": nchk, "rel_l2": rel_l2(pfx.get_array(), p64.get_array()),
-               "norm_drift": abs(pfx.norm() - p64.norm()),
-               "loss_diff": abs(pfx.all_losses()[0] - p64.all_losses()[0])}
+        if single:
+            chk = [dict(nr=a.nr, nth=a.nth, seed=2026, d=0.1, a=1.0, re=3.0, beta=0.02)]
+        else:
+            params = W.batched_instance_params(a.instances)
+            chk = [next(p for p in params if p["nth"] == t) for t in (32, 64, 128, 256)]
+        errs = []
+        for c in chk:
+            kw = dict(nr=c["nr"], nth=c["nth"], step_no=nchk, seed=c["seed"], d=c["d"], a=c["a"], re=c["re"],
+                      beta=c["beta"])
+            p64 = W.radial_angular_2d(precision="fp64", **kw)[0]
+            pfx = W.radial_angular_2d(precision=a.precision, **kw)[0]
+            p64.steps(nchk)
+            pfx.steps(nchk)
+            errs.append({"nr": c["nr"], "nth": c["nth"], "rel_l2": rel_l2(pfx.get_array(), p64.get_array()),
+                         "norm_diff": abs(pfx.norm() - p64.norm()),
+                         "loss_diff": abs(pfx.all_losses()[0] - p64.all_losses()[0])})
+        acc = {"steps": nchk, "instances": errs, "max_rel_l2": max(e["rel_l2"] for e in errs)}
         # plain FP64 GPU path throughput on the same workload (the 20x denominator)
-        p64.set_stream(stream.cuda_stream)
-        fe = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
-        for e0, e1 in fe:
-            with torch.cuda.stream(stream):
+        del batch
+        props64 = build_props(a, "fp64")
+        f64_steps = 2
+        if single:
+            p64 = props64[0]
+            evs = []
+            for _ in range(f64_steps):
                 flush.zero_()
-            e0.record(stream)
-            p64.steps(1)
-            e1.record(stream)
-        p64.synchronize()
-        torch.cuda.synchronize()
-        f64_ms = sum(e0.elapsed_time(e1) for e0, e1 in fe) / len(fe)
-        acc["fp64_gpu_value"] = points / (f64_ms / 1e3)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                p64.steps(1)
+                e1.record()
+                evs.append((e0, e1))
+            p64.synchronize()
+            torch.cuda.synchronize()
+            f64_ms = sum(x.elapsed_time(y) for x, y in evs)
+        else:
+            b64 = so.Batch(props64)
+            b64.steps(1)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            b64.steps(f64_steps)
+            e1.record()
+            torch.cuda.synchronize()
+            f64_ms = e0.elapsed_time(e1)
+        acc["fp64_gpu_value"] = points * f64_steps / (f64_ms / 1e3)
         acc["speedup_vs_fp64_gpu"] = value / world / acc["fp64_gpu_value"]
 
     if rank != 0:
         return
     cpu = None
     if not a.no_cpu_baseline:
-        cpu = cpu_baseline(a, a.cpu_seconds)
+        v, threads, desc = cpu_rate(a, a.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if a.precision == "fp64" else "f32", "data": "synthetic",
-            "config": {"workload": workload_name(a), "precision": a.precision,
-                       "l2": "flushed before every timed step (256 MiB write, untimed)",
-                       "parallelism": "replicas" if world > 1 else "single instance",
-                       "global_batch": world, "wall_s_timed_region": wall},
+            "config": {"workload": workload_name(a), "precision": a.precision, "grid_points": points,
+                       "l2": ("inputs larger than L2 (states + tables ~" + f"{points * 24 / 1e9:.1f} GB)")
+                       if not single else "flushed before every timed step (256 MiB write, untimed)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "global_batch": len(props) * world, "wall_s_timed_region": wall},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks.summary(), "accuracy_vs_fp64": acc, "passes": [list(t) for t in kt]}
     print(json.dumps(line), flush=True)

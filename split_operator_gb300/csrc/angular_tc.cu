@@ -47,20 +47,29 @@ struct TcShape {
   int nc;        // fp32 columns = MMA N
   int chunk_k;   // K per A chunk
   int nk;        // chunks per matrix
-  int nacc;      // TMEM accumulators per GEMM
+  int ksteps;    // K steps of 8 per matrix
+  int reg_cols;  // TMEM columns of one accumulator region (all M halves)
+  int nmain;     // regions for the A_hi B_hi products; one more region holds the corrections
   int sbo_a;     // A: row-group stride (bytes)
   int stage_row; // output staging row stride (floats)
   int groups;    // threads per column: 256 / bn
 };
 
+// The tensor core truncates its FP32 accumulation, so a region that accumulates t
+// products is biased toward zero by about t/2 ulps.  The large A_hi B_hi products are
+// spread over up to 7 regions (a couple of K steps each); the corrections A_hi B_lo +
+// A_lo B_hi are 2^-11 smaller and share one region.
 __host__ __device__ inline TcShape tc_shape(int n) {
   TcShape s{};
   s.mh = n == 256 ? 2 : 1;
-  s.bn = 64 / s.mh;
+  s.bn = 32;
   s.nc = 2 * s.bn;
   s.chunk_k = 32 / s.mh;
   s.nk = n / s.chunk_k;
-  s.nacc = s.nk < 4 ? s.nk : 4;
+  s.ksteps = n / 8;
+  s.reg_cols = s.nc * s.mh;
+  const int nreg = 512 / s.reg_cols;
+  s.nmain = s.ksteps < nreg - 1 ? s.ksteps : nreg - 1;
   s.sbo_a = (s.chunk_k / 4) * 128;
   s.stage_row = s.nc + 4;
   s.groups = kThreads / s.bn;
@@ -230,7 +239,7 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
   uint64_t* dbar = bars + 4;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int total_chunks = S.nk * tp.nmat;
-  const uint32_t tmem_cols = (uint32_t)S.nacc * 128u;
+  const uint32_t tmem_cols = 512u;
 
   const int64_t o = tile / g.tiles_per_outer;
   const int64_t i0 = (tile - o * g.tiles_per_outer) * S.bn;
@@ -276,20 +285,21 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
   {
     const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
     const int64_t i = i0 + c;
-    for (int kb = h; kb < n; kb += 8 * G) {
-      float2 v[8];
-      int jr[8];
-      int64_t ic[8], ix[8];
+    // a thread owns n / G rows (a multiple of 4 for every supported n): batches of 4
+    for (int kb = h; kb < n; kb += 4 * G) {
+      float2 v[4];
+      int jr[4];
+      int64_t ic[4], ix[4];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
+      for (int u = 0; u < 4; ++u) {
         jr[u] = kb + u * G;
         ic[u] = i;
         ix[u] = base + (int64_t)jr[u] * g.inner + c;
         v[u] = psi[ix[u]];
       }
-      apply_ops<8>(p, 0, tp.mat_op[0], v, jr, ic, ix, o, acc, scale_v);
+      apply_ops<4>(p, 0, tp.mat_op[0], v, jr, ic, ix, o, acc, scale_v);
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
+      for (int u = 0; u < 4; ++u) {
         float rh, rl, ih, il;
         split_tf32(v[u].x, rh, rl);
         split_tf32(v[u].y, ih, il);
@@ -305,27 +315,30 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
   __syncthreads();
 
   const uint32_t idesc = idesc_tf32(128, (uint32_t)S.nc);
-  // MMA issue for matrix m: chunk q accumulates into TMEM region (q * nacc / nk) * 128
+  // MMA issue for matrix m.  K step t (of ksteps) puts A_hi B_hi into main region
+  // t * nmain / ksteps and the two corrections into the last region (nmain).
   auto run_gemm = [&](int m) -> bool {
+    const int kpc = S.chunk_k / 8;  // K steps per chunk
     for (int q = 0; q < S.nk; ++q) {
       const int c = m * S.nk + q, s = c & 1;
-      const int a = q * S.nacc / S.nk;
-      const bool first_of_acc = (q * S.nacc) % S.nk == 0;
       if (!mbar_wait(&full[s], (uint32_t)((c >> 1) & 1), kWaitLimit)) return false;
       tc_fence_after();
-      const int ksteps = S.chunk_k / 8;
-      for (int ks = 0; ks < ksteps; ++ks) {
+      for (int ks = 0; ks < kpc; ++ks) {
+        const int t = q * kpc + ks;
+        const int rm = t * S.nmain / S.ksteps;
+        const bool first_main = t == 0 || rm != (t - 1) * S.nmain / S.ksteps;
         const int kg = q * S.chunk_k + ks * 8;
         const uint64_t bh = smem_desc(reinterpret_cast<unsigned char*>(bhi) + (kg >> 2) * kLboB, kLboB, L.sbo_b);
         const uint64_t bl = smem_desc(reinterpret_cast<unsigned char*>(blo) + (kg >> 2) * kLboB, kLboB, L.sbo_b);
         for (int hh = 0; hh < S.mh; ++hh) {
-          const uint32_t d = tmem + (uint32_t)(a * 128 + hh * 64);
+          const uint32_t dm = tmem + (uint32_t)(rm * S.reg_cols + hh * S.nc);
+          const uint32_t dc = tmem + (uint32_t)(S.nmain * S.reg_cols + hh * S.nc);
           const int aoff = hh * 16 * S.sbo_a + ks * 256;
           const uint64_t ahi = smem_desc(stage[s] + aoff, 128, (uint32_t)S.sbo_a);
           const uint64_t alo = smem_desc(stage[s] + kChunkBytes + aoff, 128, (uint32_t)S.sbo_a);
-          mma_tf32(d, ahi, bh, idesc, (first_of_acc && ks == 0) ? 0u : 1u);
-          mma_tf32(d, ahi, bl, idesc, 1u);
-          mma_tf32(d, alo, bh, idesc, 1u);
+          mma_tf32(dm, ahi, bh, idesc, first_main ? 0u : 1u);
+          mma_tf32(dc, ahi, bl, idesc, t == 0 ? 0u : 1u);
+          mma_tf32(dc, alo, bh, idesc, 1u);
         }
       }
       mma_commit(&empty[s]);
@@ -341,11 +354,10 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
   };
 
   // epilogue mapping: warp w reads TMEM lanes 32 (w & 3) .. +31; upper warps take the
-  // second column half (n <= 128) or the second 128-row half (n = 256)
+  // second 16-column chunk (n <= 128) or the second 128-row half (n = 256, both chunks)
   const int lg = warp & 3, up = warp >> 2;
   const int j = (S.mh == 2 ? 128 * up : 0) + 32 * lg + lane;  // lane-axis row
   const bool row_ok = j < n;
-  const int cbase = S.mh == 2 ? 0 : 32 * up;  // first complex column of this thread
   float* stg = bhi;  // output staging reuses the B_hi area once the last GEMM is done
 
   for (int m = 0; m < tp.nmat; ++m) {
@@ -365,18 +377,21 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
     const bool last = m + 1 == tp.nmat;
     // ops between this matrix and the next one (or the end of the program)
     const int sb = tp.mat_op[m] + 1, se = last ? p.nops : tp.mat_op[m + 1];
-    for (int cc = 0; cc < 2; ++cc) {
+    for (int cc = 0; cc < S.mh; ++cc) {
+      const int ch = S.mh == 1 ? up : cc;  // 16-column chunk of this thread
+      const uint32_t col = (uint32_t)((S.mh == 2 ? S.nc * up : 0) + 32 * ch);
+      const uint32_t lane_addr = tmem + ((uint32_t)(lg * 32) << 16) + col;
+      // main regions in order, then the correction region; round-to-nearest FP32 adds
       float v[32];
-      const uint32_t col = (uint32_t)(64 * up + 32 * cc);
-      tmem_ld32(tmem + ((uint32_t)(lg * 32) << 16) + col, v);
-      for (int a = 1; a < S.nacc; ++a) {
+      tmem_ld32(lane_addr, v);
+      for (int r = 1; r <= S.nmain; ++r) {
         float w2[32];
-        tmem_ld32(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(a * 128) + col, w2);
+        tmem_ld32(lane_addr + (uint32_t)(r * S.reg_cols), w2);
 #pragma unroll
         for (int e = 0; e < 32; ++e) v[e] += w2[e];
       }
       if (row_ok) {
-        const int c0 = cbase + 16 * cc;  // complex column of v[0..1]
+        const int c0 = 16 * ch;  // complex column of v[0..1]
         float2 x[16];
         int jr[16];
         int64_t ic[16], ix[16];
@@ -416,9 +431,9 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
   if (!s_fail) {
     // coalesced store of the staged tile: thread = complex column
     const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
-    for (int kb = h; kb < n; kb += 8 * G) {
+    for (int kb = h; kb < n; kb += 4 * G) {
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
+      for (int u = 0; u < 4; ++u) {
         const int k = kb + u * G;
         psi[base + (int64_t)k * g.inner + c] = *reinterpret_cast<const float2*>(stg + k * S.stage_row + 2 * c);
       }

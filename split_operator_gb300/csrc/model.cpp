@@ -1225,12 +1225,21 @@ Batch::Batch(std::vector<Propagation*> props) : props_(std::move(props)) {
       throw Error(SO_ERR_UNSUPPORTED, "batched propagations need multi-lane (2-D or larger) states");
   }
   stream_ = props_[0]->engine().stream;
+  if (stream_ == nullptr) {
+    // graph capture needs a stream other than the legacy default stream
+    cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "batch stream");
+    own_stream_ = true;
+  }
 }
 
 Batch::~Batch() {
   for (Timed& t : timed_) {
     cudaEventDestroy(t.a);
     cudaEventDestroy(t.b);
+  }
+  if (own_stream_) {
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
   }
 }
 

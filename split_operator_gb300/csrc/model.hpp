@@ -437,6 +437,7 @@ class Batch {
   void run_groups(std::vector<Group>& gs);
   std::vector<Propagation*> props_;
   cudaStream_t stream_ = nullptr;
+  bool own_stream_ = false;
   bool timing_ = false;
   size_t launches_per_step_ = 0;
   struct Timed {
