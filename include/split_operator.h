@@ -285,6 +285,25 @@ int so_batch_kernel_times(so_batch b, char* buf, size_t cap);
 int so_batch_launches_per_step(so_batch b, size_t* out);
 void so_batch_free(so_batch b);
 
+/* ---- Learned starting states (no counterpart in the reference) ----
+ * A multilayer perceptron (tanh hidden layers, linear output) trained with hand-written
+ * CUDA kernels: BF16 weights in the forward and backward products, FP32 accumulation,
+ * FP32 master weights updated by Adam.  Used to predict the starting wave function of
+ * imaginary-time relaxation from the potential parameters.  Host arrays are FP32. */
+typedef struct so_mlp_t* so_mlp;
+int so_mlp_new(const int* widths, size_t count, uint64_t seed, so_mlp* out);
+int so_mlp_num_params(so_mlp m, size_t* out);
+/* parameters layer by layer: W (out x in, row-major) then b */
+int so_mlp_get_params(so_mlp m, float* out);
+int so_mlp_set_params(so_mlp m, const float* in);
+int so_mlp_forward(so_mlp m, const float* x, size_t batch, float* y);
+/* mean squared error of forward(x) against target and its gradient (parameter order above) */
+int so_mlp_gradients(so_mlp m, const float* x, const float* target, size_t batch, double* loss, float* grads);
+/* `steps` full-batch Adam steps; losses[i] (may be NULL) = loss before step i */
+int so_mlp_train(so_mlp m, const float* x, const float* target, size_t batch, size_t steps, float lr,
+                 double* losses);
+void so_mlp_free(so_mlp m);
+
 /* ---- Allocation-free lane FFT + norm (no counterpart in the reference) ----
  * For callers that must not allocate GPU memory, or let a library allocate it, while
  * they run: code inside a strict device memory pool, or a host framework that hands

@@ -135,6 +135,13 @@ SIGNATURES = {
     "so_batch_set_timing": [_P, _I],
     "so_batch_kernel_times": [_P, C.c_char_p, _S],
     "so_batch_launches_per_step": [_P, _SP],
+    "so_mlp_new": [C.POINTER(C.c_int), _S, C.c_uint64, _PP],
+    "so_mlp_num_params": [_P, _SP],
+    "so_mlp_get_params": [_P, C.POINTER(C.c_float)],
+    "so_mlp_set_params": [_P, C.POINTER(C.c_float)],
+    "so_mlp_forward": [_P, C.POINTER(C.c_float), _S, C.POINTER(C.c_float)],
+    "so_mlp_gradients": [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), _S, _DP, C.POINTER(C.c_float)],
+    "so_mlp_train": [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), _S, _S, C.c_float, _DP],
 }
 VOID = {
     "so_grid_free": [_P],
@@ -143,6 +150,7 @@ VOID = {
     "so_operation_stack_free": [_P],
     "so_propagation_free": [_P],
     "so_batch_free": [_P],
+    "so_mlp_free": [_P],
 }
 OTHER = {"so_last_error": ([], C.c_char_p)}
 

@@ -686,6 +686,56 @@ class Batch(_Handle):
         return v.value
 
 
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Mlp(_Handle):
+    """Multilayer perceptron trained by the library's CUDA kernels (tanh hidden layers)."""
+
+    _free = "so_mlp_free"
+
+    def __init__(self, widths: Sequence[int], seed: int = 0):
+        w = (C.c_int * len(widths))(*widths)
+        super().__init__(_new("so_mlp_new", w, len(widths), seed))
+        self.widths = list(widths)
+
+    def num_params(self) -> int:
+        v = C.c_size_t()
+        call("so_mlp_num_params", self._h, C.byref(v))
+        return v.value
+
+    def get_params(self):
+        out = np.empty(self.num_params(), dtype=np.float32)
+        call("so_mlp_get_params", self._h, _fp(out))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        call("so_mlp_set_params", self._h, _fp(p))
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty((x.shape[0], self.widths[-1]), dtype=np.float32)
+        call("so_mlp_forward", self._h, _fp(x), x.shape[0], _fp(y))
+        return y
+
+    def gradients(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.empty(self.num_params(), dtype=np.float32)
+        loss = C.c_double()
+        call("so_mlp_gradients", self._h, _fp(x), _fp(t), x.shape[0], C.byref(loss), _fp(g))
+        return loss.value, g
+
+    def train(self, x, t, steps: int, lr: float = 1e-3):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        losses = np.empty(steps)
+        call("so_mlp_train", self._h, _fp(x), _fp(t), x.shape[0], steps, lr, _dp(losses))
+        return losses
+
+
 def launch_count() -> int:
     v = C.c_uint64()
     call("so_launch_count", C.byref(v))

@@ -1,0 +1,227 @@
+"""Learned starting states for imaginary-time ground-state relaxation.
+
+No counterpart in the reference crate.  Pipeline:
+
+1. Potential parameter sets (D, a, re, beta, mass) -- D in [0.05, 0.2], a in
+   [0.6, 1.4], re in [2, 4], beta in [0, 0.05], mass in [500, 2000] -- seeded
+   (training: default_rng(5), held out: default_rng(6)).
+2. Ground states of V = D (1 - e^{-a(r-re)})^2 + beta e^{-r/2} P2(cos th) on an
+   Nr x Ntheta radial x Gauss-Legendre grid, found by the plain FP64 solver:
+   imaginary time dt = -i * 1.0, stack [LeakControl(+loss), V/2, Legendre, Rot/2,
+   FFT, K], renormalised every step, energies from Propagation::mean_energy, run
+   until successive energies differ by <= 1e-10.  Many instances run together
+   through the batched executor.
+3. A radial basis per l: the leading `modes` left singular vectors of the training
+   ground states' radial functions at that l (eigenvectors of their covariance).
+4. A multilayer perceptron (5 -> 256 -> 256 -> 256 -> Ntheta*modes, BF16 weights, FP32
+   accumulation) trained on the library's own CUDA kernels to map the scaled
+   parameters to the standardised basis coefficients.
+5. Held-out evaluation: steps and wall time until |E - E*| <= 1e-8 (E* = the plain
+   solver's converged energy) from the learned start and from the plain Gaussian start.
+
+Set-up arithmetic (grids, Legendre matrices, basis) is host numpy; every propagation
+and every network product runs in the library's kernels.
+"""
+import argparse
+import json
+import math
+import time
+
+import numpy as np
+
+from . import api as so
+
+PARAM_LO = np.array([0.05, 0.6, 2.0, 0.0, 500.0])
+PARAM_HI = np.array([0.2, 1.4, 4.0, 0.05, 2000.0])
+
+
+def param_sets(count, seed):
+    rng = np.random.default_rng(seed)
+    return PARAM_LO + (PARAM_HI - PARAM_LO) * rng.uniform(size=(count, 5))
+
+
+def scale_params(p):
+    return (2.0 * (np.asarray(p) - PARAM_LO) / (PARAM_HI - PARAM_LO) - 1.0).astype(np.float32)
+
+
+class Grid2D:
+    """Radial x Gauss-Legendre grid and the Legendre matrices of legendre_diagonalization.rs:13-45."""
+
+    def __init__(self, nr=2048, nth=64, r_min=0.5, r_max=16.5):
+        self.nr, self.nth, self.r_min, self.r_max = nr, nth, r_min, r_max
+        step = (r_max - r_min) / (nr - 1.0)
+        self.r = np.array([r_min + step * i for i in range(nr)])
+        self.x, self.w = np.polynomial.legendre.leggauss(nth)
+        tinv = np.empty((nth, nth))
+        for l in range(nth):
+            tinv[:, l] = math.sqrt(l + 0.5) * np.polynomial.legendre.Legendre.basis(l)(self.x)
+        self.tinv = tinv                      # theta <- l
+        self.t = (tinv * self.w[:, None]).T   # l <- theta
+
+    def to_l(self, psi):  # psi[r, theta] -> psi[r, l]
+        return psi @ self.t.T
+
+    def to_theta(self, psi_l):
+        return psi_l @ self.tinv.T
+
+
+def problem(prm, g: Grid2D, psi0=None, precision="fp64"):
+    d, a, re, beta, mass = [float(v) for v in prm]
+    radial = so.Grid.new_linear_continuos("radial", g.r_min, g.r_max, g.nr, 0)
+    polar = so.Grid.new_custom("polar", np.arccos(g.x), g.w, 1)
+    r = g.r
+    p2 = 0.5 * (3.0 * g.x * g.x - 1.0)
+    v = (d * (1.0 - np.exp(-a * (r - re))) ** 2)[:, None] + (beta * np.exp(-r / 2.0))[:, None] * p2[None, :]
+    if psi0 is None:
+        # plain Gaussian start: isotropic, centred on the well, width 0.5
+        psi0 = np.exp(-((r - re) / (2.0 * 0.5)) ** 2)[:, None] * np.ones(g.nth)[None, :]
+    wf = so.WaveFunction(np.asarray(psi0, dtype=np.complex128), [radial, polar])
+    wf.normalize(1.0)
+    tg = so.TimeGrid(1.0, 10 ** 6, True)
+    leak = so.LeakControl()
+    leak.add_loss_checker("leak control")
+    st = so.OperationStack()
+    st.add_control(leak, so.FIRST_HALF | so.SECOND_HALF)
+    st.add_propagator(so.n_dim_into_propagator(v, tg, so.HALF))
+    st.add_transformation(so.legendre_diagonalization_operator(polar), so.NORMAL)
+    st.add_propagator(so.n_dim_into_propagator(so.rotational_hamiltonian(radial, polar, mass, 0.0), tg, so.HALF))
+    st.add_transformation(so.FFTTransformation(radial, "momentum"), so.NORMAL)
+    st.add_propagator(so.one_dim_into_propagator(so.kinetic_hamiltonian(radial, mass), radial, tg, so.FULL))
+    return so.Propagation(wf, tg, st, precision)
+
+
+def relax(props, every=20, max_steps=20000, tol=None, target=None, group=512):
+    """Imaginary-time steps until successive energies (every `every` steps) differ by
+    <= tol, or until |E - target[i]| <= 1e-8 when `target` is given.  Returns
+    (energies, steps incl. the energy evaluations, wall seconds)."""
+    n = len(props)
+    energy = np.full(n, np.nan)
+    prev = np.full(n, np.nan)
+    steps = np.zeros(n, dtype=np.int64)
+    done = np.zeros(n, dtype=bool)
+    t0 = time.perf_counter()
+    while not done.all():
+        active = [i for i in range(n) if not done[i]]
+        for s in range(0, len(active), group):
+            idx = active[s:s + group]
+            so.Batch([props[i] for i in idx]).steps(every)
+            for i in idx:
+                steps[i] += every + 1  # mean_energy runs one more step
+                e = props[i].mean_energy()
+                energy[i] = e
+                if target is not None:
+                    done[i] = abs(e - target[i]) <= 1e-8
+                else:
+                    done[i] = np.isfinite(prev[i]) and abs(e - prev[i]) <= tol
+                prev[i] = e
+                if steps[i] >= max_steps:
+                    done[i] = True
+    return energy, steps, time.perf_counter() - t0
+
+
+def ground_states(params, g: Grid2D, tol=1e-10, every=20, max_steps=20000, chunk=512):
+    """FP64 ground states (real parts, [count, nr, nth]), energies and step counts."""
+    states = np.empty((len(params), g.nr, g.nth), dtype=np.float32)
+    energies = np.empty(len(params))
+    nsteps = np.empty(len(params), dtype=np.int64)
+    for s in range(0, len(params), chunk):
+        props = [problem(p, g) for p in params[s:s + chunk]]
+        e, st, _ = relax(props, every=every, max_steps=max_steps, tol=tol)
+        for k, p in enumerate(props):
+            states[s + k] = p.get_array().real
+        energies[s:s + len(props)] = e
+        nsteps[s:s + len(props)] = st
+        del props
+    return states, energies, nsteps
+
+
+class RadialBasis:
+    """Per l: the leading `modes` left singular vectors of the training radial functions."""
+
+    def __init__(self, states, g: Grid2D, modes=64):
+        self.modes = modes
+        nl = g.nth
+        psil = np.stack([g.to_l(s.astype(np.float64)) for s in states])  # [count, nr, nl]
+        self.u = np.empty((nl, g.nr, modes))
+        for l in range(nl):
+            x = psil[:, :, l].T  # [nr, count]
+            cov = x @ x.T
+            evals, evecs = np.linalg.eigh(cov)
+            self.u[l] = evecs[:, ::-1][:, :modes]
+        self.g = g
+
+    def coefficients(self, state):
+        psil = self.g.to_l(np.asarray(state, dtype=np.float64))
+        return np.einsum("lrm,rl->lm", self.u, psil)
+
+    def state(self, coef):
+        psil = np.einsum("lrm,lm->rl", self.u, coef)
+        return self.g.to_theta(psil)
+
+
+class LearnedStart:
+    def __init__(self, basis: RadialBasis, hidden=(256, 256, 256), seed=0):
+        self.basis = basis
+        nout = basis.g.nth * basis.modes
+        self.net = so.Mlp([5, *hidden, nout], seed=seed)
+        self.mean = None
+        self.std = None
+
+    def fit(self, params, states, steps=3000, lr=1e-3):
+        coef = np.stack([self.basis.coefficients(s).ravel() for s in states])
+        self.mean = coef.mean(axis=0)
+        self.std = coef.std(axis=0) + 1e-12 * np.abs(coef).max()
+        y = ((coef - self.mean) / self.std).astype(np.float32)
+        return self.net.train(scale_params(params), y, steps=steps, lr=lr)
+
+    def predict(self, params):
+        y = self.net.forward(scale_params(params)).astype(np.float64)
+        coef = y * self.std + self.mean
+        return [self.basis.state(c.reshape(self.basis.g.nth, self.basis.modes)) for c in coef]
+
+
+def evaluate(model: LearnedStart, params, g: Grid2D, every=5, max_steps=20000, tol=1e-10):
+    """Held-out comparison: plain solver energies E* first, then both starts to |E - E*| <= 1e-8."""
+    _, e_star, steps_plain_full = ground_states(params, g, tol=tol, every=20, max_steps=max_steps)
+    gauss = [problem(p, g) for p in params]
+    _, steps_g, wall_g = relax(gauss, every=every, max_steps=max_steps, target=e_star)
+    starts = model.predict(params)
+    learned = [problem(p, g, psi0=s) for p, s in zip(params, starts)]
+    _, steps_l, wall_l = relax(learned, every=every, max_steps=max_steps, target=e_star)
+    return {"heldout": len(params), "energy_star_mean": float(np.mean(e_star)),
+            "steps_gaussian_mean": float(np.mean(steps_g)), "steps_learned_mean": float(np.mean(steps_l)),
+            "wall_s_gaussian": wall_g, "wall_s_learned": wall_l,
+            "wall_ratio_learned_over_gaussian": wall_l / wall_g,
+            "steps_ratio_learned_over_gaussian": float(np.mean(steps_l) / np.mean(steps_g)),
+            "converged_gaussian": int(np.sum(steps_g < max_steps)), "converged_learned": int(np.sum(steps_l < max_steps))}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=4096)
+    ap.add_argument("--heldout", type=int, default=256)
+    ap.add_argument("--nr", type=int, default=2048)
+    ap.add_argument("--nth", type=int, default=64)
+    ap.add_argument("--modes", type=int, default=64)
+    ap.add_argument("--epochs", type=int, default=3000)
+    ap.add_argument("--out", default="learned_start.json")
+    a = ap.parse_args()
+    g = Grid2D(a.nr, a.nth)
+    t0 = time.perf_counter()
+    ptrain = param_sets(a.train, 5)
+    states, energies, nsteps = ground_states(ptrain, g)
+    t_data = time.perf_counter() - t0
+    basis = RadialBasis(states, g, a.modes)
+    model = LearnedStart(basis)
+    losses = model.fit(ptrain, states, steps=a.epochs)
+    res = evaluate(model, param_sets(a.heldout, 6), g)
+    res.update({"train": a.train, "grid": [a.nr, a.nth], "modes": a.modes, "train_loss_first": float(losses[0]),
+                "train_loss_last": float(losses[-1]), "data_generation_s": t_data,
+                "train_steps_mean": float(np.mean(nsteps))})
+    with open(a.out, "w") as f:
+        json.dump(res, f, indent=1)
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()
