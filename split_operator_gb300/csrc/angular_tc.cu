@@ -131,13 +131,97 @@ __device__ __forceinline__ int64_t coord_of(const Geometry& g, int a, int64_t o,
   return 0;
 }
 
-// Point-wise ops [ob, oe) on NB values: value u sits at lane-axis row jr[u], inner
-// column ic[u], storage index ix[u].  Each op touches all NB values before the next
-// op, so table loads of one op are independent of each other.
+// Per-tile factors of the point-wise ops, built once per tile so that the per-point
+// work reads shared memory and does FP32 arithmetic only (FP64 runs on a narrow pipe).
+struct TileTabs {
+  float colw[kMaxRed][32];   // NORM: product of the FP32 weights of every non-lane axis, per tile column
+  float2 colt[kMaxOps][32];  // DIAG1D on a non-lane axis: the table value of each tile column
+  float scale[kMaxOps];      // SCALE: sqrt(target / norm)
+};
+
+__device__ __forceinline__ void build_tile_tabs(const PassParams& p, TileTabs& T, int64_t o, int64_t i0, int bn) {
+  const Geometry& g = p.g;
+  for (int idx = threadIdx.x; idx < p.nops * bn; idx += blockDim.x) {
+    const int oi = idx / bn, c = idx - oi * bn;
+    const DevOp& op = p.ops[oi];
+    const int64_t i = i0 + c;
+    if (op.kind == OP_NORM) {
+      float w = 1.0f;
+      for (int a = 0; a < g.ndim; ++a)
+        if (a != g.sweep_axis) w *= __ldg(op.wf[a] + coord_of(g, a, o, i));
+      T.colw[op.red][c] = w;
+    } else if (op.kind == OP_DIAG1D && op.axis != g.sweep_axis) {
+      T.colt[oi][c] = __ldg(reinterpret_cast<const float2*>(op.ptr) + coord_of(g, op.axis, o, i));
+    } else if (op.kind == OP_SCALE && c == 0) {
+      T.scale[oi] = (float)sqrt(__ldcg(p.slots + op.b) / __ldcg(p.slots + op.c));
+    }
+  }
+}
+
+// Point-wise ops [ob, oe) on the NB values of one lane-axis row j, tile columns
+// c0 .. c0 + NB - 1 (storage indices ix0 .. ix0 + NB - 1): the epilogue layout.
 template <int NB>
-__device__ __forceinline__ void apply_ops(const PassParams& p, int ob, int oe, float2 (&v)[NB], const int (&jr)[NB],
-                                          const int64_t (&ic)[NB], const int64_t (&ix)[NB], int64_t o, double* acc,
-                                          const double* sc) {
+__device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T, int ob, int oe, float2 (&v)[NB],
+                                          int j, int c0, int64_t ix0, double* acc) {
+  const Geometry& g = p.g;
+  for (int oi = ob; oi < oe; ++oi) {
+    const DevOp& op = p.ops[oi];
+    switch (op.kind) {
+      case OP_DIAG1D: {
+        if (op.axis == g.sweep_axis) {
+          const float2 t = __ldg(reinterpret_cast<const float2*>(op.ptr) + j);
+#pragma unroll
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], t);
+        } else {
+#pragma unroll
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], T.colt[oi][c0 + u]);
+        }
+        break;
+      }
+      case OP_DIAGND: {
+        const float2* t = reinterpret_cast<const float2*>(op.ptr) + ix0;
+        if ((reinterpret_cast<uintptr_t>(t) & 15u) == 0) {
+          float4 tv[NB / 2];
+#pragma unroll
+          for (int q = 0; q < NB / 2; ++q) tv[q] = __ldg(reinterpret_cast<const float4*>(t) + q);
+#pragma unroll
+          for (int q = 0; q < NB / 2; ++q) {
+            v[2 * q] = cmulf(v[2 * q], make_float2(tv[q].x, tv[q].y));
+            v[2 * q + 1] = cmulf(v[2 * q + 1], make_float2(tv[q].z, tv[q].w));
+          }
+        } else {
+          float2 tv[NB];
+#pragma unroll
+          for (int u = 0; u < NB; ++u) tv[u] = __ldg(t + u);
+#pragma unroll
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tv[u]);
+        }
+        break;
+      }
+      case OP_SCALE: {
+        const float f = T.scale[oi];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) v[u] = {v[u].x * f, v[u].y * f};
+        break;
+      }
+      case OP_NORM: {
+        float s = 0.0f;
+#pragma unroll
+        for (int u = 0; u < NB; ++u) s = fmaf(fmaf(v[u].x, v[u].x, v[u].y * v[u].y), T.colw[op.red][c0 + u], s);
+        acc[op.red] += (double)(s * __ldg(op.wf[g.sweep_axis] + j));
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
+// Point-wise ops [ob, oe) on the NB values of one tile column c, lane-axis rows jr[u]
+// (storage indices ix[u]): the prologue layout.
+template <int NB>
+__device__ __forceinline__ void apply_col(const PassParams& p, const TileTabs& T, int ob, int oe, float2 (&v)[NB],
+                                          const int (&jr)[NB], int c, const int64_t (&ix)[NB], double* acc) {
   const Geometry& g = p.g;
   for (int oi = ob; oi < oe; ++oi) {
     const DevOp& op = p.ops[oi];
@@ -145,11 +229,15 @@ __device__ __forceinline__ void apply_ops(const PassParams& p, int ob, int oe, f
       case OP_DIAG1D: {
         const float2* t = reinterpret_cast<const float2*>(op.ptr);
         if (op.axis == g.sweep_axis) {
+          float2 tv[NB];
 #pragma unroll
-          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], __ldg(t + jr[u]));
+          for (int u = 0; u < NB; ++u) tv[u] = __ldg(t + jr[u]);
+#pragma unroll
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tv[u]);
         } else {
+          const float2 tc = T.colt[oi][c];
 #pragma unroll
-          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], __ldg(t + coord_of(g, op.axis, o, ic[u])));
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tc);
         }
         break;
       }
@@ -163,21 +251,17 @@ __device__ __forceinline__ void apply_ops(const PassParams& p, int ob, int oe, f
         break;
       }
       case OP_SCALE: {
-        const float f = (float)sc[oi];
+        const float f = T.scale[oi];
 #pragma unroll
         for (int u = 0; u < NB; ++u) v[u] = {v[u].x * f, v[u].y * f};
         break;
       }
       case OP_NORM: {
-        double s = 0.0;
+        const float* wr = op.wf[g.sweep_axis];
+        float s = 0.0f;
 #pragma unroll
-        for (int u = 0; u < NB; ++u) {
-          double w = op.w[g.sweep_axis][jr[u]];
-          for (int a = 0; a < g.ndim; ++a)
-            if (a != g.sweep_axis) w *= op.w[a][coord_of(g, a, o, ic[u])];
-          s += ((double)v[u].x * v[u].x + (double)v[u].y * v[u].y) * w;
-        }
-        acc[op.red] += s;
+        for (int u = 0; u < NB; ++u) s = fmaf(fmaf(v[u].x, v[u].x, v[u].y * v[u].y), __ldg(wr + jr[u]), s);
+        acc[op.red] += (double)(s * T.colw[op.red][c]);
         break;
       }
       default:
@@ -215,17 +299,22 @@ struct TcParams {
   int32_t error_slot;
 };
 
-__device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) {
+__device__ __forceinline__ void tc_tile(const TcParams& gtp, const int64_t tile) {
   using namespace tc;
-  const PassParams& p = tp.p;
-  const Geometry& g = p.g;
   extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ __align__(16) TcParams tp;
+  __shared__ TileTabs tabs;
   __shared__ uint32_t tmem_base_s;
   __shared__ double scratch[kThreads / 32];
   __shared__ double blk_red[kMaxRed];
   __shared__ double totals[kMaxRed];
-  __shared__ double scale_v[kMaxOps];
   __shared__ int s_last, s_fail;
+  static_assert(sizeof(TcParams) % 4 == 0, "TcParams is copied as 32-bit words");
+  for (int k = threadIdx.x; k < (int)(sizeof(TcParams) / 4); k += kThreads)
+    reinterpret_cast<uint32_t*>(&tp)[k] = reinterpret_cast<const uint32_t*>(&gtp)[k];
+  __syncthreads();
+  const PassParams& p = tp.p;
+  const Geometry& g = p.g;
 
   const int n = (int)g.n;
   const TcShape S = tc_shape(n);
@@ -255,10 +344,7 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
     fence_mbar_init();
     s_fail = 0;
   }
-  if (tid < kMaxOps) {
-    const DevOp& op = p.ops[tid < p.nops ? tid : 0];
-    scale_v[tid] = (tid < p.nops && op.kind == OP_SCALE) ? sqrt(__ldcg(p.slots + op.b) / __ldcg(p.slots + op.c)) : 0.0;
-  }
+  build_tile_tabs(p, tabs, o, i0, S.bn);
   if (warp == 0) tmem_alloc(&tmem_base_s, tmem_cols);
   tc_fence_before();
   __syncthreads();
@@ -284,20 +370,18 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
   // ---- prologue: thread = complex column c, rows h, h + G, ... (G = groups)
   {
     const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
-    const int64_t i = i0 + c;
     // a thread owns n / G rows (a multiple of 4 for every supported n): batches of 4
     for (int kb = h; kb < n; kb += 4 * G) {
       float2 v[4];
       int jr[4];
-      int64_t ic[4], ix[4];
+      int64_t ix[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         jr[u] = kb + u * G;
-        ic[u] = i;
         ix[u] = base + (int64_t)jr[u] * g.inner + c;
         v[u] = psi[ix[u]];
       }
-      apply_ops<4>(p, 0, tp.mat_op[0], v, jr, ic, ix, o, acc, scale_v);
+      apply_col<4>(p, tabs, 0, tp.mat_op[0], v, jr, c, ix, acc);
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         float rh, rl, ih, il;
@@ -393,16 +477,9 @@ __device__ __forceinline__ void tc_tile(const TcParams& tp, const int64_t tile) 
       if (row_ok) {
         const int c0 = 16 * ch;  // complex column of v[0..1]
         float2 x[16];
-        int jr[16];
-        int64_t ic[16], ix[16];
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          x[u] = {v[2 * u], v[2 * u + 1]};
-          jr[u] = j;
-          ic[u] = i0 + c0 + u;
-          ix[u] = base + (int64_t)j * g.inner + c0 + u;
-        }
-        apply_ops<16>(p, sb, se, x, jr, ic, ix, o, acc, scale_v);
+        for (int u = 0; u < 16; ++u) x[u] = {v[2 * u], v[2 * u + 1]};
+        apply_row<16>(p, tabs, sb, se, x, j, c0, base + (int64_t)j * g.inner + c0, acc);
         if (last) {
 #pragma unroll
           for (int u = 0; u < 16; u += 2)
@@ -522,9 +599,13 @@ void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const floa
   std::memcpy(out, &tp, sizeof(TcParams));
 }
 
+// the largest dynamic shared memory any supported lane extent asks for
+static size_t tc_max_dynamic_smem() { return tc_layout(256).total; }
+
 static bool configure_once(const void* kern, bool& flag) {
   if (flag) return true;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess)
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_max_dynamic_smem()) !=
+      cudaSuccess)
     return false;
   flag = true;
   return true;
@@ -534,7 +615,7 @@ cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* off
                                       size_t smem, cudaStream_t s) {
   static bool configured = false;
   if (!configure_once((const void*)angular_tc_kernel_batched, configured)) return cudaGetLastError();
-  if (smem > 220 * 1024) return cudaErrorInvalidValue;
+  if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
   angular_tc_kernel_batched<<<(unsigned)blocks, kThreads, smem, s>>>(reinterpret_cast<const TcParams*>(params_dev),
                                                                      offsets_dev, count);
   count_launch();
@@ -591,7 +672,7 @@ cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, 
   const size_t smem = angular_tc_smem_bytes((int)p.g.n);
   static bool configured = false;
   if (!configure_once((const void*)angular_tc_kernel, configured)) return cudaGetLastError();
-  if (smem > 220 * 1024) return cudaErrorInvalidValue;
+  if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
   angular_tc_kernel<<<(unsigned)p.g.tiles, kThreads, smem, s>>>(tp);
   count_launch();
   return cudaGetLastError();

@@ -232,8 +232,7 @@ int so_wave_function_dot(so_wave_function a, so_wave_function b, double* out) {
     act.op.a = sr;
     act.op.b = si;
     act.op.ptr = y.eng->psi.ptr;
-    std::vector<const double*> w = x.weight_ptrs();
-    for (size_t k = 0; k < w.size(); ++k) act.op.w[k] = w[k];
+    x.set_weights(act.op);
     x.eng->submit(act);
     const double re = x.eng->read_slot(sr), im = x.eng->read_slot(si);
     x.eng->free_slot(sr);

@@ -51,6 +51,7 @@ struct DevOp {
   double value;   // SETC
   const void* ptr;               // table / matrix base / other wave function
   const double* w[kMaxDims];     // NORM / DOT weights per logical axis
+  const float* wf[kMaxDims];     // the same weights rounded to FP32 (FP32 passes)
 };
 
 struct Geometry {

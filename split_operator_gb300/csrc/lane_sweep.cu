@@ -134,13 +134,11 @@ __device__ __forceinline__ void dft_r(C* a, int s) {
 
 // One Stockham stage of radix RS from src to dst (ping-pong buffers): each
 // thread walks its butterflies one at a time, so it holds RS values at most.
-template <int RS, typename C>
+template <int RS, typename C, typename R>
 __device__ __forceinline__ void stockham_stage(const C* __restrict__ src, C* __restrict__ dst, int L, int n, int ls,
-                                               int p, int dir, const C* __restrict__ tw, bool last, double scale) {
-  using R = decltype(src[0].x);
+                                               int p, int dir, const C* __restrict__ tw, bool last, R sc) {
   const int nb = n / RS;
   const int total = L * nb;
-  const R sc = (R)scale;
   const int estride = n / (RS * p);
   for (int b = threadIdx.x; b < total; b += blockDim.x) {
     const int l = b / nb, i = b - l * nb;
@@ -170,10 +168,20 @@ __device__ __forceinline__ void stockham_stage(const C* __restrict__ src, C* __r
 
 // Unitary DFT of every lane of the tile (radix RMAX stages, then one smaller
 // stage); the result ends in `alt`, and the two buffer pointers are swapped.
+// 1 / sqrt(2^lg) in the state precision: a power of two, times 1/sqrt(2) for odd lg
+// (no FP64 division or square root per thread: both are long sequences on this GPU)
+template <typename R>
+__device__ __forceinline__ R inv_sqrt_pow2(int lg) {
+  R s = (R)1;
+  for (int k = 0; k < lg / 2; ++k) s *= (R)0.5;
+  return (lg & 1) ? s * (R)0.70710678118654752440 : s;
+}
+
 template <int RMAX, typename C>
 __device__ void fft_stockham(C*& buf, C*& alt, const Geometry& g, int dir, const C* __restrict__ tw) {
+  using R = decltype(buf[0].x);
   const int n = (int)g.n, L = g.lanes_per_tile, ls = g.lane_stride;
-  const double scale = 1.0 / sqrt((double)n);
+  const R scale = inv_sqrt_pow2<R>(__ffs(n) - 1);
   int p = 1;
   while (p < n) {
     const int rem = n / p;
@@ -313,6 +321,7 @@ __device__ void run_scalar(const PassParams& p, const DevOp& op, const double* t
 template <typename R, int RMAX>
 __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t tile) {
   using C = typename Cx<R>::T;
+  constexpr bool kF64 = sizeof(R) == 8;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Geometry& g = p.g;
   const int L = g.lanes_per_tile, n = (int)g.n, ls = g.lane_stride;
@@ -334,6 +343,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
   __shared__ double scratch[32];
   __shared__ double blk_red[kMaxRed];
   __shared__ double totals[kMaxRed];
+  __shared__ double scale_s;
   __shared__ int s_last;
 
   const bool pow2 = (n & (n - 1)) == 0;
@@ -422,8 +432,10 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
           break;
         }
         case OP_SCALE: {
-          const double f = sqrt(ld_slot(p.slots, op.b) / ld_slot(p.slots, op.c));
-          const R fr = (R)f;
+          // one thread forms sqrt(target / norm) in FP64, the block reads it back
+          if (tid == 0) scale_s = (R)sqrt(ld_slot(p.slots, op.b) / ld_slot(p.slots, op.c));
+          __syncthreads();
+          const R fr = (R)scale_s;
           for (int pt = tid; pt < total; pt += T) {
             const int l = pow2 ? (pt >> lg) : pt / n, x = pt - l * n;
             const int si = sidx(l, x, ls);
@@ -466,7 +478,19 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
         }
         case OP_NORM:
         case OP_DOT: {
+          const bool f32_norm = !kF64 && op.kind == OP_NORM;
+          float* lane_wf = reinterpret_cast<float*>(lane_w);  // FP32 lane weights share the space
           for (int l = tid; l < L; l += T) {
+            if (f32_norm) {
+              float w = 0.0f;
+              if (lane_base[l] >= 0) {
+                w = 1.0f;
+                for (int a = 0; a < g.ndim; ++a)
+                  if (a != g.sweep_axis) w *= op.wf[a][lane_coord[l * kMaxDims + a]];
+              }
+              lane_wf[l] = w;
+              continue;
+            }
             double w = 1.0;
             if (lane_base[l] < 0) {
               w = 0.0;
@@ -480,7 +504,20 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
           const double* wx = op.w[g.sweep_axis];
           double acc = 0.0, acc_i = 0.0;
           const C* other = reinterpret_cast<const C*>(op.ptr);
-          for (int pt = tid; pt < total; pt += T) {
+          if (f32_norm) {
+            // FP32 state: FP32 products and per-thread partial sum, folded in FP64 once
+            const float* wxf = op.wf[g.sweep_axis];
+            float part = 0.0f;
+            for (int pt = tid; pt < total; pt += T) {
+              int l, x;
+              split(pt, l, x);
+              const C v = buf[sidx(l, x, ls)];
+              const float w = lane_wf[l] * __ldg(wxf + x);
+              part = fmaf(fmaf((float)v.x, (float)v.x, (float)v.y * (float)v.y), w, part);
+            }
+            acc = (double)part;
+          }
+          for (int pt = tid; pt < total && !f32_norm; pt += T) {
             int l, x;
             split(pt, l, x);
             const C v = buf[sidx(l, x, ls)];

@@ -362,11 +362,25 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
 const double* Engine::weights(const Grid& g) {
   auto it = weights_.find(g.uid);
   if (it != weights_.end()) return it->second.as<double>();
+  // n FP64 weights followed by their FP32 roundings (read by the FP32 passes, which
+  // keep FP64 arithmetic out of their per-point work)
+  const size_t n = g.weights.size();
+  std::vector<double> packed(n + (n + 1) / 2, 0.0);
+  std::copy(g.weights.begin(), g.weights.end(), packed.begin());
+  float* f = reinterpret_cast<float*>(packed.data() + n);
+  for (size_t i = 0; i < n; ++i) f[i] = (float)g.weights[i];
   DeviceBuffer b;
-  upload(b, g.weights, stream);
+  upload(b, packed, stream);
   const double* p = b.as<double>();
   weights_.emplace(g.uid, std::move(b));
   return p;
+}
+
+void WaveFunction::set_weights(DevOp& op) {
+  for (size_t a = 0; a < grids.size(); ++a) {
+    op.w[a] = eng->weights(grids[a]);
+    op.wf[a] = reinterpret_cast<const float*>(op.w[a] + grids[a].weights.size());
+  }
 }
 
 const void* Engine::twiddle(size_t n) {
@@ -661,8 +675,7 @@ int norm_slot(WaveFunction& wf, Emitter& em) {
   Action act{};
   act.op.kind = OP_NORM;
   act.op.a = wf.cache_slot;
-  std::vector<const double*> w = wf.weight_ptrs();
-  for (size_t a = 0; a < w.size(); ++a) act.op.w[a] = w[a];
+  wf.set_weights(act.op);
   em.emit(act);
   wf.possible_norm_change = false;
   return wf.cache_slot;
@@ -1114,8 +1127,7 @@ double Propagation::mean_energy() {
   a.op.a = sre;
   a.op.b = sim;
   a.op.ptr = before.ptr;
-  std::vector<const double*> w = wf_->weight_ptrs();
-  for (size_t k = 0; k < w.size(); ++k) a.op.w[k] = w[k];
+  wf_->set_weights(a.op);
   e.submit(a);
   const double re = e.read_slot(sre), im = e.read_slot(sim);
   e.free_slot(sre);

@@ -212,6 +212,7 @@ struct WaveFunction {
   WaveFunction(const std::vector<size_t>& shape, const std::vector<Grid>& grids, const std::vector<int>& perm,
                bool fp64);
   std::vector<const double*> weight_ptrs();
+  void set_weights(DevOp& op);  // op.w / op.wf: FP64 and FP32 weights per logical axis
   size_t points() const;
 };
 

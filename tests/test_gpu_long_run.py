@@ -1,0 +1,91 @@
+"""Long-run accuracy on the 4096 x 128 radial x angular problem (Morse + P2, mass 1000,
+dt = 0.5, border damping with a loss checker), 10^4 real-time steps.
+
+* FP64 GPU path against the C++ FP64 restatement of the reference passes
+  (propagation.rs:134-182 step order): relative L2 <= 1e-9 after 10^4 steps, norm and
+  accumulated loss to the same order.
+* Each FP32 mode against the FP64 GPU path: one step from the same state within
+  relative L2 1e-6; the accumulated error at 10^2, 10^3 and 10^4 steps is reported
+  (written to precision_report.json in $SO_REPORT_DIR when set).
+"""
+import json
+import os
+import time
+
+import numpy as np
+import pytest
+
+from tests.gpu_common import ensure_built, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+NR, NTH = 4096, 128
+CHECKPOINTS = (100, 1000, 10000)
+FP32_MODES = ("fp32_simt", "fp32_tf32x3", "fp32_bf16x3")
+
+
+def _norm(psi, wr, wth):
+    return float(np.sum(np.abs(psi) ** 2 * wr[:, None] * wth[None, :]))
+
+
+def test_long_run_fp64_vs_cpu_restatement_and_fp32_modes(tmp_path):
+    ensure_built()
+    from split_operator_gb300 import workloads as W
+    from oracle import cpu_port
+
+    report = {"problem": f"radial_angular_2d {NR}x{NTH}, dt=0.5, 10^4 steps", "checkpoints": list(CHECKPOINTS)}
+    port = cpu_port.RadialAngular(NR, NTH, dt=0.5, seed=2026)
+    p64, _ = W.radial_angular_2d(nr=NR, nth=NTH, step_no=10 ** 6, precision="fp64")
+    p32 = {m: W.radial_angular_2d(nr=NR, nth=NTH, step_no=10 ** 6, precision=m)[0] for m in FP32_MODES}
+
+    # one step from the same state: each FP32 mode against the FP64 path
+    one = {}
+    x64 = p64.get_array()
+    for m, p in p32.items():
+        q, _ = W.radial_angular_2d(nr=NR, nth=NTH, step_no=10 ** 6, precision="fp64")
+        q.set_array(p.get_array())  # the FP32 mode's own (rounded) start
+        q.steps(1)
+        p.steps(1)
+        one[m] = rel_l2(p.get_array(), q.get_array())
+        p.set_array(x64)
+        p.reset_losses()
+    report["one_step_rel_l2"] = one
+
+    rows = []
+    done = 0
+    t_port = 0.0
+    for cp in CHECKPOINTS:
+        n = cp - done
+        t0 = time.perf_counter()
+        port.run(n)
+        t_port += time.perf_counter() - t0
+        p64.steps(n)
+        for p in p32.values():
+            p.steps(n)
+        done = cp
+        a64 = p64.get_array()
+        row = {"steps": cp,
+               "fp64_vs_cpu_rel_l2": rel_l2(a64, port.psi),
+               "fp64_norm": p64.norm(), "cpu_norm": _norm(port.psi, port.wr, port.wth),
+               "fp64_loss": p64.get_losses()[0], "cpu_loss": float(port.loss[0])}
+        for m, p in p32.items():
+            a = p.get_array()
+            row[m] = {"rel_l2_vs_fp64": rel_l2(a, a64), "norm_drift": p.norm() - row["fp64_norm"],
+                      "loss_diff": p.get_losses()[0] - row["fp64_loss"]}
+        rows.append(row)
+    report["rows"] = rows
+    report["cpu_seconds"] = t_port
+    out = os.environ.get("SO_REPORT_DIR") or str(tmp_path)
+    with open(os.path.join(out, "precision_report.json"), "w") as f:
+        json.dump(report, f, indent=1)
+    print(json.dumps(report))
+
+    for m, e in one.items():
+        assert e <= 1e-6, (m, e)
+    last = rows[-1]
+    assert rows[0]["fp64_vs_cpu_rel_l2"] <= 1e-10
+    assert last["fp64_vs_cpu_rel_l2"] <= 1e-9
+    assert abs(last["fp64_norm"] - last["cpu_norm"]) <= 1e-9
+    assert abs(last["fp64_loss"] - last["cpu_loss"]) <= 1e-9
+    for m in FP32_MODES:
+        assert np.isfinite(last[m]["rel_l2_vs_fp64"])
