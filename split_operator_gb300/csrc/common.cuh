@@ -83,22 +83,29 @@ struct PassParams {
   int32_t repeat;               // resident mode: program repetitions
   int32_t resident;             // 1: single CTA owns the whole array, scalars are immediate
   int32_t nonfinite_slot;       // slot set to 1 if a norm is not finite
+  int32_t one_buffer;           // 1: no op needs the second tile buffer (FFT stages run in place)
   DevOp ops[kMaxOps];
 };
 
 // Host launchers (lane_sweep.cu)
 cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);
 cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s);
-size_t pass_smem_bytes(const Geometry& g, bool fp64, bool fft);
+size_t pass_smem_bytes(const PassParams& p, bool fp64);
 int pass_threads(const Geometry& g);
+// sets p.one_buffer from the pass's ops and geometry (call once p.ops, p.nops, p.g are set)
+void pass_choose_buffers(PassParams& p, bool fp64);
 
 // Tensor-core angular sweep (angular_tc.cu): FP32 state, real lane matrices as 3xTF32.
 int angular_tc_columns(int n);  // complex columns of the inner axis per CTA tile
 bool angular_tc_eligible(const Geometry& g);
+// the pass's point-wise ops fit the per-tile tables of the tensor-core kernel
+bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis);
 size_t angular_tc_smem_bytes(int n);
 void angular_tc_images(const double* m, int n, std::vector<float>& out);
+// trace: optional per-tile phase timestamps (angular_tc_trace_slots() per tile), nullptr: off
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
-                              int error_slot, cudaStream_t s);
+                              int error_slot, cudaStream_t s, unsigned long long* trace = nullptr);
+int angular_tc_trace_slots();
 
 // Batched launches over many propagations' passes (block -> (instance, tile) by offsets)
 cudaError_t launch_pass_batched(bool fp64, const PassParams* params_dev, const int64_t* offsets_dev, int count,

@@ -71,18 +71,52 @@ __device__ __forceinline__ void dft4(C& a0, C& a1, C& a2, C& a3, int s) {
   a3 = csub(e1, o1);
 }
 
+// The rotation constants of the radix-8/16 butterflies, as FP64 values and, for the
+// FP32 path, as hi + lo pairs: a single rounded FP32 constant has |e^{i phi}| != 1 by
+// a fixed amount, and since every butterfly reuses the same few constants that error
+// would shrink (or grow) the norm systematically, stage after stage.
+constexpr double kC1 = 0.92387953251128675613;  // cos(pi/8)
+constexpr double kC2 = 0.70710678118654752440;  // cos(pi/4)
+constexpr double kC3 = 0.38268343236508977173;  // sin(pi/8)
+
+template <typename R>
+struct RotConst {
+  R hi, lo;
+};
+// FP32: hi = the constant rounded to FP32, lo = the FP32 rounding of the remainder
+// (literal values, so no FP64 arithmetic runs per butterfly); FP64: the constant itself
+template <typename R>
+__device__ __forceinline__ RotConst<R> rot_const(int which) {
+  if constexpr (sizeof(R) == 4) {
+    constexpr float hi[3] = {0x1.d906bcp-1f, 0x1.6a09e6p-1f, 0x1.87de2ap-2f};
+    constexpr float lo[3] = {0x1.e651a8p-26f, 0x1.9fcef4p-27f, 0x1.abaa58p-28f};
+    return {hi[which], lo[which]};
+  } else {
+    constexpr double v[3] = {kC1, kC2, kC3};
+    return {v[which], 0.0};
+  }
+}
+// x * c with the constant carried as hi + lo
+template <typename R>
+__device__ __forceinline__ R mulc(R x, RotConst<R> c) {
+  if constexpr (sizeof(R) == 4)
+    return fmaf(x, c.lo, x * c.hi);
+  else
+    return x * c.hi;
+}
+
 template <typename C>
 __device__ __forceinline__ void dft8(C* a, int s) {
   using R = decltype(a[0].x);
-  const R h = (R)0.70710678118654752440;
+  const RotConst<R> h = rot_const<R>(1);
   C e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
   C o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
   dft4(e0, e1, e2, e3, s);
   dft4(o0, o1, o2, o3, s);
   // o_q *= w8^q, w8 = e^{s 2 pi i / 8}
-  o1 = C{h * (o1.x - s * o1.y), h * (s * o1.x + o1.y)};
+  o1 = C{mulc<R>(o1.x - s * o1.y, h), mulc<R>(s * o1.x + o1.y, h)};
   o2 = mul_si(o2, s);
-  o3 = C{h * (-o3.x - s * o3.y), h * (s * o3.x - o3.y)};
+  o3 = C{mulc<R>(-o3.x - s * o3.y, h), mulc<R>(s * o3.x - o3.y, h)};
   a[0] = cadd(e0, o0);
   a[4] = csub(e0, o0);
   a[1] = cadd(e1, o1);
@@ -104,13 +138,22 @@ __device__ __forceinline__ void dft16(C* a, int s) {
   }
   dft8(e, s);
   dft8(o, s);
-  const R c1 = (R)0.92387953251128675613, c2 = (R)0.70710678118654752440, c3 = (R)0.38268343236508977173;
-  const R cs[8] = {(R)1, c1, c2, c3, (R)0, -c3, -c2, -c1};
-  const R sn[8] = {(R)0, c3, c2, c1, (R)1, c1, c2, c3};
+  // o_q *= w16^q = (cos(q pi/8), s sin(q pi/8)): q = 4 is (0, s); the others use the
+  // hi + lo constants (c x - s' y with both products corrected)
+  const RotConst<R> c1 = rot_const<R>(0), c2 = rot_const<R>(1), c3 = rot_const<R>(2);
+  const RotConst<R> cs[8] = {{(R)1, (R)0}, c1, c2, c3, {(R)0, (R)0}, {-c3.hi, -c3.lo}, {-c2.hi, -c2.lo},
+                             {-c1.hi, -c1.lo}};
+  const RotConst<R> sn[8] = {{(R)0, (R)0}, c3, c2, c1, {(R)1, (R)0}, c1, c2, c3};
 #pragma unroll
   for (int q = 1; q < 8; ++q) {
-    C w = C{cs[q], (R)s * sn[q]};
-    o[q] = cmul(o[q], w);
+    if (q == 4) {
+      o[q] = mul_si(o[q], s);
+      continue;
+    }
+    const C x = o[q];
+    const R re = mulc<R>(x.x, cs[q]) - (R)s * mulc<R>(x.y, sn[q]);
+    const R im = (R)s * mulc<R>(x.x, sn[q]) + mulc<R>(x.y, cs[q]);
+    o[q] = C{re, im};
   }
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
@@ -166,8 +209,6 @@ __device__ __forceinline__ void stockham_stage(const C* __restrict__ src, C* __r
   __syncthreads();
 }
 
-// Unitary DFT of every lane of the tile (radix RMAX stages, then one smaller
-// stage); the result ends in `alt`, and the two buffer pointers are swapped.
 // 1 / sqrt(2^lg) in the state precision: a power of two, times 1/sqrt(2) for odd lg
 // (no FP64 division or square root per thread: both are long sequences on this GPU)
 template <typename R>
@@ -177,11 +218,79 @@ __device__ __forceinline__ R inv_sqrt_pow2(int lg) {
   return (lg & 1) ? s * (R)0.70710678118654752440 : s;
 }
 
+// The same stage in place: every thread first reads and transforms all of its
+// butterflies (at most RMAX values: the host guarantees threads * RMAX >= points),
+// the block synchronises, then every thread writes its outputs back into `buf`.
+template <int RS, int RMAX, typename C, typename R>
+__device__ __forceinline__ void stockham_stage_inplace(C* __restrict__ buf, int L, int n, int ls, int p, int dir,
+                                                       const C* __restrict__ tw, bool last, R sc) {
+  constexpr int NBF = RMAX / RS;  // butterflies per thread
+  const int nb = n / RS;
+  const int total = L * nb;
+  const int estride = n / (RS * p);
+  C reg[NBF][RS];
+#pragma unroll
+  for (int u = 0; u < NBF; ++u) {
+    // threads past the end transform a valid butterfly and discard it
+    const int b = min((int)threadIdx.x + u * (int)blockDim.x, total - 1);
+    const int l = b / nb, i = b - l * nb;
+    const int k = i & (p - 1);
+#pragma unroll
+    for (int r = 0; r < RS; ++r) {
+      C x = buf[sidx(l, i + r * nb, ls)];
+      C w = tw[r * k * estride];
+      if (dir > 0) w.y = -w.y;
+      reg[u][r] = cmul(x, w);
+    }
+    dft_r<RS>(reg[u], dir);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < NBF; ++u) {
+    const int b = threadIdx.x + u * blockDim.x;
+    if (b < total) {
+      const int l = b / nb, i = b - l * nb;
+      const int k = i & (p - 1);
+      const int base = (i - k) * RS + k;
+#pragma unroll
+      for (int q = 0; q < RS; ++q) {
+        C v = reg[u][q];
+        if (last) v = C{v.x * sc, v.y * sc};
+        buf[sidx(l, base + q * p, ls)] = v;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Unitary DFT of every lane of the tile (radix RMAX stages, then one smaller
+// stage).  With a second buffer the stages ping-pong and the two pointers are
+// swapped at each stage; without one (alt == nullptr) they run in place.
 template <int RMAX, typename C>
 __device__ void fft_stockham(C*& buf, C*& alt, const Geometry& g, int dir, const C* __restrict__ tw) {
   using R = decltype(buf[0].x);
   const int n = (int)g.n, L = g.lanes_per_tile, ls = g.lane_stride;
   const R scale = inv_sqrt_pow2<R>(__ffs(n) - 1);
+  if (alt == nullptr) {
+    int p = 1;
+    while (p < n) {
+      const int rem = n / p;
+      if (rem >= RMAX) {
+        stockham_stage_inplace<RMAX, RMAX>(buf, L, n, ls, p, dir, tw, rem == RMAX, scale);
+        p *= RMAX;
+      } else if (rem == 8) {
+        stockham_stage_inplace<8, RMAX>(buf, L, n, ls, p, dir, tw, true, scale);
+        p *= 8;
+      } else if (rem == 4) {
+        stockham_stage_inplace<4, RMAX>(buf, L, n, ls, p, dir, tw, true, scale);
+        p *= 4;
+      } else {
+        stockham_stage_inplace<2, RMAX>(buf, L, n, ls, p, dir, tw, true, scale);
+        p *= 2;
+      }
+    }
+    return;
+  }
   int p = 1;
   while (p < n) {
     const int rem = n / p;
@@ -318,18 +427,24 @@ __device__ void run_scalar(const PassParams& p, const DevOp& op, const double* t
   }
 }
 
+// global loads a thread keeps in flight in the load and table phases of a pass
+// (64 bytes: 8 FP32 or 4 FP64 complex values)
+template <typename C>
+__host__ __device__ constexpr int load_batch() { return 64 / (int)sizeof(C); }
+
 template <typename R, int RMAX>
 __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t tile) {
   using C = typename Cx<R>::T;
   constexpr bool kF64 = sizeof(R) == 8;
+  constexpr int kLoadBatch = load_batch<C>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Geometry& g = p.g;
   const int L = g.lanes_per_tile, n = (int)g.n, ls = g.lane_stride;
   const int T = blockDim.x, tid = threadIdx.x;
   const size_t tile_bytes = ((size_t)L * ls * sizeof(C) + 15) & ~(size_t)15;
   C* buf = reinterpret_cast<C*>(smem_raw);
-  C* alt = reinterpret_cast<C*>(smem_raw + tile_bytes);
-  size_t off = 2 * tile_bytes;
+  C* alt = p.one_buffer ? nullptr : reinterpret_cast<C*>(smem_raw + tile_bytes);
+  size_t off = (p.one_buffer ? 1 : 2) * tile_bytes;
   int64_t* lane_base = reinterpret_cast<int64_t*>(smem_raw + off);
   off += (size_t)L * sizeof(int64_t);
   double* lane_w = reinterpret_cast<double*>(smem_raw + off);
@@ -388,11 +503,29 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
 
   C* psi = reinterpret_cast<C*>(p.psi);
   const int total = L * n;
-  for (int pt = tid; pt < total; pt += T) {
-    int l, x;
-    split(pt, l, x);
-    const int64_t b = lane_base[l];
-    buf[sidx(l, x, ls)] = b >= 0 ? psi[b + (int64_t)x * g.inner] : C{(R)0, (R)0};
+  // kLoadBatch independent global loads in flight per thread, then the shared stores
+  for (int p0 = tid; p0 < total; p0 += kLoadBatch * T) {
+    C v[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int pt = p0 + u * T;
+      v[u] = C{(R)0, (R)0};
+      if (pt < total) {
+        int l, x;
+        split(pt, l, x);
+        const int64_t b = lane_base[l];
+        if (b >= 0) v[u] = psi[b + (int64_t)x * g.inner];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int pt = p0 + u * T;
+      if (pt < total) {
+        int l, x;
+        split(pt, l, x);
+        buf[sidx(l, x, ls)] = v[u];
+      }
+    }
   }
   // twiddles in shared memory: the butterflies read them at scattered indices
   const C* tw = reinterpret_cast<const C*>(p.twiddle);
@@ -419,13 +552,28 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
         }
         case OP_DIAGND: {
           const C* t = reinterpret_cast<const C*>(op.ptr);
-          for (int pt = tid; pt < total; pt += T) {
-            int l, x;
-            split(pt, l, x);
-            const int64_t b = lane_base[l];
-            if (b >= 0) {
-              const int si = sidx(l, x, ls);
-              buf[si] = cmul(buf[si], t[b + (int64_t)x * g.inner]);
+          for (int p0 = tid; p0 < total; p0 += kLoadBatch * T) {
+            C tv[kLoadBatch];
+#pragma unroll
+            for (int u = 0; u < kLoadBatch; ++u) {
+              const int pt = p0 + u * T;
+              tv[u] = C{(R)1, (R)0};
+              if (pt < total) {
+                int l, x;
+                split(pt, l, x);
+                const int64_t b = lane_base[l];
+                if (b >= 0) tv[u] = t[b + (int64_t)x * g.inner];
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < kLoadBatch; ++u) {
+              const int pt = p0 + u * T;
+              if (pt < total) {
+                int l, x;
+                split(pt, l, x);
+                const int si = sidx(l, x, ls);
+                buf[si] = cmul(buf[si], tv[u]);
+              }
             }
           }
           __syncthreads();
@@ -612,7 +760,13 @@ __global__ void __launch_bounds__(512) pass_kernel_batched(const PassParams* __r
     else
       hi = mid - 1;
   }
-  pass_tile<R, RMAX>(params[lo], b - offsets[lo]);
+  // the pass description is read throughout the tile: keep a shared-memory copy
+  __shared__ __align__(16) PassParams sp;
+  static_assert(sizeof(PassParams) % 4 == 0, "PassParams is copied as 32-bit words");
+  for (int k = threadIdx.x; k < (int)(sizeof(PassParams) / 4); k += blockDim.x)
+    reinterpret_cast<uint32_t*>(&sp)[k] = reinterpret_cast<const uint32_t*>(params + lo)[k];
+  __syncthreads();
+  pass_tile<R, RMAX>(sp, b - offsets[lo]);
 }
 
 template <typename R, int RMAX>
@@ -637,13 +791,30 @@ cudaError_t launch_pass_batched(bool fp64, const PassParams* params_dev, const i
               : launch_batched_impl<float, 16>(params_dev, offsets_dev, count, blocks, threads, smem, s);
 }
 
-size_t pass_smem_bytes(const Geometry& g, bool fp64, bool fft) {
+size_t pass_smem_bytes(const PassParams& p, bool fp64) {
+  const Geometry& g = p.g;
+  const bool fft = p.twiddle != nullptr;
   const size_t cs = fp64 ? 16 : 8;
-  size_t b = 2 * (((size_t)g.lanes_per_tile * g.lane_stride * cs + 15) & ~(size_t)15);
+  size_t b = (p.one_buffer ? 1 : 2) * (((size_t)g.lanes_per_tile * g.lane_stride * cs + 15) & ~(size_t)15);
   b += (size_t)g.lanes_per_tile * (sizeof(int64_t) + sizeof(double) + kMaxDims * sizeof(int) + sizeof(int));
   b = (b + 15) & ~(size_t)15;
   if (fft) b += (size_t)g.n * cs;
   return b;
+}
+
+void pass_choose_buffers(PassParams& p, bool fp64) {
+  const Geometry& g = p.g;
+  const int64_t pts = (int64_t)g.lanes_per_tile * g.n;
+  const int rmax = fp64 ? 8 : 16;
+  // only the largest tiles, where the second buffer halves the CTAs an SM holds, and only
+  // when every thread holds exactly rmax values per stage (no idle or repeated butterflies)
+  bool one = pts >= (fp64 ? 4096 : 8192) && (int64_t)pass_threads(g) * rmax == pts;
+  for (int i = 0; i < p.nops; ++i) {
+    const int k = p.ops[i].kind;
+    if (k == OP_MAT || k == OP_MAT_LANE || k == OP_MAT_SLICE) one = false;
+    if (k == OP_FFT && !((g.n & (g.n - 1)) == 0 && g.n >= 16)) one = false;  // direct DFT
+  }
+  p.one_buffer = one ? 1 : 0;
 }
 
 int pass_threads(const Geometry& g) {
@@ -657,7 +828,7 @@ int pass_threads(const Geometry& g) {
 
 template <typename R, int RMAX>
 static cudaError_t launch_impl(const PassParams& p, cudaStream_t s) {
-  const size_t smem = pass_smem_bytes(p.g, sizeof(R) == 8, p.twiddle != nullptr);
+  const size_t smem = pass_smem_bytes(p, sizeof(R) == 8);
   auto kern = pass_kernel<R, RMAX>;
   static bool configured = false;
   if (!configured) {

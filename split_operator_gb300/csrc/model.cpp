@@ -9,6 +9,9 @@
 
 #include "model.hpp"
 
+#include <cstdio>
+#include <cstdlib>
+
 namespace so {
 
 void cuda_check(cudaError_t e, const char* what) {
@@ -330,7 +333,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
       mats[nmat++] = (int)i;
     }
   }
-  if (nmat == 0) return false;
+  if (nmat == 0 || !angular_tc_ops_fit(ops.data(), (int)ops.size(), g.sweep_axis)) return false;
   const int bn = angular_tc_columns((int)g.n);
   g.lanes_per_tile = bn;
   g.tiles_per_outer = (int32_t)(g.inner / bn);
@@ -354,7 +357,28 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     timed_begin(name);
     timed_.back().bytes = pass_bytes(ops, g);
   }
-  cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, stream), "tensor-core pass launch");
+  // SO_TC_TRACE=<file>: per-tile phase timestamps of every tensor-core pass, appended as text
+  static const char* trace_path = std::getenv("SO_TC_TRACE");
+  DeviceBuffer trace;
+  if (trace_path) {
+    trace = DeviceBuffer((size_t)g.tiles * angular_tc_trace_slots() * sizeof(unsigned long long));
+    cuda_check(cudaMemsetAsync(trace.ptr, 0, trace.bytes, stream), "trace clear");
+  }
+  cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, stream,
+                               trace_path ? trace.as<unsigned long long>() : nullptr),
+             "tensor-core pass launch");
+  if (trace_path) {
+    std::vector<unsigned long long> h(trace.bytes / sizeof(unsigned long long));
+    cuda_check(cudaMemcpyAsync(h.data(), trace.ptr, trace.bytes, cudaMemcpyDeviceToHost, stream), "trace copy");
+    cuda_check(cudaStreamSynchronize(stream), "trace sync");
+    if (FILE* f = std::fopen(trace_path, "a")) {
+      std::fprintf(f, "pass %s n=%lld tiles=%lld slots=%d\n", name.c_str(), (long long)g.n, (long long)g.tiles,
+                   angular_tc_trace_slots());
+      for (size_t i = 0; i < h.size(); ++i)
+        std::fprintf(f, "%llu%c", h[i], (i + 1) % angular_tc_trace_slots() == 0 ? '\n' : ' ');
+      std::fclose(f);
+    }
+  }
   if (timing) timed_end();
   return true;
 }
@@ -447,6 +471,7 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   }
   p.nred = nred;
   if (fft) p.twiddle = twiddle((size_t)p.g.n);
+  pass_choose_buffers(p, fp64);
   if (!fp64 && tc_tf32 && !resident && try_launch_tc(ops, axis, p)) return;
   if (!resident && (size_t)p.g.tiles > partials_cap_) {
     partials_cap_ = (size_t)p.g.tiles;
@@ -458,7 +483,7 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
     RecordedPass r{resident ? RecordedPass::Resident : RecordedPass::Generic, fp64, p, {},
-                   pass_threads(p.g), pass_smem_bytes(p.g, fp64, p.twiddle != nullptr), name, pass_bytes(ops, p.g)};
+                   pass_threads(p.g), pass_smem_bytes(p, fp64), name, pass_bytes(ops, p.g)};
     recording->push_back(std::move(r));
     return;
   }

@@ -67,11 +67,11 @@ def test_long_run_fp64_vs_cpu_restatement_and_fp32_modes(tmp_path):
         row = {"steps": cp,
                "fp64_vs_cpu_rel_l2": rel_l2(a64, port.psi),
                "fp64_norm": p64.norm(), "cpu_norm": _norm(port.psi, port.wr, port.wth),
-               "fp64_loss": p64.get_losses()[0], "cpu_loss": float(port.loss[0])}
+               "fp64_loss": p64.all_losses()[0], "cpu_loss": float(port.loss[0])}
         for m, p in p32.items():
             a = p.get_array()
             row[m] = {"rel_l2_vs_fp64": rel_l2(a, a64), "norm_drift": p.norm() - row["fp64_norm"],
-                      "loss_diff": p.get_losses()[0] - row["fp64_loss"]}
+                      "loss_diff": p.all_losses()[0] - row["fp64_loss"]}
         rows.append(row)
     report["rows"] = rows
     report["cpu_seconds"] = t_port
