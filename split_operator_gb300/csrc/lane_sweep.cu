@@ -96,11 +96,19 @@ __device__ __forceinline__ RotConst<R> rot_const(int which) {
     return {v[which], 0.0};
   }
 }
+// fused multiply-add in the state precision
+template <typename R>
+__device__ __forceinline__ R fmar(R a, R b, R c) {
+  if constexpr (sizeof(R) == 4)
+    return fmaf(a, b, c);
+  else
+    return fma(a, b, c);
+}
 // x * c with the constant carried as hi + lo
 template <typename R>
 __device__ __forceinline__ R mulc(R x, RotConst<R> c) {
   if constexpr (sizeof(R) == 4)
-    return fmaf(x, c.lo, x * c.hi);
+    return fmaf(x, c.hi, x * c.lo);
   else
     return x * c.hi;
 }
@@ -151,8 +159,10 @@ __device__ __forceinline__ void dft16(C* a, int s) {
       continue;
     }
     const C x = o[q];
-    const R re = mulc<R>(x.x, cs[q]) - (R)s * mulc<R>(x.y, sn[q]);
-    const R im = (R)s * mulc<R>(x.x, sn[q]) + mulc<R>(x.y, cs[q]);
+    const R ys = (R)s * x.y, xs = (R)s * x.x;
+    // (c x - s' y, s' x + c y) with the lo parts of c and s' folded in first
+    const R re = fmar(x.x, cs[q].hi, fmar(-ys, sn[q].hi, x.x * cs[q].lo - ys * sn[q].lo));
+    const R im = fmar(xs, sn[q].hi, fmar(x.y, cs[q].hi, xs * sn[q].lo + x.y * cs[q].lo));
     o[q] = C{re, im};
   }
 #pragma unroll
@@ -218,79 +228,13 @@ __device__ __forceinline__ R inv_sqrt_pow2(int lg) {
   return (lg & 1) ? s * (R)0.70710678118654752440 : s;
 }
 
-// The same stage in place: every thread first reads and transforms all of its
-// butterflies (at most RMAX values: the host guarantees threads * RMAX >= points),
-// the block synchronises, then every thread writes its outputs back into `buf`.
-template <int RS, int RMAX, typename C, typename R>
-__device__ __forceinline__ void stockham_stage_inplace(C* __restrict__ buf, int L, int n, int ls, int p, int dir,
-                                                       const C* __restrict__ tw, bool last, R sc) {
-  constexpr int NBF = RMAX / RS;  // butterflies per thread
-  const int nb = n / RS;
-  const int total = L * nb;
-  const int estride = n / (RS * p);
-  C reg[NBF][RS];
-#pragma unroll
-  for (int u = 0; u < NBF; ++u) {
-    // threads past the end transform a valid butterfly and discard it
-    const int b = min((int)threadIdx.x + u * (int)blockDim.x, total - 1);
-    const int l = b / nb, i = b - l * nb;
-    const int k = i & (p - 1);
-#pragma unroll
-    for (int r = 0; r < RS; ++r) {
-      C x = buf[sidx(l, i + r * nb, ls)];
-      C w = tw[r * k * estride];
-      if (dir > 0) w.y = -w.y;
-      reg[u][r] = cmul(x, w);
-    }
-    dft_r<RS>(reg[u], dir);
-  }
-  __syncthreads();
-#pragma unroll
-  for (int u = 0; u < NBF; ++u) {
-    const int b = threadIdx.x + u * blockDim.x;
-    if (b < total) {
-      const int l = b / nb, i = b - l * nb;
-      const int k = i & (p - 1);
-      const int base = (i - k) * RS + k;
-#pragma unroll
-      for (int q = 0; q < RS; ++q) {
-        C v = reg[u][q];
-        if (last) v = C{v.x * sc, v.y * sc};
-        buf[sidx(l, base + q * p, ls)] = v;
-      }
-    }
-  }
-  __syncthreads();
-}
-
 // Unitary DFT of every lane of the tile (radix RMAX stages, then one smaller
-// stage).  With a second buffer the stages ping-pong and the two pointers are
-// swapped at each stage; without one (alt == nullptr) they run in place.
+// stage); the result ends in `alt`, and the two buffer pointers are swapped.
 template <int RMAX, typename C>
 __device__ void fft_stockham(C*& buf, C*& alt, const Geometry& g, int dir, const C* __restrict__ tw) {
   using R = decltype(buf[0].x);
   const int n = (int)g.n, L = g.lanes_per_tile, ls = g.lane_stride;
   const R scale = inv_sqrt_pow2<R>(__ffs(n) - 1);
-  if (alt == nullptr) {
-    int p = 1;
-    while (p < n) {
-      const int rem = n / p;
-      if (rem >= RMAX) {
-        stockham_stage_inplace<RMAX, RMAX>(buf, L, n, ls, p, dir, tw, rem == RMAX, scale);
-        p *= RMAX;
-      } else if (rem == 8) {
-        stockham_stage_inplace<8, RMAX>(buf, L, n, ls, p, dir, tw, true, scale);
-        p *= 8;
-      } else if (rem == 4) {
-        stockham_stage_inplace<4, RMAX>(buf, L, n, ls, p, dir, tw, true, scale);
-        p *= 4;
-      } else {
-        stockham_stage_inplace<2, RMAX>(buf, L, n, ls, p, dir, tw, true, scale);
-        p *= 2;
-      }
-    }
-    return;
-  }
   int p = 1;
   while (p < n) {
     const int rem = n / p;
@@ -742,14 +686,14 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
 }
 
 template <typename R, int RMAX>
-__global__ void __launch_bounds__(512) pass_kernel(const __grid_constant__ PassParams p) {
+__global__ void __launch_bounds__(512, 2) pass_kernel(const __grid_constant__ PassParams p) {
   pass_tile<R, RMAX>(p, blockIdx.x);
 }
 
 // Many propagations' passes in one launch: block b runs tile (b - offsets[i]) of
 // params[i], offsets[i] <= b < offsets[i + 1].
 template <typename R, int RMAX>
-__global__ void __launch_bounds__(512) pass_kernel_batched(const PassParams* __restrict__ params,
+__global__ void __launch_bounds__(512, 2) pass_kernel_batched(const PassParams* __restrict__ params,
                                                            const int64_t* __restrict__ offsets, int count) {
   const int64_t b = blockIdx.x;
   int lo = 0, hi = count - 1;
@@ -803,18 +747,8 @@ size_t pass_smem_bytes(const PassParams& p, bool fp64) {
 }
 
 void pass_choose_buffers(PassParams& p, bool fp64) {
-  const Geometry& g = p.g;
-  const int64_t pts = (int64_t)g.lanes_per_tile * g.n;
-  const int rmax = fp64 ? 8 : 16;
-  // only the largest tiles, where the second buffer halves the CTAs an SM holds, and only
-  // when every thread holds exactly rmax values per stage (no idle or repeated butterflies)
-  bool one = pts >= (fp64 ? 4096 : 8192) && (int64_t)pass_threads(g) * rmax == pts;
-  for (int i = 0; i < p.nops; ++i) {
-    const int k = p.ops[i].kind;
-    if (k == OP_MAT || k == OP_MAT_LANE || k == OP_MAT_SLICE) one = false;
-    if (k == OP_FFT && !((g.n & (g.n - 1)) == 0 && g.n >= 16)) one = false;  // direct DFT
-  }
-  p.one_buffer = one ? 1 : 0;
+  (void)fp64;
+  p.one_buffer = 0;  // every pass keeps the ping-pong pair of tile buffers
 }
 
 int pass_threads(const Geometry& g) {
