@@ -8,27 +8,29 @@
 // border_dumping.rs:57-93, wave_function.rs:68-85).
 //
 // Layout: the state is stored [outer][n][inner] (n = lane axis, e.g. theta; inner =
-// radial points).  A CTA owns a tile of BN complex columns of the inner axis for all
-// n rows.  Treating (re, im) as two real columns, a lane-matrix product is the real
-// GEMM D[M x 2BN] = A[M x n] . B[n x 2BN], A the (zero-padded) matrix, B the tile:
-//   n <= 128: M = 128, BN = 64 (N = 128), A chunks of K = 32
-//   n = 256 : M = 256 as two 128-row halves, BN = 32 (N = 64), A chunks of K = 16
+// radial points).  A tile is BN complex columns of the inner axis for all n rows.
+// Treating (re, im) as two real columns, a lane-matrix product is the real GEMM
+// D[M x 2BN] = A[M x n] . B[n x 2BN], A the (zero-padded) matrix, B the tile:
+//   n <= 128: M = 128, BN = 64 (N = 128), A chunks of K = 16
+//   n = 256 : M = 256 as two 128-row halves, BN = 32 (N = 64), A chunks of K = 8
+// (wide N: every tcgen05.mma instruction has a fixed issue cost, so few wide ones)
 // 3xTF32: A = A_hi + A_lo (split once from the FP64 matrix on the host), B = B_hi +
 // B_lo (split on the fly), both parts tf32-exact, D = A_hi B_hi + A_hi B_lo + A_lo B_hi.
-// The tensor core's FP32 accumulation truncates; to keep that bias small each K chunk
-// group accumulates in its own TMEM region (up to 4) and the epilogue adds them with
-// round-to-nearest FP32 adds.
 //
-//   prologue  (thread = column): load tile, pre-ops, split -> B_hi/B_lo (smem)
-//   GEMM 1    (one thread issues tcgen05.mma; A chunks stream in by bulk TMA)
-//   epilogue 1 (thread = row, tcgen05.ld from TMEM): mid-ops, split -> B for GEMM 2
-//   GEMM 2
-//   epilogue 2: post-ops -> staging -> coalesced store
-//   FP64 norm partials folded by the last CTA in a fixed order (as lane_sweep.cu).
-// Point-wise ops run on batches of 8-16 values per thread so each thread keeps that
-// many table / state loads in flight.
+// Persistent CTAs, one per SM, each walking its share of the tiles of the launch:
+//   warps 0-7  load the tile, run the point-wise ops, split it into the B operand,
+//              drain the accumulators, run the ops between / after the matrices,
+//              store, and fold the norms (named barrier 1 among themselves)
+//   warp 8     streams the A chunks of every tile, in order, through kStages
+//              shared-memory stages by bulk TMA (it runs ahead across tiles)
+//   warp 9     issues tcgen05.mma (one lane) as chunks land and the B operand is ready
+// The tensor core truncates its FP32 accumulation, so the A_hi B_hi products go to
+// three 128-column TMEM regions a couple of K steps each and the work warps drain the
+// regions into registers (round-to-nearest adds) every kFillSteps K steps; the
+// corrections, 2^-11 smaller, share a fourth region.  FP32 norm partials are folded per tile in
+// float-float and across tiles in FP64 by the last tile of the pass, in a fixed order.
 // Every mbarrier wait is bounded (2 s); on a timeout the CTA records an error in a
-// slot, waits (bounded) for its own copies, frees its tensor memory and returns.
+// slot, lets its copies and MMAs finish (bounded), frees its tensor memory and returns.
 #include "common.cuh"
 #include "tc_common.cuh"
 
@@ -37,13 +39,15 @@ namespace so {
 namespace {
 
 constexpr int kChunkBytes = 8192;   // one of hi / lo: 128 rows x 16 K or 256 rows x 8 K
+constexpr int kStages = 4;          // A chunk stages (16 KB each) in flight per CTA
 constexpr int kLboB = 144;          // B: core matrices along K (16 B padding vs 128)
 constexpr uint64_t kWaitLimit = 2000000000ull;  // 2 s per wait
-constexpr int kWorkThreads = 256;            // warps 0-7: loads, point-wise ops, TMEM drains, stores
-constexpr int kThreads = kWorkThreads + 32;  // warp 8: A-chunk TMA producer and MMA issuer (one lane)
-constexpr uint32_t kTmemCols = 256;  // half of the SM's tensor memory: two CTAs share an SM
-constexpr int kRegions = 4;          // 64-column accumulator regions in kTmemCols
+constexpr int kWorkThreads = 256;               // warps 0-7
+constexpr int kThreads = kWorkThreads + 64;     // + warp 8 (TMA) + warp 9 (MMA)
+constexpr uint32_t kTmemCols = 512;  // all of the SM's tensor memory: one CTA per SM
+constexpr int kRegions = 4;          // 128-column accumulator regions in kTmemCols
 constexpr int kFillSteps = 6;        // K steps between two drains of the main regions
+constexpr int kVals = 64;            // FP32 accumulator columns a work thread drains
 constexpr int kColtSlots = 4;        // DIAG1D ops on a non-lane axis per pass
 
 struct TcShape {
@@ -57,6 +61,7 @@ struct TcShape {
   int nmain;     // regions for the A_hi B_hi products; one more region holds the corrections
   int fills;     // drains of the main regions per matrix
   int sbo_a;     // A: row-group stride (bytes)
+  int a_half16;  // A descriptor step to the second 128-row half ((16 row groups x sbo_a) >> 4)
   int stage_row; // output staging row stride (floats)
   int groups;    // work threads per column: 256 / bn
 };
@@ -71,7 +76,7 @@ struct TcShape {
 __host__ __device__ inline TcShape tc_shape(int n) {
   TcShape s{};
   s.mh = n == 256 ? 2 : 1;
-  s.bn = n == 256 ? 16 : 32;
+  s.bn = n == 256 ? 32 : 64;
   s.nc = 2 * s.bn;
   s.chunk_k = 16 / s.mh;
   s.nk = n / s.chunk_k;
@@ -80,28 +85,29 @@ __host__ __device__ inline TcShape tc_shape(int n) {
   s.nmain = kRegions - 1;
   s.fills = (s.ksteps + kFillSteps - 1) / kFillSteps;
   s.sbo_a = (s.chunk_k / 4) * 128;
+  s.a_half16 = (16 * s.sbo_a) >> 4;
   s.stage_row = s.nc + 4;
   s.groups = kWorkThreads / s.bn;
   return s;
 }
 
 struct TcSmemLayout {
-  uint32_t stage0, stage1, bhi, blo, bars, sbo_b, bbytes, total;
+  uint32_t stage0, bhi, blo, bars, sbo_b, bbytes, total;
 };
 
+// [kStages x 16 KB A stages][B_hi][B_lo][mbarriers: full[kStages], empty[kStages], dbar,
+// freebar, bready, quiet]
 __host__ __device__ inline TcSmemLayout tc_layout(int n) {
   const TcShape s = tc_shape(n);
   TcSmemLayout L{};
   L.sbo_b = (uint32_t)(n / 4) * kLboB + 16;
   L.bbytes = (uint32_t)(s.nc / 8) * L.sbo_b;
   L.bbytes = (L.bbytes + 127u) & ~127u;
-  const uint32_t stage_bytes = 2u * kChunkBytes;
   L.stage0 = 0;
-  L.stage1 = stage_bytes;
-  L.bhi = 2 * stage_bytes;
+  L.bhi = kStages * 2u * kChunkBytes;
   L.blo = L.bhi + L.bbytes;
   L.bars = L.blo + L.bbytes;
-  L.total = L.bars + 64;
+  L.total = L.bars + (2 * kStages + 4) * 8;
   return L;
 }
 
@@ -126,8 +132,24 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
   return {hi, e - (hi - s)};
 }
 
-// fixed-order sum of one float per thread over the whole block, in float-float;
-// valid in thread 0
+// barrier among the work warps only (the TMA and MMA warps run their own loops)
+__device__ __forceinline__ void work_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kWorkThreads) : "memory"); }
+
+// the same barrier, returning whether v holds in every work thread
+__device__ __forceinline__ bool work_all(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, 1, %2, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "n"(kWorkThreads)
+      : "memory");
+  return r != 0;
+}
+
+// fixed-order sum of one float per work thread, in float-float; valid in thread 0
 __device__ FF block_sum(float v, FF* scratch) {
   FF a{v, 0.0f};
 #pragma unroll
@@ -136,11 +158,11 @@ __device__ FF block_sum(float v, FF* scratch) {
     a = ff_add(a, b);
   }
   if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = a;
-  __syncthreads();
+  work_sync();
   FF r{0.0f, 0.0f};
   if (threadIdx.x == 0)
-    for (int w = 0; w < kThreads / 32; ++w) r = ff_add(r, scratch[w]);
-  __syncthreads();
+    for (int w = 0; w < kWorkThreads / 32; ++w) r = ff_add(r, scratch[w]);
+  work_sync();
   return r;
 }
 
@@ -161,11 +183,11 @@ __device__ __forceinline__ int64_t coord_of(const Geometry& g, int a, int64_t o,
   return 0;
 }
 
-// Per-tile factors of the point-wise ops, built once per tile so that the per-point
+// Per-tile factors of the point-wise ops, built once per tile (by the work warps) so that the per-point
 // work reads shared memory and does FP32 arithmetic only (FP64 runs on a narrow pipe).
 struct TileTabs {
-  float colw[kMaxRed][32];   // NORM: product of the FP32 weights of every non-lane axis, per tile column
-  float2 colt[kColtSlots][32];  // DIAG1D on a non-lane axis: the table value of each tile column
+  float colw[kMaxRed][64];      // NORM: product of the FP32 weights of every non-lane axis, per tile column
+  float2 colt[kColtSlots][64];  // DIAG1D on a non-lane axis: the table value of each tile column
   float scale[kMaxOps];         // SCALE: sqrt(target / norm)
   int8_t slot[kMaxOps];         // DIAG1D on a non-lane axis: its colt row
 };
@@ -181,8 +203,8 @@ __device__ __forceinline__ void build_tile_tabs(const PassParams& p, TileTabs& T
     for (int q = 0; q < (int)threadIdx.x; ++q) k += diag1d_across(p.ops[q], g.sweep_axis);
     T.slot[threadIdx.x] = (int8_t)k;
   }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < p.nops * bn; idx += blockDim.x) {
+  work_sync();
+  for (int idx = threadIdx.x; idx < p.nops * bn; idx += kWorkThreads) {
     const int oi = idx / bn, c = idx - oi * bn;
     const DevOp& op = p.ops[oi];
     const int64_t i = i0 + c;
@@ -372,389 +394,443 @@ struct TcParams {
   unsigned long long* trace;  // optional phase timestamps, kTraceSlots per tile (nullptr: off)
 };
 
-// Phase timestamps (%globaltimer, ns) of the optional trace, per tile.
+// Phase timestamps (%globaltimer, ns) of the optional trace, per tile (work thread 0).
 enum TraceSlot {
-  TR_START, TR_SETUP, TR_PROLOGUE, TR_DRAIN0, TR_MAT0, TR_EPI0, TR_MAT1, TR_EPI1, TR_JOIN, TR_STORE, TR_NORMS,
-  TR_TICKET, TR_END, TR_CHUNK0, TR_ISSUE0, TR_ISSUE1,
-  TR_TMA4, TR_FULL4, TR_MMA4, TR_DONE4,  // chunk 4: copy issued, landed, MMAs issued, MMAs completed
-  kTraceSlots
+  TR_START, TR_PROLOGUE, TR_MAT0, TR_EPI0, TR_MAT1, TR_EPI1, TR_STORE, TR_END,
+  TR_TMA = 8,     // + c: chunk c (< 8) of the tile: copy issued (TMA warp)
+  TR_FULL = 16,   // + c: chunk c landed (MMA warp)
+  TR_MMA = 24,    // + c: chunk c's MMAs issued and committed (MMA warp)
+  kTraceSlots = 32
 };
 __device__ __forceinline__ void trace_mark(const TcParams& tp, int64_t tile, int slot) {
   if (tp.trace) tp.trace[tile * kTraceSlots + slot] = tc::globaltimer_ns();
 }
 
-// The producer / MMA lane.  A chunks (hi 8 KB + lo 8 KB) stream through two stages by bulk
-// TMA; for each matrix (once its B operand is written) and each fill it issues the K
-// steps of the fill -- step t puts A_hi B_hi into main region (t - t0) nused / span and
-// both corrections into the correction region -- and commits the fill to dbar.  Once the
-// MMAs of chunk c complete, its stage is refilled with chunk c + 2.
-// Every wait is bounded; on a failure it waits (bounded) for the copies and MMAs already
-// issued and returns false.  Chunks 0 .. preissued-1 were issued at kernel entry.
-__device__ __noinline__ bool mma_producer(const TcShape S, const TcSmemLayout L, uint32_t sm0, const float* img0,
-                                          const float* img1, int nmat, uint32_t tmem, unsigned long long* tr,
-                                          int preissued) {
+// K steps [t0, t1) of fill f split into at most nmain regions
+struct FillSpan {
+  int t0, t1, nused;
+};
+__device__ __forceinline__ FillSpan fill_span(const TcShape& S, int f) {
+  FillSpan r;
+  r.t0 = f * S.ksteps / S.fills;
+  r.t1 = (f + 1) * S.ksteps / S.fills;
+  r.nused = (r.t1 - r.t0) < S.nmain ? (r.t1 - r.t0) : S.nmain;
+  return r;
+}
+
+// A tile of a launch: its pass description and its index within the pass.
+struct TileRef {
+  const TcParams* prm;
+  int64_t tile;
+};
+
+// Warp 8, lane 0: the A chunks of every tile of this CTA, in order, through the stages.
+template <typename Resolve>
+__device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const TcShape S, uint32_t sm0,
+                                          const TcSmemLayout L, volatile int* fail) {
   using namespace tc;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm_ptr(sm0 + L.bars));
-  uint64_t* full = bars;
-  uint64_t* empty = bars + 2;
-  uint64_t* dbar = bars + 4;
-  uint64_t* freebar = bars + 5;
-  uint64_t* bready = bars + 6;
-  uint64_t* quiet = bars + 7;
-  const int total_chunks = S.nk * nmat;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm_ptr(sm0 + L.bars));
+  uint64_t* empty = full + kStages;
   const uint32_t stage_bytes = 2u * kChunkBytes;
-  int issued = 0, landed = 0;
-  auto issue_chunk = [&](int c) {
-    const int m = c / S.nk, q = c - m * S.nk;
-    const int s = c & 1;
-    if (tr && c == 4) tr[TR_TMA4] = globaltimer_ns();
-    mbar_expect_tx(&full[s], stage_bytes);
-    bulk_g2s(sm_ptr(sm0 + L.stage0 + (uint32_t)s * stage_bytes), (m == 0 ? img0 : img1) + (size_t)q * 2 * (kChunkBytes / 4),
-             stage_bytes, &full[s]);
-    issued = c + 1;
-  };
+  int64_t cc = 0;  // chunks issued
+  bool ok = true;
+  for (int64_t gt = blockIdx.x; gt < total && ok && !*fail; gt += gridDim.x) {
+    const TileRef r = resolve(gt);
+    const int nmat = r.prm->nmat;
+    for (int m = 0; m < nmat && ok; ++m) {
+      const float* img = r.prm->images[m];
+      for (int q = 0; q < S.nk; ++q) {
+        const int s = (int)(cc % kStages);
+        const uint32_t use = (uint32_t)(cc / kStages);
+        if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1u, kWaitLimit)) {
+          ok = false;
+          break;
+        }
+        const int ct = m * S.nk + q;  // chunk within the tile
+        if (r.prm->trace && ct < 8) r.prm->trace[r.tile * kTraceSlots + TR_TMA + ct] = globaltimer_ns();
+        mbar_expect_tx(&full[s], stage_bytes);
+        bulk_g2s(sm_ptr(sm0 + L.stage0 + (uint32_t)s * stage_bytes), img + (size_t)q * 2 * (kChunkBytes / 4),
+                 stage_bytes, &full[s]);
+        ++cc;
+      }
+    }
+  }
+  if (!ok) {
+    *fail = 1;
+    // let the copies in flight land before the CTA lets go of its shared memory
+    for (int64_t c = cc - kStages < 0 ? 0 : cc - kStages; c < cc; ++c)
+      mbar_wait(&full[c % kStages], (uint32_t)((c / kStages) & 1), kWaitLimit);
+  }
+}
+
+// Warp 9, lane 0: for each tile and matrix (once its B operand is written) and each
+// fill, the K steps of the fill -- step t puts A_hi B_hi into main region
+// (t - t0) nused / span and both corrections into the correction region -- then a
+// commit of the fill to dbar.  Each chunk's MMAs are committed to its stage's empty
+// barrier, which the TMA warp waits on before refilling the stage.
+template <typename Resolve>
+__device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const TcShape S, uint32_t sm0,
+                                        const TcSmemLayout L, uint32_t tmem, volatile int* fail) {
+  using namespace tc;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm_ptr(sm0 + L.bars));
+  uint64_t* empty = full + kStages;
+  uint64_t* dbar = full + 2 * kStages;
+  uint64_t* freebar = dbar + 1;
+  uint64_t* bready = dbar + 2;
+  uint64_t* quiet = dbar + 3;
+  const uint32_t stage_bytes = 2u * kChunkBytes;
   const uint32_t idesc = idesc_tf32(128, (uint32_t)S.nc);
   const uint64_t bbits = smem_desc_bits(kLboB, L.sbo_b), abits = smem_desc_bits(128, (uint32_t)S.sbo_a);
   const int kpc = S.chunk_k / 8;  // K steps per chunk
+  int64_t cc = 0;                 // chunks consumed
+  int s = 0;                      // stage of the chunk being consumed
+  uint64_t ahi = 0;               // A_hi descriptor of the current K step (a chunk may span two fills)
+  uint32_t nready = 0, nfree = 0;
   bool ok = true;
-  issued = preissued;  // chunks 0 and 1 went out at kernel entry
-  int nfree = 0;
-  for (int m = 0; m < nmat && ok; ++m) {
-    ok = mbar_wait(bready, (uint32_t)(m & 1), kWaitLimit);
-    tc_fence_after();
-    for (int f = 0; f < S.fills && ok; ++f) {
-      if (f > 0) {
-        ok = mbar_wait(freebar, (uint32_t)(nfree & 1), kWaitLimit);
-        ++nfree;
-        tc_fence_after();
-        if (!ok) break;
-      }
-      const int t0 = f * S.ksteps / S.fills, t1 = (f + 1) * S.ksteps / S.fills;
-      const int span = t1 - t0, nused = span < S.nmain ? span : S.nmain;
-      for (int t = t0; t < t1 && ok; ++t) {
-        const int q = t / kpc, ks = t - q * kpc;
-        const int c = m * S.nk + q, s = c & 1;
-        if (ks == 0) {
-          ok = mbar_wait(&full[s], (uint32_t)((c >> 1) & 1), kWaitLimit);
-          if (!ok) break;
-          if (tr && c == 0) tr[TR_CHUNK0] = globaltimer_ns();
-          if (tr && c == 4) tr[TR_FULL4] = globaltimer_ns();
-          landed = c + 1;
+  for (int64_t gt = blockIdx.x; gt < total && ok; gt += gridDim.x) {
+    const TileRef tr = resolve(gt);
+    const int nmat = tr.prm->nmat;
+    unsigned long long* trace = tr.prm->trace ? tr.prm->trace + tr.tile * kTraceSlots : nullptr;
+    const int64_t cc_tile = cc;  // first chunk of this tile
+    for (int m = 0; m < nmat && ok; ++m) {
+      ok = mbar_wait(bready, nready & 1u, kWaitLimit);
+      ++nready;
+      tc_fence_after();
+      for (int f = 0; f < S.fills && ok; ++f) {
+        if (f > 0) {
+          ok = mbar_wait(freebar, nfree & 1u, kWaitLimit);
+          ++nfree;
           tc_fence_after();
+          if (!ok) break;
         }
-        const int rm = (t - t0) * nused / span;
-        const bool first_main = t == t0 || rm != (t - 1 - t0) * nused / span;
-        const uint32_t kb = (uint32_t)(((q * S.chunk_k + ks * 8) >> 2) * kLboB);
-        const uint64_t bh = smem_desc_at(bbits, sm0 + L.bhi + kb), bl = smem_desc_at(bbits, sm0 + L.blo + kb);
-        const uint32_t st = sm0 + L.stage0 + (uint32_t)s * stage_bytes + (uint32_t)(ks * 256);
-        for (int hh = 0; hh < S.mh; ++hh) {
-          const uint32_t dm = tmem + (uint32_t)(rm * S.reg_cols + hh * S.nc);
-          const uint32_t dc = tmem + (uint32_t)(S.nmain * S.reg_cols + hh * S.nc);
-          const uint32_t aoff = st + (uint32_t)(hh * 16 * S.sbo_a);
-          mma_tf32(dm, smem_desc_at(abits, aoff), bh, idesc, first_main ? 0u : 1u);
-          mma_tf32(dc, smem_desc_at(abits, aoff), bl, idesc, t == 0 ? 0u : 1u);
-          mma_tf32(dc, smem_desc_at(abits, aoff + kChunkBytes), bh, idesc, 1u);
-        }
-        if (ks == kpc - 1) {
-          // refill this stage with chunk c + 2 as soon as the MMAs reading it complete, so
-          // that both stages always have a copy in flight
-          mma_commit(&empty[s]);
-          if (tr && c == 4) tr[TR_MMA4] = globaltimer_ns();
-          if (c + 2 < total_chunks) {
-            ok = mbar_wait(&empty[s], (uint32_t)((c >> 1) & 1), kWaitLimit);
-            if (tr && c == 4) tr[TR_DONE4] = globaltimer_ns();
-            if (ok) issue_chunk(c + 2);
+        const FillSpan fs = fill_span(S, f);
+        const int span = fs.t1 - fs.t0;
+        // descriptors and TMEM addresses advance by constant steps (no division per step):
+        // B by 2 K core matrices (2 x kLboB bytes) per K step, A by 256 bytes per K step
+        // within a chunk; the main region index moves when (t - t0) nused crosses span
+        uint64_t bh = smem_desc_at(bbits, sm0 + L.bhi + (uint32_t)(fs.t0 * 2 * kLboB));
+        uint64_t bl = smem_desc_at(bbits, sm0 + L.blo + (uint32_t)(fs.t0 * 2 * kLboB));
+        int rm = 0, racc = 0;
+        bool newreg = true;  // this step starts region rm
+        uint32_t dm0 = tmem;
+        const uint32_t dc0 = tmem + (uint32_t)(S.nmain * S.reg_cols);
+        for (int t = fs.t0; t < fs.t1; ++t) {
+          const int ks = t & (kpc - 1);  // kpc is 1 or 2
+          if (ks == 0) {
+            s = (int)(cc % kStages);
+            ok = mbar_wait(&full[s], (uint32_t)((cc / kStages) & 1), kWaitLimit);
+            if (!ok) break;
+            if (trace && (int)(cc - cc_tile) < 8) trace[TR_FULL + (int)(cc - cc_tile)] = globaltimer_ns();
+            tc_fence_after();
+            ahi = smem_desc_at(abits, sm0 + L.stage0 + (uint32_t)s * stage_bytes);
+          }
+          const uint32_t first_main = newreg ? 0u : 1u;  // 0: the step starts the region
+          const uint32_t first_corr = t == 0 ? 0u : 1u;
+          for (int hh = 0; hh < S.mh; ++hh) {
+            const uint64_t ah = ahi + (uint64_t)(hh * S.a_half16);
+            mma_tf32(dm0 + (uint32_t)(hh * S.nc), ah, bh, idesc, first_main);
+            mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah, bl, idesc, first_corr);
+            mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(kChunkBytes >> 4), bh, idesc, 1u);
+          }
+          bh += (uint64_t)(2 * kLboB >> 4);
+          bl += (uint64_t)(2 * kLboB >> 4);
+          ahi += (uint64_t)(256 >> 4);
+          racc += fs.nused;
+          newreg = racc >= span;
+          if (newreg) {
+            racc -= span;
+            ++rm;
+            dm0 = tmem + (uint32_t)(rm * S.reg_cols);
+          }
+          if (ks == kpc - 1) {
+            mma_commit(&empty[s]);
+            if (trace && (int)(cc - cc_tile) < 8) trace[TR_MMA + (int)(cc - cc_tile)] = globaltimer_ns();
+            ++cc;
           }
         }
+        if (ok) mma_commit(dbar);
       }
-      if (ok) mma_commit(dbar);
     }
-    if (tr && m < 2) tr[TR_ISSUE0 + m] = globaltimer_ns();
   }
   if (!ok) {
-    // let every copy and MMA already issued finish before the CTA lets go of its memory
-    for (int c = landed; c < issued; ++c) mbar_wait(&full[c & 1], (uint32_t)((c >> 1) & 1), kWaitLimit);
+    *fail = 1;
+    // every MMA already issued completes before the tensor memory is released
     mma_commit(quiet);
     mbar_wait(quiet, 0u, kWaitLimit);
   }
-  return ok;
 }
 
-__device__ __forceinline__ void tc_tile(const TcParams& gtp, const int64_t tile) {
+// The tiles blockIdx.x, blockIdx.x + gridDim.x, ... of a launch (every tile of a launch
+// has the same lane extent n).
+template <typename Resolve>
+__device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t total) {
   using namespace tc;
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ __align__(16) TcParams tp;
+  __shared__ __align__(16) TcParams tp;  // the pass of the work warps' current tile
   __shared__ TileTabs tabs;
   __shared__ uint32_t tmem_base_s;
-  __shared__ FF scratch[kThreads / 32];
+  __shared__ FF scratch[kWorkThreads / 32];
   __shared__ double blk_red[kMaxRed];
   __shared__ double totals[kMaxRed];
   __shared__ int s_last;
   __shared__ volatile int s_fail;
   static_assert(sizeof(TcParams) % 4 == 0, "TcParams is copied as 32-bit words");
-  // every supported lane extent has nk >= 2 chunks per matrix: chunks 0 and 1 go out here
-  if (threadIdx.x == kWorkThreads) {
-    // producer lane: barriers, then the first two A chunks, before anything else
-    const TcSmemLayout L0 = tc_layout((int)gtp.p.g.n);
-    uint64_t* b0 = reinterpret_cast<uint64_t*>(sm + L0.bars);
-    for (int k = 0; k < 5; ++k) tc::mbar_init(b0 + k, 1);  // full[2], empty[2], dbar
-    tc::mbar_init(b0 + 5, kWorkThreads);                   // freebar
-    tc::mbar_init(b0 + 6, kWorkThreads);                   // bready
-    tc::mbar_init(b0 + 7, 1);                              // quiet
-    tc::fence_mbar_init();
-    const float* img0 = gtp.images[0];
-    for (int c = 0; c < 2; ++c) {
-      tc::mbar_expect_tx(b0 + c, 2u * kChunkBytes);
-      tc::bulk_g2s(sm + L0.stage0 + c * 2 * kChunkBytes, img0 + (size_t)c * 2 * (kChunkBytes / 4), 2u * kChunkBytes,
-                   b0 + c);
-    }
-    // the rest of the A sequence toward L2 now: the CTAs of a pass walk it in lock step,
-    // and a chunk that is not yet in L2 costs each of them a DRAM round trip
-    const int nk = tc_shape((int)gtp.p.g.n).nk;
-    for (int m = 0; m < gtp.nmat; ++m)
-      for (int q = m == 0 ? 2 : 0; q < nk; ++q)
-        tc::prefetch_l2(gtp.images[m] + (size_t)q * 2 * (kChunkBytes / 4), 2u * kChunkBytes);
-  }
-  for (int k = threadIdx.x; k < (int)(sizeof(TcParams) / 4); k += kThreads)
-    reinterpret_cast<uint32_t*>(&tp)[k] = reinterpret_cast<const uint32_t*>(&gtp)[k];
-  __syncthreads();
-  if (threadIdx.x == 0) trace_mark(tp, tile, TR_START);
-  const PassParams& p = tp.p;
-  const Geometry& g = p.g;
-
-  const int n = (int)g.n;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (blockIdx.x >= total) return;
+  const int n = (int)resolve(blockIdx.x).prm->p.g.n;
   const TcShape S = tc_shape(n);
   const TcSmemLayout L = tc_layout(n);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars);
+  uint64_t* dbar = bars + 2 * kStages;  // MMAs of a fill completed (the work warps drain)
+  uint64_t* freebar = dbar + 1;         // the work warps drained a fill (regions free again)
+  uint64_t* bready = dbar + 2;          // the B operand of the next matrix is written
   float* bhi = reinterpret_cast<float*>(sm + L.bhi);
   float* blo = reinterpret_cast<float*>(sm + L.blo);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars);
-  // bars: full[2] (A chunk landed), empty[2] (MMAs reading a stage completed), then:
-  uint64_t* dbar = bars + 4;     // MMAs of a fill completed (work warps drain)
-  uint64_t* freebar = bars + 5;  // work warps drained a fill (regions free again)
-  uint64_t* bready = bars + 6;   // B operand of the next matrix written
-  // bars + 7: every MMA issued has completed (producer failure path)
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  const int64_t o = tile / g.tiles_per_outer;
-  const int64_t i0 = (tile - o * g.tiles_per_outer) * S.bn;
-  const int64_t base = o * g.n * g.inner + i0;  // element (row 0, column 0) of the tile
-  float2* psi = reinterpret_cast<float2*>(p.psi);
-
-  if (tid == 0) s_fail = 0;
-  build_tile_tabs(p, tabs, o, i0, S.bn);
-  // full-size tables read after the first lane matrix: start their tile rows toward L2
-  // now, so the epilogue loads do not wait for DRAM
-  for (int oi = tp.mat_op[0] + 1; oi < p.nops; ++oi) {
-    const DevOp& op = p.ops[oi];
-    if (op.kind != OP_DIAGND) continue;
-    bool seen = false;
-    for (int q = tp.mat_op[0] + 1; q < oi; ++q) seen |= p.ops[q].kind == OP_DIAGND && p.ops[q].ptr == op.ptr;
-    const float2* t = reinterpret_cast<const float2*>(op.ptr) + base;
-    if (!seen && (reinterpret_cast<uintptr_t>(t) & 15u) == 0)
-      for (int j = tid; j < n; j += kThreads) prefetch_l2(t + (int64_t)j * g.inner, (uint32_t)(S.bn * sizeof(float2)));
+  if (tid == 0) {
+    for (int k = 0; k < 2 * kStages; ++k) mbar_init(bars + k, 1);  // full[], empty[]
+    mbar_init(dbar, 1);
+    mbar_init(freebar, kWorkThreads);
+    mbar_init(bready, kWorkThreads);
+    mbar_init(dbar + 3, 1);  // quiet
+    fence_mbar_init();
+    s_fail = 0;
   }
   if (warp == 0) tmem_alloc(&tmem_base_s, kTmemCols);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
-  if (tid == 0) trace_mark(tp, tile, TR_SETUP);
-
-  // per-thread FP32 partial sums of the norms (at most a few dozen terms each); the
-  // block folds them in float-float and the last CTA in FP64
-  float acc[kMaxRed];
-#pragma unroll
-  for (int r = 0; r < kMaxRed; ++r) acc[r] = 0.0f;
+  const uint32_t sm0 = smem_u32(sm);
 
   if (warp == kWorkThreads / 32) {
-    // ================= producer / MMA warp (lane 0)
-    if (lane == 0 && !mma_producer(S, L, smem_u32(sm), tp.images[0], tp.images[1], tp.nmat, tmem,
-                                   tp.trace ? tp.trace + tile * kTraceSlots : nullptr, 2))
-      s_fail = 1;
+    if (lane == 0) tma_producer(resolve, total, S, sm0, L, &s_fail);
+  } else if (warp == kWorkThreads / 32 + 1) {
+    if (lane == 0) mma_issuer(resolve, total, S, sm0, L, tmem, &s_fail);
   } else {
     // ================= work warps
-    {
-      // prologue: thread = complex column c, rows h, h + G, ... (G = groups); a thread owns
-      // n / G rows (4, 8, 16 or 32) and keeps the loads of a batch in flight together
-      const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
-      if (n / G >= 16)
-        prologue_rows<16>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
-      else if (n / G >= 8)
-        prologue_rows<8>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
-      else
-        prologue_rows<4>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
-      fence_proxy_async();
-      mbar_arrive(bready);
-      if (tid == 0) trace_mark(tp, tile, TR_PROLOGUE);
-    }
-    // drain mapping: warp w reads TMEM lanes 32 (w & 3) .. +31 and one 32-column slice:
-    // n <= 128: the upper warps take the second slice of N = 64; n = 256: the upper warps
-    // take the second 128-row half (N = 32)
     const int lg = warp & 3, up = warp >> 2;
-    const int j = (S.mh == 2 ? 128 * up : 0) + 32 * lg + lane;  // lane-axis row
+    const int j = (S.mh == 2 ? 128 * up : 0) + 32 * lg + lane;  // lane-axis row of the drains
     const bool row_ok = j < n;
-    const uint32_t slice = (uint32_t)(S.mh == 2 ? S.nc * up : 32 * up);
-    const int c0 = S.mh == 2 ? 0 : 16 * up;  // complex column of v[0..1]
+    // 64 FP32 columns per thread: n <= 128 the upper warps take the second half of N =
+    // 128, n = 256 the second 128-row half (its N = 64 columns)
+    const uint32_t slice = (uint32_t)(64 * up);
+    const int c0 = S.mh == 2 ? 0 : 32 * up;  // complex column of v[0..1]
     const uint32_t lane_addr = tmem + ((uint32_t)(lg * 32) << 16) + slice;
     float* stg = bhi;  // output staging reuses the B_hi area once the last GEMM is done
-    int drains = 0;    // completed phases of dbar
-    // the lane-axis weight of this row for the norms after the first matrix, loaded now
-    // (it arrives while the GEMM runs)
-    const float* rw_ptr = nullptr;
-    float rw_val = 0.0f;
-    for (int oi = tp.mat_op[0] + 1; oi < p.nops && rw_ptr == nullptr; ++oi)
-      if (p.ops[oi].kind == OP_NORM) rw_ptr = p.ops[oi].wf[g.sweep_axis];
-    if (rw_ptr && row_ok) rw_val = __ldg(rw_ptr + j);
-    for (int m = 0; m < tp.nmat; ++m) {
-      float v[32];
-#pragma unroll
-      for (int e = 0; e < 32; ++e) v[e] = 0.0f;
-      bool ok = true;
-      for (int f = 0; f < S.fills; ++f) {
-        ok = mbar_wait(dbar, (uint32_t)(drains & 1), kWaitLimit);
-        ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld below is warp-collective
-        if (!ok) break;
-        ++drains;
-        tc_fence_after();
-        // main regions of this fill, then (after the last fill) the correction region;
-        // round-to-nearest FP32 adds in a fixed order
-        const int t0 = f * S.ksteps / S.fills, t1 = (f + 1) * S.ksteps / S.fills;
-        const int nused = (t1 - t0) < S.nmain ? (t1 - t0) : S.nmain;
-        // regions 0 .. nused-1 of the fill, then after the last fill the correction region
-        const int nr = nused + (f + 1 == S.fills ? 1 : 0);
-#pragma unroll 1
-        for (int k = 0; k < nr; ++k) {
-          const int r = k < nused ? k : S.nmain;
-          float w2[16];
-          tmem_ld16(lane_addr + (uint32_t)(r * S.reg_cols), w2);
-#pragma unroll
-          for (int e = 0; e < 16; ++e) v[e] += w2[e];
-          tmem_ld16(lane_addr + (uint32_t)(r * S.reg_cols + 16), w2);
-#pragma unroll
-          for (int e = 0; e < 16; ++e) v[16 + e] += w2[e];
-        }
-        tc_fence_before();
-        if (f + 1 < S.fills) mbar_arrive(freebar);
-        if (tid == 0 && m == 0 && f == 0) trace_mark(tp, tile, TR_DRAIN0);
+    uint32_t drains = 0;
+    const TcParams* cur = nullptr;
+    for (int64_t gt = blockIdx.x; gt < total; gt += gridDim.x) {
+      const TileRef r = resolve(gt);
+      if (r.prm != cur) {
+        for (int k = tid; k < (int)(sizeof(TcParams) / 4); k += kWorkThreads)
+          reinterpret_cast<uint32_t*>(&tp)[k] = reinterpret_cast<const uint32_t*>(r.prm)[k];
+        cur = r.prm;
+        work_sync();
       }
-      if (tid == 0 && m < 2) trace_mark(tp, tile, TR_MAT0 + 2 * m);
-      if (!ok) {
-        s_fail = 1;
-        break;
+      const PassParams& p = tp.p;
+      const Geometry& g = p.g;
+      const int64_t tile = r.tile;
+      const int64_t o = tile / g.tiles_per_outer;
+      const int64_t i0 = (tile - o * g.tiles_per_outer) * S.bn;
+      const int64_t base = o * g.n * g.inner + i0;  // element (row 0, column 0) of the tile
+      float2* psi = reinterpret_cast<float2*>(p.psi);
+      if (tid == 0) trace_mark(tp, tile, TR_START);
+
+      build_tile_tabs(p, tabs, o, i0, S.bn);
+      // full-size tables read after the first lane matrix: start their tile rows toward L2
+      for (int oi = tp.mat_op[0] + 1; oi < p.nops; ++oi) {
+        const DevOp& op = p.ops[oi];
+        if (op.kind != OP_DIAGND) continue;
+        bool seen = false;
+        for (int q = tp.mat_op[0] + 1; q < oi; ++q) seen |= p.ops[q].kind == OP_DIAGND && p.ops[q].ptr == op.ptr;
+        const float2* t = reinterpret_cast<const float2*>(op.ptr) + base;
+        if (!seen && (reinterpret_cast<uintptr_t>(t) & 15u) == 0)
+          for (int jj = tid; jj < n; jj += kWorkThreads)
+            prefetch_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * sizeof(float2)));
       }
-      const bool last = m + 1 == tp.nmat;
-      // ops between this matrix and the next one (or the end of the program)
-      const int sb = tp.mat_op[m] + 1, se = last ? p.nops : tp.mat_op[m + 1];
-      // two halves of 8 complex columns
+      work_sync();  // tabs complete; the previous tile's staging has been stored
+
+      // per-thread FP32 partial sums of the norms of this tile
+      float acc[kMaxRed];
 #pragma unroll
-      for (int hv = 0; hv < 2; ++hv) {
-        if (!row_ok) break;
-        float2 x[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) x[u] = {v[16 * hv + 2 * u], v[16 * hv + 2 * u + 1]};
-        const int cb = c0 + 8 * hv;
-        apply_row<8>(p, tabs, sb, se, x, j, cb, base + (int64_t)j * g.inner + cb, acc, rw_ptr, rw_val);
-        if (last) {
-#pragma unroll
-          for (int u = 0; u < 8; u += 2)
-            *reinterpret_cast<float4*>(stg + j * S.stage_row + 2 * (cb + u)) =
-                make_float4(x[u].x, x[u].y, x[u + 1].x, x[u + 1].y);
-        } else {
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            float h0, l0;
-            const int q = 2 * (cb + u);
-            split_tf32(x[u].x, h0, l0);
-            bhi[boff(q, j, L.sbo_b) >> 2] = h0;
-            blo[boff(q, j, L.sbo_b) >> 2] = l0;
-            split_tf32(x[u].y, h0, l0);
-            bhi[boff(q + 1, j, L.sbo_b) >> 2] = h0;
-            blo[boff(q + 1, j, L.sbo_b) >> 2] = l0;
-          }
-        }
-      }
-      if (!last) {
+      for (int k = 0; k < kMaxRed; ++k) acc[k] = 0.0f;
+      {
+        // prologue: thread = complex column c, rows h, h + G, ... (G = groups)
+        const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
+        if (n / G >= 32)
+          prologue_rows<32>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
+        else if (n / G >= 16)
+          prologue_rows<16>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
+        else if (n / G >= 8)
+          prologue_rows<8>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
+        else
+          prologue_rows<4>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
         fence_proxy_async();
         mbar_arrive(bready);
       }
-      if (tid == 0 && m < 2) trace_mark(tp, tile, TR_EPI0 + 2 * m);
-    }
-  }
-  __syncthreads();
-  if (tid == 0) trace_mark(tp, tile, TR_JOIN);
+      if (tid == 0) trace_mark(tp, tile, TR_PROLOGUE);
+      // the lane-axis weight of this row for the norms after the first matrix, loaded
+      // now (it arrives while the GEMM runs)
+      const float* rw_ptr = nullptr;
+      float rw_val = 0.0f;
+      for (int oi = tp.mat_op[0] + 1; oi < p.nops && rw_ptr == nullptr; ++oi)
+        if (p.ops[oi].kind == OP_NORM) rw_ptr = p.ops[oi].wf[g.sweep_axis];
+      if (rw_ptr && row_ok) rw_val = __ldg(rw_ptr + j);
 
-  if (!s_fail && tid < kWorkThreads) {
-    // coalesced store of the staged tile: thread = complex column
-    const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
-    for (int kb = h; kb < n; kb += 4 * G) {
+      bool ok = true;
+      for (int m = 0; m < tp.nmat && ok; ++m) {
+        float v[kVals];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int k = kb + u * G;
-        psi[base + (int64_t)k * g.inner + c] = *reinterpret_cast<const float2*>(bhi + k * S.stage_row + 2 * c);
+        for (int e = 0; e < kVals; ++e) v[e] = 0.0f;
+        for (int f = 0; f < S.fills; ++f) {
+          ok = work_all(mbar_wait(dbar, drains & 1u, kWaitLimit));
+          if (!ok) break;
+          ++drains;
+          tc_fence_after();
+          const FillSpan fs = fill_span(S, f);
+          // regions 0 .. nused-1 of the fill, then after the last fill the correction
+          // region; round-to-nearest FP32 adds in a fixed order
+          const int nr = fs.nused + (f + 1 == S.fills ? 1 : 0);
+#pragma unroll 1
+          for (int k = 0; k < nr; ++k) {
+            const int rg = k < fs.nused ? k : S.nmain;
+#pragma unroll
+            for (int hv = 0; hv < kVals / 16; ++hv) {
+              float w2[16];
+              tmem_ld16(lane_addr + (uint32_t)(rg * S.reg_cols + 16 * hv), w2);
+#pragma unroll
+              for (int e = 0; e < 16; ++e) v[16 * hv + e] += w2[e];
+            }
+          }
+          tc_fence_before();
+          if (f + 1 < S.fills) mbar_arrive(freebar);
+        }
+        if (!ok) break;
+        if (tid == 0 && m < 2) trace_mark(tp, tile, TR_MAT0 + 2 * m);
+        const bool last = m + 1 == tp.nmat;
+        // ops between this matrix and the next one (or the end of the program)
+        const int sb = tp.mat_op[m] + 1, se = last ? p.nops : tp.mat_op[m + 1];
+        if (row_ok) {
+          // op-major over the thread's 32 complex values: the table loads of an op are all
+          // in flight together
+          float2 x[kVals / 2];
+#pragma unroll
+          for (int u = 0; u < kVals / 2; ++u) x[u] = {v[2 * u], v[2 * u + 1]};
+          apply_row<kVals / 2>(p, tabs, sb, se, x, j, c0, base + (int64_t)j * g.inner + c0, acc, rw_ptr, rw_val);
+          if (last) {
+#pragma unroll
+            for (int u = 0; u < kVals / 2; u += 2)
+              *reinterpret_cast<float4*>(stg + j * S.stage_row + 2 * (c0 + u)) =
+                  make_float4(x[u].x, x[u].y, x[u + 1].x, x[u + 1].y);
+          } else {
+            // B rows q = 2 (c0 + u) (+1) of K row j: c0 is a multiple of 8, so the core-matrix
+            // group of q is c0 / 4 + u / 4 and its row within the group 2 (u % 4) (+1)
+            const uint32_t w0 = boff(2 * c0, j, L.sbo_b) >> 2;  // word offset of (q = 2 c0, k = j)
+#pragma unroll
+            for (int u = 0; u < kVals / 2; ++u) {
+              const uint32_t w = w0 + (uint32_t)(u >> 2) * (L.sbo_b >> 2) + (uint32_t)(u & 3) * 8u;
+              float h0, l0;
+              split_tf32(x[u].x, h0, l0);
+              bhi[w] = h0;
+              blo[w] = l0;
+              split_tf32(x[u].y, h0, l0);
+              bhi[w + 4] = h0;
+              blo[w + 4] = l0;
+            }
+          }
+        }
+        if (!last) {
+          fence_proxy_async();
+          mbar_arrive(bready);
+        }
+        if (tid == 0 && m < 2) trace_mark(tp, tile, TR_EPI0 + 2 * m);
       }
-    }
-  }
-  if (tid == 0) trace_mark(tp, tile, TR_STORE);
+      if (!ok) {
+        if (tid == 0) s_fail = 1;
+        break;
+      }
+      work_sync();  // staging complete
 
-  // ---- norm partials (fixed order) and last-CTA finalize
-  for (int r = 0; r < p.nred; ++r) {
-    const FF t = block_sum(acc[r], scratch);
-    if (tid == 0) blk_red[r] = (double)t.hi + (double)t.lo;
-  }
-  __syncthreads();
-  if (tid == 0) trace_mark(tp, tile, TR_NORMS);
-  if (tid == 0) {
-    if (s_fail && tp.error_slot >= 0) p.slots[tp.error_slot] = 1.0;
-    for (int r = 0; r < p.nred; ++r) p.partials[(int64_t)r * g.tiles + tile] = blk_red[r];
-    __threadfence();
-    const unsigned int ticket = atomicAdd(p.counter, 1u);
-    s_last = ticket == (unsigned int)(g.tiles - 1);
-    trace_mark(tp, tile, TR_TICKET);
-  }
-  __syncthreads();
-  if (s_last) {
-    __threadfence();
-    for (int r = warp; r < p.nred; r += kThreads / 32) {
-      double v = 0.0;
-      for (int64_t b = lane; b < g.tiles; b += 32) v += __ldcg(p.partials + (int64_t)r * g.tiles + b);
+      // coalesced store of the staged tile: thread = complex column
+      {
+        const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
+        for (int kb = h; kb < n; kb += 4 * G) {
 #pragma unroll
-      for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_down_sync(0xffffffffu, v, o2);
-      if (lane == 0) totals[r] = v;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      for (int oi = 0; oi < p.nops; ++oi) run_scalar_tc(p, p.ops[oi], totals);
-      __threadfence();
-      *p.counter = 0u;
+          for (int u = 0; u < 4; ++u) {
+            const int k = kb + u * G;
+            psi[base + (int64_t)k * g.inner + c] = *reinterpret_cast<const float2*>(stg + k * S.stage_row + 2 * c);
+          }
+        }
+      }
+      if (tid == 0) trace_mark(tp, tile, TR_STORE);
+
+      // norm partials of this tile (float-float, fixed order) and the last tile's FP64 fold
+      for (int k = 0; k < p.nred; ++k) {
+        const FF t = block_sum(acc[k], scratch);
+        if (tid == 0) blk_red[k] = (double)t.hi + (double)t.lo;
+      }
+      if (tid == 0) {
+        for (int k = 0; k < p.nred; ++k) p.partials[(int64_t)k * g.tiles + tile] = blk_red[k];
+        __threadfence();
+        const unsigned int ticket = atomicAdd(p.counter, 1u);
+        s_last = ticket == (unsigned int)(g.tiles - 1);
+      }
+      work_sync();
+      if (s_last) {
+        __threadfence();
+        for (int k = warp; k < p.nred; k += kWorkThreads / 32) {
+          double a = 0.0;
+          for (int64_t b = lane; b < g.tiles; b += 32) a += __ldcg(p.partials + (int64_t)k * g.tiles + b);
+#pragma unroll
+          for (int o2 = 16; o2 > 0; o2 >>= 1) a += __shfl_down_sync(0xffffffffu, a, o2);
+          if (lane == 0) totals[k] = a;
+        }
+        work_sync();
+        if (tid == 0) {
+          for (int oi = 0; oi < p.nops; ++oi) run_scalar_tc(p, p.ops[oi], totals);
+          __threadfence();
+          *p.counter = 0u;
+        }
+      }
+      if (tid == 0) trace_mark(tp, tile, TR_END);
     }
   }
-
-  // ---- teardown: tensor memory (every MMA has completed: drained, or waited on above)
+  __syncthreads();
+  if (tid == 0 && s_fail) {
+    // the pass of the first tile records the failure
+    const TcParams* f0 = resolve(blockIdx.x).prm;
+    if (f0->error_slot >= 0) f0->p.slots[f0->error_slot] = 1.0;
+  }
+  // teardown: every MMA has completed (drained, or waited on by the MMA warp)
   tc_fence_before();
   __syncthreads();
-  if (tid == 0) trace_mark(tp, tile, TR_END);
   if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
-__global__ void __launch_bounds__(kThreads, 2) angular_tc_kernel(const __grid_constant__ TcParams tp) {
-  tc_tile(tp, blockIdx.x);
+__global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_constant__ TcParams tp) {
+  const TcParams* prm = &tp;
+  tc_persistent([prm](int64_t t) { return TileRef{prm, t}; }, tp.p.g.tiles);
 }
 
-// Many propagations' lane-matrix passes in one launch: block b runs tile
-// (b - offsets[i]) of params[i], offsets[i] <= b < offsets[i + 1].
-__global__ void __launch_bounds__(kThreads, 2) angular_tc_kernel_batched(const TcParams* __restrict__ params,
+// Many propagations' lane-matrix passes in one launch (all with the same lane extent):
+// global tile b is tile (b - offsets[i]) of params[i], offsets[i] <= b < offsets[i + 1];
+// offsets[count] is the total.
+__global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel_batched(const TcParams* __restrict__ params,
                                                                         const int64_t* __restrict__ offsets,
                                                                         int count) {
-  const int64_t b = blockIdx.x;
-  int lo = 0, hi = count - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (offsets[mid] <= b)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  tc_tile(params[lo], b - offsets[lo]);
+  auto resolve = [params, offsets, count](int64_t b) {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (offsets[mid] <= b)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    return TileRef{params + lo, b - offsets[lo]};
+  };
+  tc_persistent(resolve, offsets[count]);
 }
 
 // ------------------------------------------------------------------ host side
@@ -784,7 +860,7 @@ static size_t tc_max_dynamic_smem() {
   return m;
 }
 
-// two CTAs per SM: the whole shared-memory carveout, each CTA below half of it
+// one persistent CTA per SM, with the whole shared-memory carveout
 static bool configure_once(const void* kern, bool& flag) {
   if (flag) return true;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_max_dynamic_smem()) !=
@@ -797,13 +873,25 @@ static bool configure_once(const void* kern, bool& flag) {
   return true;
 }
 
+// persistent grid: one CTA per SM (fewer when there are fewer tiles)
+static unsigned persistent_grid(int64_t tiles) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+      sms = 1;
+  }
+  return (unsigned)(tiles < sms ? tiles : sms);
+}
+
 cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,
                                       size_t smem, cudaStream_t s) {
   static bool configured = false;
   if (!configure_once((const void*)angular_tc_kernel_batched, configured)) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
-  angular_tc_kernel_batched<<<(unsigned)blocks, kThreads, smem, s>>>(reinterpret_cast<const TcParams*>(params_dev),
-                                                                     offsets_dev, count);
+  angular_tc_kernel_batched<<<persistent_grid(blocks), kThreads, smem, s>>>(
+      reinterpret_cast<const TcParams*>(params_dev), offsets_dev, count);
   count_launch();
   return cudaGetLastError();
 }
@@ -868,7 +956,7 @@ cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, 
   static bool configured = false;
   if (!configure_once((const void*)angular_tc_kernel, configured)) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
-  angular_tc_kernel<<<(unsigned)p.g.tiles, kThreads, smem, s>>>(tp);
+  angular_tc_kernel<<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
   count_launch();
   return cudaGetLastError();
 }

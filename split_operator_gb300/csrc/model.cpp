@@ -347,7 +347,8 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
   std::string name = "f32 tc3xtf32 axis" + std::to_string(axis) + ":";
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
-    RecordedPass r{RecordedPass::TensorCore, false, p, std::vector<unsigned char>(tc_params_bytes()), 128,
+    // threads: the lane extent (one batched launch serves one n; the kernel's thread count is fixed)
+    RecordedPass r{RecordedPass::TensorCore, false, p, std::vector<unsigned char>(tc_params_bytes()), (int)g.n,
                    angular_tc_smem_bytes((int)g.n), name, pass_bytes(ops, g)};
     make_tc_params(p, mats, nmat, images, timeout_slot, r.tcp.data());
     recording->push_back(std::move(r));
