@@ -31,6 +31,10 @@
 // float-float and across tiles in FP64 by the last tile of the pass, in a fixed order.
 // Every mbarrier wait is bounded (2 s); on a timeout the CTA records an error in a
 // slot, lets its copies and MMAs finish (bounded), frees its tensor memory and returns.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
 #include "common.cuh"
 #include "tc_common.cuh"
 
@@ -51,6 +55,8 @@ constexpr int kVals = 64;            // FP32 accumulator columns a work thread d
 constexpr int kColtSlots = 4;        // DIAG1D ops on a non-lane axis per pass
 
 struct TcShape {
+  bool par;      // parity-split lane matrices (two K = n/2 GEMMs, one per M half)
+  int kdim;      // K of each GEMM: n, or n / 2 with par
   int mh;        // 128-row halves of M
   int bn;        // complex columns per tile
   int nc;        // fp32 columns = MMA N
@@ -73,14 +79,18 @@ struct TcShape {
 // corrections A_hi B_lo + A_lo B_hi are 2^-11 smaller and share the fourth region.
 //   n <= 128: M = 128, BN = 32 (N = 64), A chunks of K = 16
 //   n = 256 : M = 256 as two 128-row halves, BN = 16 (N = 32), A chunks of K = 8
-__host__ __device__ inline TcShape tc_shape(int n) {
+// par: the two lane matrices split by parity into two half-size GEMMs (n = 256 only):
+// K = n / 2, the 128-row halves of M are the even and odd parts, each with its own B
+__host__ __device__ inline TcShape tc_shape(int n, bool par = false) {
   TcShape s{};
+  s.par = par && n == 256;
   s.mh = n == 256 ? 2 : 1;
   s.bn = n == 256 ? 32 : 64;
   s.nc = 2 * s.bn;
   s.chunk_k = 16 / s.mh;
-  s.nk = n / s.chunk_k;
-  s.ksteps = n / 8;
+  s.kdim = s.par ? n / 2 : n;
+  s.nk = s.kdim / s.chunk_k;
+  s.ksteps = s.kdim / 8;
   s.reg_cols = s.nc * s.mh;
   s.nmain = kRegions - 1;
   s.fills = (s.ksteps + kFillSteps - 1) / kFillSteps;
@@ -92,16 +102,18 @@ __host__ __device__ inline TcShape tc_shape(int n) {
 }
 
 struct TcSmemLayout {
-  uint32_t stage0, bhi, blo, bars, sbo_b, bbytes, total;
+  uint32_t stage0, bhi, blo, bars, sbo_b, bhalf, bbytes, total;
 };
 
 // [kStages x 16 KB A stages][B_hi][B_lo][mbarriers: full[kStages], empty[kStages], dbar,
-// freebar, bready, quiet]
-__host__ __device__ inline TcSmemLayout tc_layout(int n) {
-  const TcShape s = tc_shape(n);
+// freebar, bready, quiet].  With par each of B_hi / B_lo holds two K = n/2 operands,
+// bhalf bytes apart (the even / odd or sum / difference halves).
+__host__ __device__ inline TcSmemLayout tc_layout(int n, bool par = false) {
+  const TcShape s = tc_shape(n, par);
   TcSmemLayout L{};
-  L.sbo_b = (uint32_t)(n / 4) * kLboB + 16;
-  L.bbytes = (uint32_t)(s.nc / 8) * L.sbo_b;
+  L.sbo_b = (uint32_t)(s.kdim / 4) * kLboB + 16;
+  L.bhalf = (uint32_t)(s.nc / 8) * L.sbo_b;
+  L.bbytes = (s.par ? 2u : 1u) * L.bhalf;
   L.bbytes = (L.bbytes + 127u) & ~127u;
   L.stage0 = 0;
   L.bhi = kStages * 2u * kChunkBytes;
@@ -337,11 +349,13 @@ __device__ __forceinline__ void apply_col(const PassParams& p, const TileTabs& T
 }
 
 // Prologue of one thread (tile column c, rows h, h + G, ...): loads, the ops before the
-// first lane matrix, and the split into the B_hi / B_lo operand images.
+// first lane matrix, and the split into the B_hi / B_lo operand images (row j goes to K
+// row j >> kshift: kshift = 1 for the even / odd halves of a parity-split matrix, whose
+// half the caller selects through bhi / blo).
 template <int NB>
 __device__ __forceinline__ void prologue_rows(const PassParams& p, const TileTabs& T, int oe, const float2* psi,
                                               int64_t base, int c, int h, int G, int n, float* bhi, float* blo,
-                                              uint32_t sbo_b, float* acc) {
+                                              uint32_t sbo_b, float* acc, int kshift = 0) {
   const int64_t rstride = (int64_t)G * p.g.inner;
   for (int kb = h; kb < n; kb += NB * G) {
     const int64_t ix0 = base + (int64_t)kb * p.g.inner + c;
@@ -355,13 +369,82 @@ __device__ __forceinline__ void prologue_rows(const PassParams& p, const TileTab
       float rh, rl, ih, il;
       tc::split_tf32(v[u].x, rh, rl);
       tc::split_tf32(v[u].y, ih, il);
-      const uint32_t a0 = boff(2 * c, j, sbo_b) >> 2, a1 = boff(2 * c + 1, j, sbo_b) >> 2;
+      const uint32_t a0 = boff(2 * c, j >> kshift, sbo_b) >> 2, a1 = boff(2 * c + 1, j >> kshift, sbo_b) >> 2;
       bhi[a0] = rh;
       blo[a0] = rl;
       bhi[a1] = ih;
       blo[a1] = il;
     }
   }
+}
+
+// Prologue before a sum / difference parity-split matrix (rows j and n-1-j of every
+// pair j < n/2): the ops before the first matrix on both rows, then s = a + b into the
+// first B half and d = a - b into the second, at K row j.
+template <int NB>
+__device__ __forceinline__ void prologue_pairs(const PassParams& p, const TileTabs& T, int oe, const float2* psi,
+                                               int64_t base, int c, int h, int G, int n, float* bhi, float* blo,
+                                               uint32_t bhalf_words, uint32_t sbo_b, float* acc) {
+  const int64_t rstride = (int64_t)G * p.g.inner;
+  for (int kb = h; kb < n / 2; kb += NB * G) {
+    const int64_t ia = base + (int64_t)kb * p.g.inner + c;
+    const int64_t ib = base + (int64_t)(n - 1 - kb) * p.g.inner + c;
+    float2 a[NB], b[NB];
+#pragma unroll
+    for (int u = 0; u < NB; ++u) {
+      a[u] = psi[ia + u * rstride];
+      b[u] = psi[ib - u * rstride];
+    }
+    apply_col<NB>(p, T, 0, oe, a, kb, G, c, ia, rstride, acc);
+    apply_col<NB>(p, T, 0, oe, b, n - 1 - kb, -G, c, ib, -rstride, acc);
+#pragma unroll
+    for (int u = 0; u < NB; ++u) {
+      const int j = kb + u * G;
+      const uint32_t a0 = boff(2 * c, j, sbo_b) >> 2, a1 = boff(2 * c + 1, j, sbo_b) >> 2;
+      float h0, l0;
+      tc::split_tf32(a[u].x + b[u].x, h0, l0);
+      bhi[a0] = h0;
+      blo[a0] = l0;
+      tc::split_tf32(a[u].y + b[u].y, h0, l0);
+      bhi[a1] = h0;
+      blo[a1] = l0;
+      tc::split_tf32(a[u].x - b[u].x, h0, l0);
+      bhi[bhalf_words + a0] = h0;
+      blo[bhalf_words + a0] = l0;
+      tc::split_tf32(a[u].y - b[u].y, h0, l0);
+      bhi[bhalf_words + a1] = h0;
+      blo[bhalf_words + a1] = l0;
+    }
+  }
+}
+
+// B operand row of NV complex values: columns c0 .. c0 + NV - 1 (c0 a multiple of 8) at K
+// row k, split into tf32 hi / lo
+template <int NV>
+__device__ __forceinline__ void write_b_row(const float2 (&x)[NV], int c0, int k, float* bhi, float* blo,
+                                            uint32_t sbo_b) {
+  // column q = 2 (c0 + u) (+1): core-matrix group c0 / 4 + u / 4, row 2 (u % 4) (+1)
+  const uint32_t w0 = boff(2 * c0, k, sbo_b) >> 2;
+#pragma unroll
+  for (int u = 0; u < NV; ++u) {
+    const uint32_t w = w0 + (uint32_t)(u >> 2) * (sbo_b >> 2) + (uint32_t)(u & 3) * 8u;
+    float h0, l0;
+    tc::split_tf32(x[u].x, h0, l0);
+    bhi[w] = h0;
+    blo[w] = l0;
+    tc::split_tf32(x[u].y, h0, l0);
+    bhi[w + 4] = h0;
+    blo[w + 4] = l0;
+  }
+}
+
+// NV complex values of row j, columns c0 .., into the output staging
+template <int NV>
+__device__ __forceinline__ void stage_row(const float2 (&x)[NV], int c0, int j, float* stg, int stage_row_floats) {
+#pragma unroll
+  for (int u = 0; u < NV; u += 2)
+    *reinterpret_cast<float4*>(stg + j * stage_row_floats + 2 * (c0 + u)) =
+        make_float4(x[u].x, x[u].y, x[u + 1].x, x[u + 1].y);
 }
 
 __device__ void run_scalar_tc(const PassParams& p, const DevOp& op, const double* totals) {
@@ -391,6 +474,7 @@ struct TcParams {
   int32_t nmat;
   const float* images[2]; // A chunk images per matrix: nk x (hi 8 KB, lo 8 KB)
   int32_t error_slot;
+  int32_t parity[2];          // per matrix: 0 plain; 1 sum / difference rows; 2 even / odd columns
   unsigned long long* trace;  // optional phase timestamps, kTraceSlots per tile (nullptr: off)
 };
 
@@ -482,6 +566,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
   const uint32_t idesc = idesc_tf32(128, (uint32_t)S.nc);
   const uint64_t bbits = smem_desc_bits(kLboB, L.sbo_b), abits = smem_desc_bits(128, (uint32_t)S.sbo_a);
   const int kpc = S.chunk_k / 8;  // K steps per chunk
+  const uint64_t bstep_half = S.par ? (uint64_t)(L.bhalf >> 4) : 0u;
   int64_t cc = 0;                 // chunks consumed
   int s = 0;                      // stage of the chunk being consumed
   uint64_t ahi = 0;               // A_hi descriptor of the current K step (a chunk may span two fills)
@@ -528,9 +613,10 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
           const uint32_t first_corr = t == 0 ? 0u : 1u;
           for (int hh = 0; hh < S.mh; ++hh) {
             const uint64_t ah = ahi + (uint64_t)(hh * S.a_half16);
-            mma_tf32(dm0 + (uint32_t)(hh * S.nc), ah, bh, idesc, first_main);
-            mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah, bl, idesc, first_corr);
-            mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(kChunkBytes >> 4), bh, idesc, 1u);
+            const uint64_t bo = (uint64_t)hh * bstep_half;  // parity split: each half its own B
+            mma_tf32(dm0 + (uint32_t)(hh * S.nc), ah, bh + bo, idesc, first_main);
+            mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah, bl + bo, idesc, first_corr);
+            mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(kChunkBytes >> 4), bh + bo, idesc, 1u);
           }
           bh += (uint64_t)(2 * kLboB >> 4);
           bl += (uint64_t)(2 * kLboB >> 4);
@@ -577,9 +663,11 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   static_assert(sizeof(TcParams) % 4 == 0, "TcParams is copied as 32-bit words");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (blockIdx.x >= total) return;
-  const int n = (int)resolve(blockIdx.x).prm->p.g.n;
-  const TcShape S = tc_shape(n);
-  const TcSmemLayout L = tc_layout(n);
+  const TcParams* first = resolve(blockIdx.x).prm;  // every tile of a launch shares n and parity mode
+  const int n = (int)first->p.g.n;
+  const bool par = first->parity[0] != 0;
+  const TcShape S = tc_shape(n, par);
+  const TcSmemLayout L = tc_layout(n, par);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars);
   uint64_t* dbar = bars + 2 * kStages;  // MMAs of a fill completed (the work warps drain)
   uint64_t* freebar = dbar + 1;         // the work warps drained a fill (regions free again)
@@ -610,13 +698,16 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   } else {
     // ================= work warps
     const int lg = warp & 3, up = warp >> 2;
-    const int j = (S.mh == 2 ? 128 * up : 0) + 32 * lg + lane;  // lane-axis row of the drains
+    const int i = 32 * lg + lane;                    // TMEM lane within a 128-row half
+    const int j = (S.mh == 2 ? 128 * up : 0) + i;    // lane-axis row of a plain drain
     const bool row_ok = j < n;
-    // 64 FP32 columns per thread: n <= 128 the upper warps take the second half of N =
-    // 128, n = 256 the second 128-row half (its N = 64 columns)
-    const uint32_t slice = (uint32_t)(64 * up);
-    const int c0 = S.mh == 2 ? 0 : 32 * up;  // complex column of v[0..1]
-    const uint32_t lane_addr = tmem + ((uint32_t)(lg * 32) << 16) + slice;
+    // 64 FP32 columns per thread.  Plain: n <= 128 the upper warps take the second half
+    // of N = 128, n = 256 the second 128-row half (its N = 64 columns).  Parity split,
+    // sum / difference matrix: as plain, the row of half h lane i being 2 i + h.  Even /
+    // odd matrix: columns 16 up .. 16 up + 15 of both halves (E, O), rows i and n-1-i.
+    const int c0 = S.mh == 2 ? 0 : 32 * up;  // complex column of v[0..1] (plain)
+    const uint32_t lane_base = tmem + ((uint32_t)(lg * 32) << 16);
+    const uint32_t bhw = L.bhalf / 4;  // words between the two B halves
     float* stg = bhi;  // output staging reuses the B_hi area once the last GEMM is done
     uint32_t drains = 0;
     const TcParams* cur = nullptr;
@@ -658,7 +749,13 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       {
         // prologue: thread = complex column c, rows h, h + G, ... (G = groups)
         const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
-        if (n / G >= 32)
+        const int k0 = tp.parity[0];
+        if (k0 == 1)
+          prologue_pairs<16>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc);
+        else if (k0 == 2)  // G is even: every row of this thread has the parity of h
+          prologue_rows<32>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi + (h & 1) * bhw, blo + (h & 1) * bhw,
+                            L.sbo_b, acc, 1);
+        else if (n / G >= 32)
           prologue_rows<32>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
         else if (n / G >= 16)
           prologue_rows<16>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
@@ -670,16 +767,24 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         mbar_arrive(bready);
       }
       if (tid == 0) trace_mark(tp, tile, TR_PROLOGUE);
-      // the lane-axis weight of this row for the norms after the first matrix, loaded
-      // now (it arrives while the GEMM runs)
+      // lane-axis weights of this thread's epilogue rows for the norms after the first
+      // matrix, loaded now (they arrive while the GEMM runs)
       const float* rw_ptr = nullptr;
-      float rw_val = 0.0f;
       for (int oi = tp.mat_op[0] + 1; oi < p.nops && rw_ptr == nullptr; ++oi)
         if (p.ops[oi].kind == OP_NORM) rw_ptr = p.ops[oi].wf[g.sweep_axis];
-      if (rw_ptr && row_ok) rw_val = __ldg(rw_ptr + j);
+      float rw_plain = 0.0f, rw_sum = 0.0f, rw_a = 0.0f, rw_b = 0.0f;
+      if (rw_ptr) {
+        if (row_ok) rw_plain = __ldg(rw_ptr + j);
+        if (S.par) {
+          rw_sum = __ldg(rw_ptr + 2 * i + up);
+          rw_a = __ldg(rw_ptr + i);
+          rw_b = __ldg(rw_ptr + (n - 1 - i));
+        }
+      }
 
       bool ok = true;
       for (int m = 0; m < tp.nmat && ok; ++m) {
+        const int kind = tp.parity[m];
         float v[kVals];
 #pragma unroll
         for (int e = 0; e < kVals; ++e) v[e] = 0.0f;
@@ -697,8 +802,10 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             const int rg = k < fs.nused ? k : S.nmain;
 #pragma unroll
             for (int hv = 0; hv < kVals / 16; ++hv) {
+              const uint32_t col = kind == 2 ? (uint32_t)((hv >> 1) * S.nc + 32 * up + 16 * (hv & 1))
+                                             : (uint32_t)(64 * up + 16 * hv);
               float w2[16];
-              tmem_ld16(lane_addr + (uint32_t)(rg * S.reg_cols + 16 * hv), w2);
+              tmem_ld16(lane_base + (uint32_t)(rg * S.reg_cols) + col, w2);
 #pragma unroll
               for (int e = 0; e < 16; ++e) v[16 * hv + e] += w2[e];
             }
@@ -709,35 +816,53 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         if (!ok) break;
         if (tid == 0 && m < 2) trace_mark(tp, tile, TR_MAT0 + 2 * m);
         const bool last = m + 1 == tp.nmat;
+        const int next = last ? -1 : tp.parity[m + 1];
         // ops between this matrix and the next one (or the end of the program)
         const int sb = tp.mat_op[m] + 1, se = last ? p.nops : tp.mat_op[m + 1];
-        if (row_ok) {
-          // op-major over the thread's 32 complex values: the table loads of an op are all
-          // in flight together
-          float2 x[kVals / 2];
+        if (kind != 2) {
+          const int jr = kind == 1 ? 2 * i + up : j;
+          if (jr < n) {
+            // op-major over the thread's 32 complex values: the table loads of an op are all
+            // in flight together
+            float2 x[kVals / 2];
 #pragma unroll
-          for (int u = 0; u < kVals / 2; ++u) x[u] = {v[2 * u], v[2 * u + 1]};
-          apply_row<kVals / 2>(p, tabs, sb, se, x, j, c0, base + (int64_t)j * g.inner + c0, acc, rw_ptr, rw_val);
+            for (int u = 0; u < kVals / 2; ++u) x[u] = {v[2 * u], v[2 * u + 1]};
+            apply_row<kVals / 2>(p, tabs, sb, se, x, jr, c0, base + (int64_t)jr * g.inner + c0, acc, rw_ptr,
+                                 kind == 1 ? rw_sum : rw_plain);
+            if (last)
+              stage_row<kVals / 2>(x, c0, jr, stg, S.stage_row);
+            else if (next == 2)
+              write_b_row<kVals / 2>(x, c0, jr >> 1, bhi + (jr & 1) * bhw, blo + (jr & 1) * bhw, L.sbo_b);
+            else
+              write_b_row<kVals / 2>(x, c0, jr, bhi, blo, L.sbo_b);
+          }
+        } else {
+          // even / odd matrix: psi_i = E + O, psi_{n-1-i} = E - O
+          const int cc0 = 16 * up, ja = i, jb = n - 1 - i;
+          float2 xa[kVals / 4], xb[kVals / 4];
+#pragma unroll
+          for (int u = 0; u < kVals / 4; ++u) {
+            const float er = v[2 * u], ei = v[2 * u + 1], orr = v[kVals / 2 + 2 * u], oi = v[kVals / 2 + 2 * u + 1];
+            xa[u] = {er + orr, ei + oi};
+            xb[u] = {er - orr, ei - oi};
+          }
+          apply_row<kVals / 4>(p, tabs, sb, se, xa, ja, cc0, base + (int64_t)ja * g.inner + cc0, acc, rw_ptr, rw_a);
+          apply_row<kVals / 4>(p, tabs, sb, se, xb, jb, cc0, base + (int64_t)jb * g.inner + cc0, acc, rw_ptr, rw_b);
           if (last) {
+            stage_row<kVals / 4>(xa, cc0, ja, stg, S.stage_row);
+            stage_row<kVals / 4>(xb, cc0, jb, stg, S.stage_row);
+          } else if (next == 1) {
+            // sum / difference operand of the next matrix, K row i
+            float2 sd[kVals / 4];
 #pragma unroll
-            for (int u = 0; u < kVals / 2; u += 2)
-              *reinterpret_cast<float4*>(stg + j * S.stage_row + 2 * (c0 + u)) =
-                  make_float4(x[u].x, x[u].y, x[u + 1].x, x[u + 1].y);
+            for (int u = 0; u < kVals / 4; ++u) sd[u] = {xa[u].x + xb[u].x, xa[u].y + xb[u].y};
+            write_b_row<kVals / 4>(sd, cc0, i, bhi, blo, L.sbo_b);
+#pragma unroll
+            for (int u = 0; u < kVals / 4; ++u) sd[u] = {xa[u].x - xb[u].x, xa[u].y - xb[u].y};
+            write_b_row<kVals / 4>(sd, cc0, i, bhi + bhw, blo + bhw, L.sbo_b);
           } else {
-            // B rows q = 2 (c0 + u) (+1) of K row j: c0 is a multiple of 8, so the core-matrix
-            // group of q is c0 / 4 + u / 4 and its row within the group 2 (u % 4) (+1)
-            const uint32_t w0 = boff(2 * c0, j, L.sbo_b) >> 2;  // word offset of (q = 2 c0, k = j)
-#pragma unroll
-            for (int u = 0; u < kVals / 2; ++u) {
-              const uint32_t w = w0 + (uint32_t)(u >> 2) * (L.sbo_b >> 2) + (uint32_t)(u & 3) * 8u;
-              float h0, l0;
-              split_tf32(x[u].x, h0, l0);
-              bhi[w] = h0;
-              blo[w] = l0;
-              split_tf32(x[u].y, h0, l0);
-              bhi[w + 4] = h0;
-              blo[w + 4] = l0;
-            }
+            write_b_row<kVals / 4>(xa, cc0, ja >> 1, bhi + (ja & 1) * bhw, blo + (ja & 1) * bhw, L.sbo_b);
+            write_b_row<kVals / 4>(xb, cc0, jb >> 1, bhi + (jb & 1) * bhw, blo + (jb & 1) * bhw, L.sbo_b);
           }
         }
         if (!last) {
@@ -834,20 +959,21 @@ __global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel_batched(const T
 }
 
 // ------------------------------------------------------------------ host side
-size_t angular_tc_smem_bytes(int n) { return tc_layout(n).total; }
+size_t angular_tc_smem_bytes(int n, bool par) { return tc_layout(n, par).total; }
 
 int angular_tc_columns(int n) { return tc_shape(n).bn; }
 
 size_t tc_params_bytes() { return sizeof(TcParams); }
 
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
-                    void* out) {
+                    const int* parity, void* out) {
   TcParams tp{};
   tp.p = p;
   tp.nmat = nmat;
   for (int i = 0; i < nmat; ++i) {
     tp.mat_op[i] = mat_op[i];
     tp.images[i] = images[i];
+    tp.parity[i] = parity ? parity[i] : 0;
   }
   tp.error_slot = error_slot;
   std::memcpy(out, &tp, sizeof(TcParams));
@@ -856,7 +982,8 @@ void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const floa
 // the largest dynamic shared memory any supported lane extent asks for
 static size_t tc_max_dynamic_smem() {
   size_t m = 0;
-  for (int n = 32; n <= 256; n *= 2) m = tc_layout(n).total > m ? tc_layout(n).total : m;
+  for (int n = 32; n <= 256; n *= 2)
+    for (int par = 0; par < 2; ++par) m = tc_layout(n, par).total > m ? tc_layout(n, par).total : m;
   return m;
 }
 
@@ -908,11 +1035,11 @@ bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis) {
   return across <= kColtSlots;
 }
 
-// Chunk images of one real n x n matrix (row-major FP64) for the 3xTF32 A operand: per
-// K chunk, 16 KB of tf32-exact high parts then 16 KB of tf32-exact remainders, each in
-// the K-major core-matrix order (row-group stride sbo_a, K core-matrix stride 128 B).
-void angular_tc_images(const double* m, int n, std::vector<float>& out) {
-  const TcShape S = tc_shape(n);
+// Chunk images of the 3xTF32 A operand: rows x kdim values a(r, k), per K chunk 8 KB of
+// tf32-exact high parts then 8 KB of tf32-exact remainders, each in the K-major
+// core-matrix order (row-group stride sbo_a, K core-matrix stride 128 B).
+template <typename F>
+static void tc_images(const TcShape& S, F a, std::vector<float>& out) {
   const int rows = 128 * S.mh;
   out.assign((size_t)S.nk * 2 * (kChunkBytes / 4), 0.0f);
   auto tf32 = [](float x) {
@@ -928,8 +1055,7 @@ void angular_tc_images(const double* m, int n, std::vector<float>& out) {
     float* lo = hi + kChunkBytes / 4;
     for (int r = 0; r < rows; ++r)
       for (int kk = 0; kk < S.chunk_k; ++kk) {
-        const int k = q * S.chunk_k + kk;
-        const double v = (r < n && k < n) ? m[(size_t)r * n + k] : 0.0;
+        const double v = a(r, q * S.chunk_k + kk);
         const float h = tf32((float)v);
         const float l = tf32((float)(v - (double)h));  // the tensor core would truncate an unrounded remainder
         const size_t off = (size_t)(r >> 3) * (S.sbo_a / 4) + (size_t)(kk >> 2) * 32 + (size_t)(r & 7) * 4 + (kk & 3);
@@ -939,10 +1065,46 @@ void angular_tc_images(const double* m, int n, std::vector<float>& out) {
   }
 }
 
+// One real n x n matrix (row-major FP64: out[r] = sum_k m[r][k] in[k]), zero-padded to M.
+void angular_tc_images(const double* m, int n, std::vector<float>& out) {
+  tc_images(tc_shape(n), [&](int r, int k) { return (r < n && k < n) ? m[(size_t)r * n + k] : 0.0; }, out);
+}
+
+// Parity structure of a lane matrix for the split form (n = 256 only):
+//   1  m[l][n-1-j] = (-1)^l m[l][j]  (e.g. the Legendre transform T[l][j] = sqrt(l+1/2) P_l(x_j) w_j
+//      on symmetric nodes): out[2a + h] = sum_{j < n/2} m[2a + h][j] (in[j] +- in[n-1-j])
+//   2  m[n-1-j][l] = (-1)^l m[j][l]  (its inverse P_l(x_j) sqrt(l+1/2)): with E_j / O_j the
+//      sums over even / odd l, out[j] = E_j + O_j and out[n-1-j] = E_j - O_j
+//   0  neither (to 1e-12 of the largest entry)
+int angular_tc_parity(const double* m, int n) {
+  if (n != 256) return 0;
+  double amax = 0.0;
+  for (int i = 0; i < n * n; ++i) amax = std::max(amax, std::fabs(m[i]));
+  const double tol = 1e-12 * amax;
+  bool rowp = true, colp = true;
+  for (int a = 0; a < n && (rowp || colp); ++a)
+    for (int b = 0; b < n; ++b) {
+      const double sg = (a & 1) ? -1.0 : 1.0;
+      if (rowp && std::fabs(m[(size_t)a * n + (n - 1 - b)] - sg * m[(size_t)a * n + b]) > tol) rowp = false;
+      if (colp && std::fabs(m[(size_t)(n - 1 - b) * n + a] - sg * m[(size_t)b * n + a]) > tol) colp = false;
+    }
+  return rowp ? 1 : (colp ? 2 : 0);
+}
+
+// A images of the split form: rows 0..127 the first half (even l, or E), rows 128..255
+// the second (odd l, or O), K = n / 2.
+void angular_tc_parity_images(const double* m, int n, int kind, std::vector<float>& out) {
+  const int hn = n / 2;
+  if (kind == 1)
+    tc_images(tc_shape(n, true), [&](int r, int k) { return m[(size_t)(2 * (r % hn) + r / hn) * n + k]; }, out);
+  else
+    tc_images(tc_shape(n, true), [&](int r, int k) { return m[(size_t)(r % hn) * n + 2 * k + r / hn]; }, out);
+}
+
 int angular_tc_trace_slots() { return kTraceSlots; }
 
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
-                              int error_slot, cudaStream_t s, unsigned long long* trace) {
+                              int error_slot, const int* parity, cudaStream_t s, unsigned long long* trace) {
   TcParams tp{};
   tp.trace = trace;
   tp.p = p;
@@ -950,9 +1112,10 @@ cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, 
   for (int i = 0; i < nmat; ++i) {
     tp.mat_op[i] = mat_op[i];
     tp.images[i] = images[i];
+    tp.parity[i] = parity ? parity[i] : 0;
   }
   tp.error_slot = error_slot;
-  const size_t smem = angular_tc_smem_bytes((int)p.g.n);
+  const size_t smem = angular_tc_smem_bytes((int)p.g.n, tp.parity[0] != 0);
   static bool configured = false;
   if (!configure_once((const void*)angular_tc_kernel, configured)) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;

@@ -100,11 +100,15 @@ int angular_tc_columns(int n);  // complex columns of the inner axis per CTA til
 bool angular_tc_eligible(const Geometry& g);
 // the pass's point-wise ops fit the per-tile tables of the tensor-core kernel
 bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis);
-size_t angular_tc_smem_bytes(int n);
+size_t angular_tc_smem_bytes(int n, bool par = false);
 void angular_tc_images(const double* m, int n, std::vector<float>& out);
-// trace: optional per-tile phase timestamps (angular_tc_trace_slots() per tile), nullptr: off
+// parity structure of a real n x n lane matrix (0 none, 1 row signs, 2 column signs; n = 256 only)
+int angular_tc_parity(const double* m, int n);
+void angular_tc_parity_images(const double* m, int n, int kind, std::vector<float>& out);
+// parity: per matrix 0 / 1 / 2 (all 0, or all non-zero with the split images); trace: optional
+// per-tile phase timestamps (angular_tc_trace_slots() per tile), nullptr: off
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
-                              int error_slot, cudaStream_t s, unsigned long long* trace = nullptr);
+                              int error_slot, const int* parity, cudaStream_t s, unsigned long long* trace = nullptr);
 int angular_tc_trace_slots();
 
 // Batched launches over many propagations' passes (block -> (instance, tile) by offsets)
@@ -112,7 +116,7 @@ cudaError_t launch_pass_batched(bool fp64, const PassParams* params_dev, const i
                                 int64_t blocks, int threads, size_t smem, cudaStream_t s);
 size_t tc_params_bytes();
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
-                    void* out);
+                    const int* parity, void* out);
 cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,
                                       size_t smem, cudaStream_t s);
 

@@ -313,6 +313,15 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
     angular_tc_images(md.data(), (int)n, img);
     upload(c.tc_images, img, stream);
     tc_images_by_matrix_[c.buf.ptr] = c.tc_images.as<float>();
+    // the parity-split form as well, when the matrix has the structure (Legendre pairs)
+    const int kind = angular_tc_parity(md.data(), (int)n);
+    if (kind) {
+      angular_tc_parity_images(md.data(), (int)n, kind, img);
+      upload(c.tc_par_images, img, stream);
+      tc_parity_by_matrix_[c.buf.ptr] = {kind, c.tc_par_images.as<float>()};
+    } else {
+      tc_parity_by_matrix_.erase(c.buf.ptr);
+    }
   }
   return c.buf.ptr;
 }
@@ -334,6 +343,25 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     }
   }
   if (nmat == 0 || !angular_tc_ops_fit(ops.data(), (int)ops.size(), g.sweep_axis)) return false;
+  // parity-split GEMMs when every matrix of the pass has the structure and no sum /
+  // difference matrix follows anything but an even / odd one (SO_TC_PARITY=0 turns it off)
+  int parity[2] = {0, 0};
+  const char* par_env = std::getenv("SO_TC_PARITY");
+  bool par = g.n == 256 && !(par_env && par_env[0] == '0');
+  for (int m = 0; m < nmat && par; ++m) {
+    auto it = tc_parity_by_matrix_.find(ops[mats[m]].ptr);
+    if (it == tc_parity_by_matrix_.end()) {
+      par = false;
+      break;
+    }
+    parity[m] = it->second.first;
+    if (m > 0 && parity[m] == 1 && parity[m - 1] != 2) par = false;
+  }
+  if (par) {
+    for (int m = 0; m < nmat; ++m) images[m] = tc_parity_by_matrix_[ops[mats[m]].ptr].second;
+  } else {
+    parity[0] = parity[1] = 0;
+  }
   const int bn = angular_tc_columns((int)g.n);
   g.lanes_per_tile = bn;
   g.tiles_per_outer = (int32_t)(g.inner / bn);
@@ -344,13 +372,14 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
     p.partials = partials_.as<double>();
   }
-  std::string name = "f32 tc3xtf32 axis" + std::to_string(axis) + ":";
+  std::string name = std::string(par ? "f32 tc3xtf32 parity axis" : "f32 tc3xtf32 axis") + std::to_string(axis) + ":";
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
-    // threads: the lane extent (one batched launch serves one n; the kernel's thread count is fixed)
-    RecordedPass r{RecordedPass::TensorCore, false, p, std::vector<unsigned char>(tc_params_bytes()), (int)g.n,
-                   angular_tc_smem_bytes((int)g.n), name, pass_bytes(ops, g)};
-    make_tc_params(p, mats, nmat, images, timeout_slot, r.tcp.data());
+    // threads: the lane extent and the parity mode (one batched launch serves one of each;
+    // the kernel's thread count is fixed)
+    RecordedPass r{RecordedPass::TensorCore, false, p, std::vector<unsigned char>(tc_params_bytes()),
+                   (int)g.n | (par ? 1 << 16 : 0), angular_tc_smem_bytes((int)g.n, par), name, pass_bytes(ops, g)};
+    make_tc_params(p, mats, nmat, images, timeout_slot, parity, r.tcp.data());
     recording->push_back(std::move(r));
     return true;
   }
@@ -365,7 +394,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     trace = DeviceBuffer((size_t)g.tiles * angular_tc_trace_slots() * sizeof(unsigned long long));
     cuda_check(cudaMemsetAsync(trace.ptr, 0, trace.bytes, stream), "trace clear");
   }
-  cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, stream,
+  cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, parity, stream,
                                trace_path ? trace.as<unsigned long long>() : nullptr),
              "tensor-core pass launch");
   if (trace_path) {

@@ -186,10 +186,12 @@ class Engine {
     uint64_t version;
     DeviceBuffer buf;
     bool real;
-    DeviceBuffer tc_images;  // 3xTF32 A-operand chunk images (tensor-core passes)
+    DeviceBuffer tc_images;      // 3xTF32 A-operand chunk images (tensor-core passes)
+    DeviceBuffer tc_par_images;  // the same for the parity-split form (when the matrix has it)
   };
   std::map<std::pair<const void*, int>, Cached> tables_;
   std::map<const void*, const float*> tc_images_by_matrix_;
+  std::map<const void*, std::pair<int, const float*>> tc_parity_by_matrix_;  // parity kind, split images
   bool try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& p);
   std::map<uint64_t, DeviceBuffer> weights_;
   std::map<size_t, DeviceBuffer> twiddles_;

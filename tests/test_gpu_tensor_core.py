@@ -124,3 +124,25 @@ def test_radial_angular_tf32x3_close_to_oracle(so, nr, nth):
     # FP32 state: ~2.7e-7 norm drift per step from FP32-rounded phase tables, plus the
     # tensor-core accumulation bias (larger at n = 256, where 3 accumulators share 32 K steps)
     assert abs(prop.norm() - oprop.wave_function.norm()) < (6e-5 if nth == 256 else 2.5e-5)
+
+
+def test_parity_split_legendre_pair_matches_plain_form(so, monkeypatch):
+    """n = 256 Legendre pair: the parity-split GEMMs (two K = 128 halves) give the same
+    propagation as the plain 256 x 256 form, both within FP32 accuracy of FP64."""
+    from split_operator_gb300 import workloads as W
+    out = {}
+    for flag in ("1", "0"):
+        monkeypatch.setenv("SO_TC_PARITY", flag)
+        prop, _ = W.radial_angular_2d(nr=512, nth=256, step_no=10 ** 6, precision="fp32_tf32x3")
+        prop.set_timing(True)
+        prop.steps(6)
+        names = [t[0] for t in prop.kernel_times()]
+        assert any("parity" in nm for nm in names) == (flag == "1"), names
+        out[flag] = prop.get_array()
+    ref, _ = W.radial_angular_2d(nr=512, nth=256, step_no=10 ** 6, precision="fp64")
+    ref.steps(6)
+    r = ref.get_array()
+    e_split, e_plain = rel_l2(out["1"], r), rel_l2(out["0"], r)
+    # FP32 state: about 3e-7 per step against FP64
+    assert e_split < 1e-5 and e_plain < 1e-5, (e_split, e_plain)
+    assert rel_l2(out["1"], out["0"]) < 1e-5
