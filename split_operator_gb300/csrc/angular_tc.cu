@@ -348,72 +348,94 @@ __device__ __forceinline__ void apply_col(const PassParams& p, const TileTabs& T
   }
 }
 
-// Prologue of one thread (tile column c, rows h, h + G, ...): loads, the ops before the
-// first lane matrix, and the split into the B_hi / B_lo operand images (row j goes to K
-// row j >> kshift: kshift = 1 for the even / odd halves of a parity-split matrix, whose
-// half the caller selects through bhi / blo).
-template <int NB>
-__device__ __forceinline__ void prologue_rows(const PassParams& p, const TileTabs& T, int oe, const float2* psi,
-                                              int64_t base, int c, int h, int G, int n, float* bhi, float* blo,
-                                              uint32_t sbo_b, float* acc, int kshift = 0) {
-  const int64_t rstride = (int64_t)G * p.g.inner;
-  for (int kb = h; kb < n; kb += NB * G) {
-    const int64_t ix0 = base + (int64_t)kb * p.g.inner + c;
-    float2 v[NB];
-#pragma unroll
-    for (int u = 0; u < NB; ++u) v[u] = psi[ix0 + u * rstride];
-    apply_col<NB>(p, T, 0, oe, v, kb, G, c, ix0, rstride, acc);
-#pragma unroll
-    for (int u = 0; u < NB; ++u) {
-      const int j = kb + u * G;
-      float rh, rl, ih, il;
-      tc::split_tf32(v[u].x, rh, rl);
-      tc::split_tf32(v[u].y, ih, il);
-      const uint32_t a0 = boff(2 * c, j >> kshift, sbo_b) >> 2, a1 = boff(2 * c + 1, j >> kshift, sbo_b) >> 2;
-      bhi[a0] = rh;
-      blo[a0] = rl;
-      bhi[a1] = ih;
-      blo[a1] = il;
-    }
-  }
+// tf32 hi / lo of four values as two float4 (one 16-byte core-matrix row each)
+__device__ __forceinline__ void split4(float a, float b, float c, float d, float4& hi, float4& lo) {
+  tc::split_tf32(a, hi.x, lo.x);
+  tc::split_tf32(b, hi.y, lo.y);
+  tc::split_tf32(c, hi.z, lo.z);
+  tc::split_tf32(d, hi.w, lo.w);
 }
 
-// Prologue before a sum / difference parity-split matrix (rows j and n-1-j of every
-// pair j < n/2): the ops before the first matrix on both rows, then s = a + b into the
-// first B half and d = a - b into the second, at K row j.
-template <int NB>
-__device__ __forceinline__ void prologue_pairs(const PassParams& p, const TileTabs& T, int oe, const float2* psi,
-                                               int64_t base, int c, int h, int G, int n, float* bhi, float* blo,
-                                               uint32_t bhalf_words, uint32_t sbo_b, float* acc) {
-  const int64_t rstride = (int64_t)G * p.g.inner;
-  for (int kb = h; kb < n / 2; kb += NB * G) {
-    const int64_t ia = base + (int64_t)kb * p.g.inner + c;
-    const int64_t ib = base + (int64_t)(n - 1 - kb) * p.g.inner + c;
-    float2 a[NB], b[NB];
+// Prologue with 16-byte operand stores.  Thread (column c, block a) owns the row blocks
+// RB (a + G k) .. + RB - 1, k < NK: its loads are coalesced across the warp (consecutive
+// columns of one row) and, since K is the contiguous direction of a core-matrix row, four
+// consecutive K rows of one B column are one float4.
+//   mode 0: row j -> K row j (RB = 4)
+//   mode 2: even / odd halves, row j -> half j & 1, K row j >> 1 (RB = 8)
+//   mode 1: sum / difference pairs, rows j < n/2 and n-1-j -> K row j of both halves (RB = 4)
+template <int NK, int RB, int MODE>
+__device__ __forceinline__ void prologue_vec(const PassParams& p, const TileTabs& T, int oe, const float2* psi,
+                                             int64_t base, int c, int a, int G, int n, float* bhi, float* blo,
+                                             uint32_t bhalf_words, uint32_t sbo_b, float* acc,
+                                             unsigned long long* loaded_mark) {
+  const int64_t inner = p.g.inner;
+  const int64_t bstride = (int64_t)RB * G;  // rows between a thread's row blocks
+  float2 v[RB][NK];
+  float2 w[MODE == 1 ? RB : 1][MODE == 1 ? NK : 1];  // mirrored rows n-1-j (sum / difference)
 #pragma unroll
-    for (int u = 0; u < NB; ++u) {
-      a[u] = psi[ia + u * rstride];
-      b[u] = psi[ib - u * rstride];
+  for (int r = 0; r < RB; ++r)
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const int64_t j = (int64_t)RB * a + r + bstride * k;
+      v[r][k] = psi[base + j * inner + c];
+      if constexpr (MODE == 1) w[r][k] = psi[base + (n - 1 - j) * inner + c];
     }
-    apply_col<NB>(p, T, 0, oe, a, kb, G, c, ia, rstride, acc);
-    apply_col<NB>(p, T, 0, oe, b, n - 1 - kb, -G, c, ib, -rstride, acc);
+  if (loaded_mark) {
+    // the first value consumed: every load of this thread has returned
+    float s = 0.0f;
 #pragma unroll
-    for (int u = 0; u < NB; ++u) {
-      const int j = kb + u * G;
-      const uint32_t a0 = boff(2 * c, j, sbo_b) >> 2, a1 = boff(2 * c + 1, j, sbo_b) >> 2;
-      float h0, l0;
-      tc::split_tf32(a[u].x + b[u].x, h0, l0);
-      bhi[a0] = h0;
-      blo[a0] = l0;
-      tc::split_tf32(a[u].y + b[u].y, h0, l0);
-      bhi[a1] = h0;
-      blo[a1] = l0;
-      tc::split_tf32(a[u].x - b[u].x, h0, l0);
-      bhi[bhalf_words + a0] = h0;
-      blo[bhalf_words + a0] = l0;
-      tc::split_tf32(a[u].y - b[u].y, h0, l0);
-      bhi[bhalf_words + a1] = h0;
-      blo[bhalf_words + a1] = l0;
+    for (int r = 0; r < RB; ++r)
+#pragma unroll
+      for (int k = 0; k < NK; ++k) s += v[r][k].x;
+    if (s != 12345.678f) *loaded_mark = tc::globaltimer_ns();
+  }
+#pragma unroll
+  for (int r = 0; r < RB; ++r) {
+    const int j0 = RB * a + r;
+    apply_col<NK>(p, T, 0, oe, v[r], j0, (int)bstride, c, base + (int64_t)j0 * inner + c, bstride * inner, acc);
+    if constexpr (MODE == 1)
+      apply_col<NK>(p, T, 0, oe, w[r], n - 1 - j0, -(int)bstride, c, base + (int64_t)(n - 1 - j0) * inner + c,
+                    -bstride * inner, acc);
+  }
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int j0 = RB * a + (int)bstride * k;  // first row of the block
+    float4 h, l;
+    if constexpr (MODE == 0) {
+      const uint32_t wr = boff(2 * c, j0, sbo_b) >> 2, wi = boff(2 * c + 1, j0, sbo_b) >> 2;
+      split4(v[0][k].x, v[1][k].x, v[2][k].x, v[3][k].x, h, l);
+      *reinterpret_cast<float4*>(bhi + wr) = h;
+      *reinterpret_cast<float4*>(blo + wr) = l;
+      split4(v[0][k].y, v[1][k].y, v[2][k].y, v[3][k].y, h, l);
+      *reinterpret_cast<float4*>(bhi + wi) = h;
+      *reinterpret_cast<float4*>(blo + wi) = l;
+    } else if constexpr (MODE == 2) {
+#pragma unroll
+      for (int hf = 0; hf < 2; ++hf) {
+        const uint32_t o = hf * bhalf_words;
+        const uint32_t wr = o + (boff(2 * c, j0 >> 1, sbo_b) >> 2), wi = o + (boff(2 * c + 1, j0 >> 1, sbo_b) >> 2);
+        split4(v[hf][k].x, v[2 + hf][k].x, v[4 + hf][k].x, v[6 + hf][k].x, h, l);
+        *reinterpret_cast<float4*>(bhi + wr) = h;
+        *reinterpret_cast<float4*>(blo + wr) = l;
+        split4(v[hf][k].y, v[2 + hf][k].y, v[4 + hf][k].y, v[6 + hf][k].y, h, l);
+        *reinterpret_cast<float4*>(bhi + wi) = h;
+        *reinterpret_cast<float4*>(blo + wi) = l;
+      }
+    } else {
+      const uint32_t wr = boff(2 * c, j0, sbo_b) >> 2, wi = boff(2 * c + 1, j0, sbo_b) >> 2;
+#pragma unroll
+      for (int hf = 0; hf < 2; ++hf) {
+        const float sg = hf ? -1.0f : 1.0f;
+        const uint32_t o = hf * bhalf_words;
+        split4(v[0][k].x + sg * w[0][k].x, v[1][k].x + sg * w[1][k].x, v[2][k].x + sg * w[2][k].x,
+               v[3][k].x + sg * w[3][k].x, h, l);
+        *reinterpret_cast<float4*>(bhi + o + wr) = h;
+        *reinterpret_cast<float4*>(blo + o + wr) = l;
+        split4(v[0][k].y + sg * w[0][k].y, v[1][k].y + sg * w[1][k].y, v[2][k].y + sg * w[2][k].y,
+               v[3][k].y + sg * w[3][k].y, h, l);
+        *reinterpret_cast<float4*>(bhi + o + wi) = h;
+        *reinterpret_cast<float4*>(blo + o + wi) = l;
+      }
     }
   }
 }
@@ -484,7 +506,9 @@ enum TraceSlot {
   TR_TMA = 8,     // + c: chunk c (< 8) of the tile: copy issued (TMA warp)
   TR_FULL = 16,   // + c: chunk c landed (MMA warp)
   TR_MMA = 24,    // + c: chunk c's MMAs issued and committed (MMA warp)
-  kTraceSlots = 32
+  TR_TABS = 32,   // per-tile tables built (work warps)
+  TR_LOADED = 33, // prologue values in registers (work thread 0)
+  kTraceSlots = 34
 };
 __device__ __forceinline__ void trace_mark(const TcParams& tp, int64_t tile, int slot) {
   if (tp.trace) tp.trace[tile * kTraceSlots + slot] = tc::globaltimer_ns();
@@ -741,6 +765,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             prefetch_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * sizeof(float2)));
       }
       work_sync();  // tabs complete; the previous tile's staging has been stored
+      if (tid == 0) trace_mark(tp, tile, TR_TABS);
 
       // per-thread FP32 partial sums of the norms of this tile
       float acc[kMaxRed];
@@ -748,21 +773,21 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       for (int k = 0; k < kMaxRed; ++k) acc[k] = 0.0f;
       {
         // prologue: thread = complex column c, rows h, h + G, ... (G = groups)
+        // rows per thread: n / G = 8, 16 or 32 (n / 2 / G = 16 for the sum / difference pairs)
         const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
         const int k0 = tp.parity[0];
+        const int mo = tp.mat_op[0];
+        unsigned long long* lm = (tid == 0 && tp.trace) ? tp.trace + tile * kTraceSlots + TR_LOADED : nullptr;
         if (k0 == 1)
-          prologue_pairs<16>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc);
-        else if (k0 == 2)  // G is even: every row of this thread has the parity of h
-          prologue_rows<32>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi + (h & 1) * bhw, blo + (h & 1) * bhw,
-                            L.sbo_b, acc, 1);
-        else if (n / G >= 32)
-          prologue_rows<32>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
-        else if (n / G >= 16)
-          prologue_rows<16>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
-        else if (n / G >= 8)
-          prologue_rows<8>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
+          prologue_vec<4, 4, 1>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc, lm);
+        else if (k0 == 2)
+          prologue_vec<4, 8, 2>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc, lm);
+        else if (n / G == 32)
+          prologue_vec<8, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
+        else if (n / G == 16)
+          prologue_vec<4, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
         else
-          prologue_rows<4>(p, tabs, tp.mat_op[0], psi, base, c, h, G, n, bhi, blo, L.sbo_b, acc);
+          prologue_vec<2, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
         fence_proxy_async();
         mbar_arrive(bready);
       }
