@@ -43,15 +43,16 @@ namespace so {
 namespace {
 
 constexpr int kChunkBytes = 8192;   // one of hi / lo: 128 rows x 16 K or 256 rows x 8 K
-constexpr int kStages = 4;          // A chunk stages (16 KB each) in flight per CTA
+constexpr int kStages = 2;          // A chunk stages (16 KB each) in flight per CTA
 constexpr int kLboB = 144;          // B: core matrices along K (16 B padding vs 128)
 constexpr uint64_t kWaitLimit = 2000000000ull;  // 2 s per wait
 constexpr int kWorkThreads = 256;               // warps 0-7
 constexpr int kThreads = kWorkThreads + 64;     // + warp 8 (TMA) + warp 9 (MMA)
-constexpr uint32_t kTmemCols = 512;  // all of the SM's tensor memory: one CTA per SM
-constexpr int kRegions = 4;          // 128-column accumulator regions in kTmemCols
+constexpr uint32_t kTmemCols = 256;  // half of the SM's tensor memory: two CTAs per SM
+constexpr int kRegions = 4;          // 64-column accumulator regions in kTmemCols
 constexpr int kFillSteps = 6;        // K steps between two drains of the main regions
-constexpr int kVals = 64;            // FP32 accumulator columns a work thread drains
+constexpr int kVals = 32;            // FP32 accumulator columns a work thread drains
+constexpr int kCtasPerSm = 2;        // persistent CTAs per SM (each one's memory latency hides behind the other)
 constexpr int kColtSlots = 4;        // DIAG1D ops on a non-lane axis per pass
 
 struct TcShape {
@@ -85,7 +86,7 @@ __host__ __device__ inline TcShape tc_shape(int n, bool par = false) {
   TcShape s{};
   s.par = par && n == 256;
   s.mh = n == 256 ? 2 : 1;
-  s.bn = n == 256 ? 32 : 64;
+  s.bn = n == 256 ? 16 : 32;
   s.nc = 2 * s.bn;
   s.chunk_k = 16 / s.mh;
   s.kdim = s.par ? n / 2 : n;
@@ -198,8 +199,8 @@ __device__ __forceinline__ int64_t coord_of(const Geometry& g, int a, int64_t o,
 // Per-tile factors of the point-wise ops, built once per tile (by the work warps) so that the per-point
 // work reads shared memory and does FP32 arithmetic only (FP64 runs on a narrow pipe).
 struct TileTabs {
-  float colw[kMaxRed][64];      // NORM: product of the FP32 weights of every non-lane axis, per tile column
-  float2 colt[kColtSlots][64];  // DIAG1D on a non-lane axis: the table value of each tile column
+  float colw[kMaxRed][32];      // NORM: product of the FP32 weights of every non-lane axis, per tile column
+  float2 colt[kColtSlots][32];  // DIAG1D on a non-lane axis: the table value of each tile column
   float scale[kMaxOps];         // SCALE: sqrt(target / norm)
   int8_t slot[kMaxOps];         // DIAG1D on a non-lane axis: its colt row
 };
@@ -508,7 +509,8 @@ enum TraceSlot {
   TR_MMA = 24,    // + c: chunk c's MMAs issued and committed (MMA warp)
   TR_TABS = 32,   // per-tile tables built (work warps)
   TR_LOADED = 33, // prologue values in registers (work thread 0)
-  kTraceSlots = 34
+  TR_STORED = 34, // prologue operand stores issued (work thread 0)
+  kTraceSlots = 35
 };
 __device__ __forceinline__ void trace_mark(const TcParams& tp, int64_t tile, int slot) {
   if (tp.trace) tp.trace[tile * kTraceSlots + slot] = tc::globaltimer_ns();
@@ -550,7 +552,7 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
       for (int q = 0; q < S.nk; ++q) {
         const int s = (int)(cc % kStages);
         const uint32_t use = (uint32_t)(cc / kStages);
-        if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1u, kWaitLimit)) {
+        if (use > 0 && !mbar_poll(&empty[s], (use - 1) & 1u, kWaitLimit)) {
           ok = false;
           break;
         }
@@ -567,7 +569,7 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
     *fail = 1;
     // let the copies in flight land before the CTA lets go of its shared memory
     for (int64_t c = cc - kStages < 0 ? 0 : cc - kStages; c < cc; ++c)
-      mbar_wait(&full[c % kStages], (uint32_t)((c / kStages) & 1), kWaitLimit);
+      mbar_poll(&full[c % kStages], (uint32_t)((c / kStages) & 1), kWaitLimit);
   }
 }
 
@@ -602,12 +604,12 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
     unsigned long long* trace = tr.prm->trace ? tr.prm->trace + tr.tile * kTraceSlots : nullptr;
     const int64_t cc_tile = cc;  // first chunk of this tile
     for (int m = 0; m < nmat && ok; ++m) {
-      ok = mbar_wait(bready, nready & 1u, kWaitLimit);
+      ok = mbar_poll(bready, nready & 1u, kWaitLimit);
       ++nready;
       tc_fence_after();
       for (int f = 0; f < S.fills && ok; ++f) {
         if (f > 0) {
-          ok = mbar_wait(freebar, nfree & 1u, kWaitLimit);
+          ok = mbar_poll(freebar, nfree & 1u, kWaitLimit);
           ++nfree;
           tc_fence_after();
           if (!ok) break;
@@ -627,7 +629,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
           const int ks = t & (kpc - 1);  // kpc is 1 or 2
           if (ks == 0) {
             s = (int)(cc % kStages);
-            ok = mbar_wait(&full[s], (uint32_t)((cc / kStages) & 1), kWaitLimit);
+            ok = mbar_poll(&full[s], (uint32_t)((cc / kStages) & 1), kWaitLimit);
             if (!ok) break;
             if (trace && (int)(cc - cc_tile) < 8) trace[TR_FULL + (int)(cc - cc_tile)] = globaltimer_ns();
             tc_fence_after();
@@ -666,7 +668,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
     *fail = 1;
     // every MMA already issued completes before the tensor memory is released
     mma_commit(quiet);
-    mbar_wait(quiet, 0u, kWaitLimit);
+    mbar_poll(quiet, 0u, kWaitLimit);
   }
 }
 
@@ -729,8 +731,9 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
     // of N = 128, n = 256 the second 128-row half (its N = 64 columns).  Parity split,
     // sum / difference matrix: as plain, the row of half h lane i being 2 i + h.  Even /
     // odd matrix: columns 16 up .. 16 up + 15 of both halves (E, O), rows i and n-1-i.
-    const int c0 = S.mh == 2 ? 0 : 32 * up;  // complex column of v[0..1] (plain)
+    const int c0 = S.mh == 2 ? 0 : (kVals / 2) * up;  // complex column of v[0..1] (plain)
     const uint32_t lane_base = tmem + ((uint32_t)(lg * 32) << 16);
+    constexpr int kLd = kVals / 32;  // 16-column loads per half of a thread's columns (even / odd form)
     const uint32_t bhw = L.bhalf / 4;  // words between the two B halves
     float* stg = bhi;  // output staging reuses the B_hi area once the last GEMM is done
     uint32_t drains = 0;
@@ -764,6 +767,16 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
           for (int jj = tid; jj < n; jj += kWorkThreads)
             prefetch_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * sizeof(float2)));
       }
+      // the next tile's state rows toward L2 (its prologue loads then hit L2)
+      if (gt + gridDim.x < total) {
+        const TileRef rn = resolve(gt + gridDim.x);
+        const Geometry& gn = rn.prm->p.g;
+        const int64_t on = rn.tile / gn.tiles_per_outer;
+        const float2* pn = reinterpret_cast<const float2*>(rn.prm->p.psi) + on * gn.n * gn.inner +
+                           (rn.tile - on * gn.tiles_per_outer) * S.bn;
+        for (int jj = tid; jj < n; jj += kWorkThreads)
+          prefetch_l2(pn + (int64_t)jj * gn.inner, (uint32_t)(S.bn * sizeof(float2)));
+      }
       work_sync();  // tabs complete; the previous tile's staging has been stored
       if (tid == 0) trace_mark(tp, tile, TR_TABS);
 
@@ -773,21 +786,22 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       for (int k = 0; k < kMaxRed; ++k) acc[k] = 0.0f;
       {
         // prologue: thread = complex column c, rows h, h + G, ... (G = groups)
-        // rows per thread: n / G = 8, 16 or 32 (n / 2 / G = 16 for the sum / difference pairs)
+        // rows per thread: n / G = 4, 8 or 16 (n / 2 / G = 8 for the sum / difference pairs)
         const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
         const int k0 = tp.parity[0];
         const int mo = tp.mat_op[0];
         unsigned long long* lm = (tid == 0 && tp.trace) ? tp.trace + tile * kTraceSlots + TR_LOADED : nullptr;
         if (k0 == 1)
-          prologue_vec<4, 4, 1>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc, lm);
+          prologue_vec<2, 4, 1>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc, lm);
         else if (k0 == 2)
-          prologue_vec<4, 8, 2>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc, lm);
-        else if (n / G == 32)
-          prologue_vec<8, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
+          prologue_vec<2, 8, 2>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc, lm);
         else if (n / G == 16)
           prologue_vec<4, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
-        else
+        else if (n / G == 8)
           prologue_vec<2, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
+        else
+          prologue_vec<1, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
+        if (tid == 0) trace_mark(tp, tile, TR_STORED);
         fence_proxy_async();
         mbar_arrive(bready);
       }
@@ -827,8 +841,8 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             const int rg = k < fs.nused ? k : S.nmain;
 #pragma unroll
             for (int hv = 0; hv < kVals / 16; ++hv) {
-              const uint32_t col = kind == 2 ? (uint32_t)((hv >> 1) * S.nc + 32 * up + 16 * (hv & 1))
-                                             : (uint32_t)(64 * up + 16 * hv);
+              const uint32_t col = kind == 2 ? (uint32_t)((hv / kLd) * S.nc + (kVals / 2) * up + 16 * (hv % kLd))
+                                             : (uint32_t)(kVals * up + 16 * hv);
               float w2[16];
               tmem_ld16(lane_base + (uint32_t)(rg * S.reg_cols) + col, w2);
 #pragma unroll
@@ -863,7 +877,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
           }
         } else {
           // even / odd matrix: psi_i = E + O, psi_{n-1-i} = E - O
-          const int cc0 = 16 * up, ja = i, jb = n - 1 - i;
+          const int cc0 = (kVals / 4) * up, ja = i, jb = n - 1 - i;
           float2 xa[kVals / 4], xb[kVals / 4];
 #pragma unroll
           for (int u = 0; u < kVals / 4; ++u) {
@@ -958,7 +972,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
-__global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_constant__ TcParams tp) {
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel(const __grid_constant__ TcParams tp) {
   const TcParams* prm = &tp;
   tc_persistent([prm](int64_t t) { return TileRef{prm, t}; }, tp.p.g.tiles);
 }
@@ -966,7 +980,7 @@ __global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel(const __grid_co
 // Many propagations' lane-matrix passes in one launch (all with the same lane extent):
 // global tile b is tile (b - offsets[i]) of params[i], offsets[i] <= b < offsets[i + 1];
 // offsets[count] is the total.
-__global__ void __launch_bounds__(kThreads, 1) angular_tc_kernel_batched(const TcParams* __restrict__ params,
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel_batched(const TcParams* __restrict__ params,
                                                                         const int64_t* __restrict__ offsets,
                                                                         int count) {
   auto resolve = [params, offsets, count](int64_t b) {
@@ -1034,7 +1048,8 @@ static unsigned persistent_grid(int64_t tiles) {
                                                   cudaSuccess)
       sms = 1;
   }
-  return (unsigned)(tiles < sms ? tiles : sms);
+  const int64_t slots = (int64_t)sms * kCtasPerSm;
+  return (unsigned)(tiles < slots ? tiles : slots);
 }
 
 cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,

@@ -50,6 +50,30 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
   return t;
 }
 
+// try_wait without a suspend hint: returns promptly (the single issuing lanes poll with it,
+// so they see a completed phase without a wake-up delay)
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded polling wait for a single lane: false after `limit_ns` without completion.
+__device__ __forceinline__ bool mbar_poll(uint64_t* bar, uint32_t phase, uint64_t limit_ns) {
+  if (mbar_test(bar, phase)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  while (true) {
+    if (mbar_test(bar, phase)) return true;
+    if (globaltimer_ns() - t0 > limit_ns) return false;
+  }
+}
+
 // Bounded wait: false when `limit_ns` nanoseconds passed without the phase completing.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint64_t limit_ns) {
   if (mbar_try_wait(bar, phase)) return true;

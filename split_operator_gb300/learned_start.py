@@ -100,12 +100,19 @@ def relax(props, every=20, max_steps=20000, tol=None, target=None, group=512):
     steps = np.zeros(n, dtype=np.int64)
     done = np.zeros(n, dtype=bool)
     t0 = time.perf_counter()
+    batches = []  # (member indices, Batch); rebuilt when a quarter of its members finished
     while not done.all():
         active = [i for i in range(n) if not done[i]]
-        for s in range(0, len(active), group):
-            idx = active[s:s + group]
-            so.Batch([props[i] for i in idx]).steps(every)
+        live = sum(len([i for i in idx if not done[i]]) for idx, _ in batches)
+        members = sum(len(idx) for idx, _ in batches)
+        if not batches or live < 0.75 * members:
+            batches = [(active[s:s + group], so.Batch([props[i] for i in active[s:s + group]]))
+                       for s in range(0, len(active), group)]
+        for idx, b in batches:
+            b.steps(every)  # finished members of a batch keep stepping until it is rebuilt
             for i in idx:
+                if done[i]:
+                    continue
                 steps[i] += every + 1  # mean_energy runs one more step
                 e = props[i].mean_energy()
                 energy[i] = e
