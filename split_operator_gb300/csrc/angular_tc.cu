@@ -57,6 +57,8 @@ constexpr int kColtSlots = 4;        // DIAG1D ops on a non-lane axis per pass
 
 struct TcShape {
   bool par;      // parity-split lane matrices (two K = n/2 GEMMs, one per M half)
+  int kc;        // K values per 16-byte core-matrix row (4 tf32, 8 bf16)
+  int km;        // K per MMA instruction (8 tf32, 16 bf16)
   int kdim;      // K of each GEMM: n, or n / 2 with par
   int mh;        // 128-row halves of M
   int bn;        // complex columns per tile
@@ -81,21 +83,26 @@ struct TcShape {
 //   n <= 128: M = 128, BN = 32 (N = 64), A chunks of K = 16
 //   n = 256 : M = 256 as two 128-row halves, BN = 16 (N = 32), A chunks of K = 8
 // par: the two lane matrices split by parity into two half-size GEMMs (n = 256 only):
-// K = n / 2, the 128-row halves of M are the even and odd parts, each with its own B
-__host__ __device__ inline TcShape tc_shape(int n, bool par = false) {
+// K = n / 2, the 128-row halves of M are the even and odd parts, each with its own B.
+// bf: split-BF16x3 operands (2-byte elements, 8 K values per 16-byte core-matrix row,
+// K = 16 per instruction) instead of 3xTF32 (4-byte, 4 per row, K = 8); in bytes the
+// chunk, core-matrix and descriptor steps are the same.
+__host__ __device__ inline TcShape tc_shape(int n, bool par = false, bool bf = false) {
   TcShape s{};
   s.par = par && n == 256;
+  s.kc = bf ? 8 : 4;
+  s.km = bf ? 16 : 8;
   s.mh = n == 256 ? 2 : 1;
   s.bn = n == 256 ? 16 : 32;
   s.nc = 2 * s.bn;
-  s.chunk_k = 16 / s.mh;
+  s.chunk_k = (bf ? 32 : 16) / s.mh;
   s.kdim = s.par ? n / 2 : n;
   s.nk = s.kdim / s.chunk_k;
-  s.ksteps = s.kdim / 8;
+  s.ksteps = s.kdim / s.km;
   s.reg_cols = s.nc * s.mh;
   s.nmain = kRegions - 1;
   s.fills = (s.ksteps + kFillSteps - 1) / kFillSteps;
-  s.sbo_a = (s.chunk_k / 4) * 128;
+  s.sbo_a = (s.chunk_k / s.kc) * 128;
   s.a_half16 = (16 * s.sbo_a) >> 4;
   s.stage_row = s.nc + 4;
   s.groups = kWorkThreads / s.bn;
@@ -109,10 +116,10 @@ struct TcSmemLayout {
 // [kStages x 16 KB A stages][B_hi][B_lo][mbarriers: full[kStages], empty[kStages], dbar,
 // freebar, bready, quiet].  With par each of B_hi / B_lo holds two K = n/2 operands,
 // bhalf bytes apart (the even / odd or sum / difference halves).
-__host__ __device__ inline TcSmemLayout tc_layout(int n, bool par = false) {
-  const TcShape s = tc_shape(n, par);
+__host__ __device__ inline TcSmemLayout tc_layout(int n, bool par = false, bool bf = false) {
+  const TcShape s = tc_shape(n, par, bf);
   TcSmemLayout L{};
-  L.sbo_b = (uint32_t)(s.kdim / 4) * kLboB + 16;
+  L.sbo_b = (uint32_t)(s.kdim / s.kc) * kLboB + 16;
   L.bhalf = (uint32_t)(s.nc / 8) * L.sbo_b;
   L.bbytes = (s.par ? 2u : 1u) * L.bhalf;
   L.bbytes = (L.bbytes + 127u) & ~127u;
@@ -124,8 +131,11 @@ __host__ __device__ inline TcSmemLayout tc_layout(int n, bool par = false) {
   return L;
 }
 
+// byte offset of B operand element (column q, K row k) in the K-major core-matrix layout
+template <bool BF>
 __device__ __forceinline__ uint32_t boff(int q, int k, uint32_t sbo) {
-  return (uint32_t)(q >> 3) * sbo + (uint32_t)(k >> 2) * kLboB + (uint32_t)(q & 7) * 16u + (uint32_t)(k & 3) * 4u;
+  constexpr int kc = BF ? 8 : 4, es = BF ? 2 : 4;
+  return (uint32_t)(q >> 3) * sbo + (uint32_t)(k / kc) * kLboB + (uint32_t)(q & 7) * 16u + (uint32_t)(k % kc) * es;
 }
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
@@ -349,25 +359,58 @@ __device__ __forceinline__ void apply_col(const PassParams& p, const TileTabs& T
   }
 }
 
-// tf32 hi / lo of four values as two float4 (one 16-byte core-matrix row each)
-__device__ __forceinline__ void split4(float a, float b, float c, float d, float4& hi, float4& lo) {
-  tc::split_tf32(a, hi.x, lo.x);
-  tc::split_tf32(b, hi.y, lo.y);
-  tc::split_tf32(c, hi.z, lo.z);
-  tc::split_tf32(d, hi.w, lo.w);
+// hi / lo operand parts of four consecutive K values of one B column, stored at byte
+// offset `off` of the hi and lo images: two 16-byte rows (tf32) or two 8-byte halves of
+// rows (bf16)
+template <bool BF>
+__device__ __forceinline__ void store4(unsigned char* bh, unsigned char* bl, uint32_t off, float a, float b, float c,
+                                       float d) {
+  if constexpr (BF) {
+    uint16_t h[4], l[4];
+    tc::split_bf16(a, h[0], l[0]);
+    tc::split_bf16(b, h[1], l[1]);
+    tc::split_bf16(c, h[2], l[2]);
+    tc::split_bf16(d, h[3], l[3]);
+    *reinterpret_cast<uint2*>(bh + off) = make_uint2(h[0] | (uint32_t)h[1] << 16, h[2] | (uint32_t)h[3] << 16);
+    *reinterpret_cast<uint2*>(bl + off) = make_uint2(l[0] | (uint32_t)l[1] << 16, l[2] | (uint32_t)l[3] << 16);
+  } else {
+    float4 h, l;
+    tc::split_tf32(a, h.x, l.x);
+    tc::split_tf32(b, h.y, l.y);
+    tc::split_tf32(c, h.z, l.z);
+    tc::split_tf32(d, h.w, l.w);
+    *reinterpret_cast<float4*>(bh + off) = h;
+    *reinterpret_cast<float4*>(bl + off) = l;
+  }
 }
 
-// Prologue with 16-byte operand stores.  Thread (column c, block a) owns the row blocks
+// one operand element: hi / lo parts at byte offset `off`
+template <bool BF>
+__device__ __forceinline__ void store1(unsigned char* bh, unsigned char* bl, uint32_t off, float x) {
+  if constexpr (BF) {
+    uint16_t h, l;
+    tc::split_bf16(x, h, l);
+    *reinterpret_cast<uint16_t*>(bh + off) = h;
+    *reinterpret_cast<uint16_t*>(bl + off) = l;
+  } else {
+    float h, l;
+    tc::split_tf32(x, h, l);
+    *reinterpret_cast<float*>(bh + off) = h;
+    *reinterpret_cast<float*>(bl + off) = l;
+  }
+}
+
+// Prologue with vector operand stores.  Thread (column c, block a) owns the row blocks
 // RB (a + G k) .. + RB - 1, k < NK: its loads are coalesced across the warp (consecutive
 // columns of one row) and, since K is the contiguous direction of a core-matrix row, four
-// consecutive K rows of one B column are one float4.
+// consecutive K rows of one B column are one vector store.
 //   mode 0: row j -> K row j (RB = 4)
 //   mode 2: even / odd halves, row j -> half j & 1, K row j >> 1 (RB = 8)
 //   mode 1: sum / difference pairs, rows j < n/2 and n-1-j -> K row j of both halves (RB = 4)
-template <int NK, int RB, int MODE>
+template <int NK, int RB, int MODE, bool BF>
 __device__ __forceinline__ void prologue_vec(const PassParams& p, const TileTabs& T, int oe, const float2* psi,
-                                             int64_t base, int c, int a, int G, int n, float* bhi, float* blo,
-                                             uint32_t bhalf_words, uint32_t sbo_b, float* acc,
+                                             int64_t base, int c, int a, int G, int n, unsigned char* bh,
+                                             unsigned char* bl, uint32_t bhalf, uint32_t sbo_b, float* acc,
                                              unsigned long long* loaded_mark) {
   const int64_t inner = p.g.inner;
   const int64_t bstride = (int64_t)RB * G;  // rows between a thread's row blocks
@@ -401,63 +444,45 @@ __device__ __forceinline__ void prologue_vec(const PassParams& p, const TileTabs
 #pragma unroll
   for (int k = 0; k < NK; ++k) {
     const int j0 = RB * a + (int)bstride * k;  // first row of the block
-    float4 h, l;
     if constexpr (MODE == 0) {
-      const uint32_t wr = boff(2 * c, j0, sbo_b) >> 2, wi = boff(2 * c + 1, j0, sbo_b) >> 2;
-      split4(v[0][k].x, v[1][k].x, v[2][k].x, v[3][k].x, h, l);
-      *reinterpret_cast<float4*>(bhi + wr) = h;
-      *reinterpret_cast<float4*>(blo + wr) = l;
-      split4(v[0][k].y, v[1][k].y, v[2][k].y, v[3][k].y, h, l);
-      *reinterpret_cast<float4*>(bhi + wi) = h;
-      *reinterpret_cast<float4*>(blo + wi) = l;
+      const uint32_t orr = boff<BF>(2 * c, j0, sbo_b), oim = boff<BF>(2 * c + 1, j0, sbo_b);
+      store4<BF>(bh, bl, orr, v[0][k].x, v[1][k].x, v[2][k].x, v[3][k].x);
+      store4<BF>(bh, bl, oim, v[0][k].y, v[1][k].y, v[2][k].y, v[3][k].y);
     } else if constexpr (MODE == 2) {
 #pragma unroll
       for (int hf = 0; hf < 2; ++hf) {
-        const uint32_t o = hf * bhalf_words;
-        const uint32_t wr = o + (boff(2 * c, j0 >> 1, sbo_b) >> 2), wi = o + (boff(2 * c + 1, j0 >> 1, sbo_b) >> 2);
-        split4(v[hf][k].x, v[2 + hf][k].x, v[4 + hf][k].x, v[6 + hf][k].x, h, l);
-        *reinterpret_cast<float4*>(bhi + wr) = h;
-        *reinterpret_cast<float4*>(blo + wr) = l;
-        split4(v[hf][k].y, v[2 + hf][k].y, v[4 + hf][k].y, v[6 + hf][k].y, h, l);
-        *reinterpret_cast<float4*>(bhi + wi) = h;
-        *reinterpret_cast<float4*>(blo + wi) = l;
+        const uint32_t o = hf * bhalf;
+        const uint32_t orr = o + boff<BF>(2 * c, j0 >> 1, sbo_b), oim = o + boff<BF>(2 * c + 1, j0 >> 1, sbo_b);
+        store4<BF>(bh, bl, orr, v[hf][k].x, v[2 + hf][k].x, v[4 + hf][k].x, v[6 + hf][k].x);
+        store4<BF>(bh, bl, oim, v[hf][k].y, v[2 + hf][k].y, v[4 + hf][k].y, v[6 + hf][k].y);
       }
     } else {
-      const uint32_t wr = boff(2 * c, j0, sbo_b) >> 2, wi = boff(2 * c + 1, j0, sbo_b) >> 2;
+      const uint32_t orr = boff<BF>(2 * c, j0, sbo_b), oim = boff<BF>(2 * c + 1, j0, sbo_b);
 #pragma unroll
       for (int hf = 0; hf < 2; ++hf) {
         const float sg = hf ? -1.0f : 1.0f;
-        const uint32_t o = hf * bhalf_words;
-        split4(v[0][k].x + sg * w[0][k].x, v[1][k].x + sg * w[1][k].x, v[2][k].x + sg * w[2][k].x,
-               v[3][k].x + sg * w[3][k].x, h, l);
-        *reinterpret_cast<float4*>(bhi + o + wr) = h;
-        *reinterpret_cast<float4*>(blo + o + wr) = l;
-        split4(v[0][k].y + sg * w[0][k].y, v[1][k].y + sg * w[1][k].y, v[2][k].y + sg * w[2][k].y,
-               v[3][k].y + sg * w[3][k].y, h, l);
-        *reinterpret_cast<float4*>(bhi + o + wi) = h;
-        *reinterpret_cast<float4*>(blo + o + wi) = l;
+        const uint32_t o = hf * bhalf;
+        store4<BF>(bh, bl, o + orr, v[0][k].x + sg * w[0][k].x, v[1][k].x + sg * w[1][k].x,
+                   v[2][k].x + sg * w[2][k].x, v[3][k].x + sg * w[3][k].x);
+        store4<BF>(bh, bl, o + oim, v[0][k].y + sg * w[0][k].y, v[1][k].y + sg * w[1][k].y,
+                   v[2][k].y + sg * w[2][k].y, v[3][k].y + sg * w[3][k].y);
       }
     }
   }
 }
 
 // B operand row of NV complex values: columns c0 .. c0 + NV - 1 (c0 a multiple of 8) at K
-// row k, split into tf32 hi / lo
-template <int NV>
-__device__ __forceinline__ void write_b_row(const float2 (&x)[NV], int c0, int k, float* bhi, float* blo,
-                                            uint32_t sbo_b) {
-  // column q = 2 (c0 + u) (+1): core-matrix group c0 / 4 + u / 4, row 2 (u % 4) (+1)
-  const uint32_t w0 = boff(2 * c0, k, sbo_b) >> 2;
+// row k.  Column q = 2 (c0 + u) (+1) sits in core-matrix group c0 / 4 + u / 4, row 2 (u % 4)
+// (+1): byte offsets (u / 4) sbo + (u % 4) 32 (+16) from that of q = 2 c0.
+template <int NV, bool BF>
+__device__ __forceinline__ void write_b_row(const float2 (&x)[NV], int c0, int k, unsigned char* bh,
+                                            unsigned char* bl, uint32_t sbo_b) {
+  const uint32_t o0 = boff<BF>(2 * c0, k, sbo_b);
 #pragma unroll
   for (int u = 0; u < NV; ++u) {
-    const uint32_t w = w0 + (uint32_t)(u >> 2) * (sbo_b >> 2) + (uint32_t)(u & 3) * 8u;
-    float h0, l0;
-    tc::split_tf32(x[u].x, h0, l0);
-    bhi[w] = h0;
-    blo[w] = l0;
-    tc::split_tf32(x[u].y, h0, l0);
-    bhi[w + 4] = h0;
-    blo[w + 4] = l0;
+    const uint32_t o = o0 + (uint32_t)(u >> 2) * sbo_b + (uint32_t)(u & 3) * 32u;
+    store1<BF>(bh, bl, o, x[u].x);
+    store1<BF>(bh, bl, o + 16, x[u].y);
   }
 }
 
@@ -578,7 +603,7 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
 // (t - t0) nused / span and both corrections into the correction region -- then a
 // commit of the fill to dbar.  Each chunk's MMAs are committed to its stage's empty
 // barrier, which the TMA warp waits on before refilling the stage.
-template <typename Resolve>
+template <bool BF, typename Resolve>
 __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const TcShape S, uint32_t sm0,
                                         const TcSmemLayout L, uint32_t tmem, volatile int* fail) {
   using namespace tc;
@@ -589,9 +614,9 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
   uint64_t* bready = dbar + 2;
   uint64_t* quiet = dbar + 3;
   const uint32_t stage_bytes = 2u * kChunkBytes;
-  const uint32_t idesc = idesc_tf32(128, (uint32_t)S.nc);
+  const uint32_t idesc = BF ? idesc_bf16(128, (uint32_t)S.nc) : idesc_tf32(128, (uint32_t)S.nc);
   const uint64_t bbits = smem_desc_bits(kLboB, L.sbo_b), abits = smem_desc_bits(128, (uint32_t)S.sbo_a);
-  const int kpc = S.chunk_k / 8;  // K steps per chunk
+  const int kpc = S.chunk_k / S.km;  // K steps per chunk
   const uint64_t bstep_half = S.par ? (uint64_t)(L.bhalf >> 4) : 0u;
   int64_t cc = 0;                 // chunks consumed
   int s = 0;                      // stage of the chunk being consumed
@@ -640,9 +665,15 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
           for (int hh = 0; hh < S.mh; ++hh) {
             const uint64_t ah = ahi + (uint64_t)(hh * S.a_half16);
             const uint64_t bo = (uint64_t)hh * bstep_half;  // parity split: each half its own B
-            mma_tf32(dm0 + (uint32_t)(hh * S.nc), ah, bh + bo, idesc, first_main);
-            mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah, bl + bo, idesc, first_corr);
-            mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(kChunkBytes >> 4), bh + bo, idesc, 1u);
+            if constexpr (BF) {
+              mma_bf16(dm0 + (uint32_t)(hh * S.nc), ah, bh + bo, idesc, first_main);
+              mma_bf16(dc0 + (uint32_t)(hh * S.nc), ah, bl + bo, idesc, first_corr);
+              mma_bf16(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(kChunkBytes >> 4), bh + bo, idesc, 1u);
+            } else {
+              mma_tf32(dm0 + (uint32_t)(hh * S.nc), ah, bh + bo, idesc, first_main);
+              mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah, bl + bo, idesc, first_corr);
+              mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(kChunkBytes >> 4), bh + bo, idesc, 1u);
+            }
           }
           bh += (uint64_t)(2 * kLboB >> 4);
           bl += (uint64_t)(2 * kLboB >> 4);
@@ -674,7 +705,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
 
 // The tiles blockIdx.x, blockIdx.x + gridDim.x, ... of a launch (every tile of a launch
 // has the same lane extent n).
-template <typename Resolve>
+template <bool BF, typename Resolve>
 __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t total) {
   using namespace tc;
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -692,14 +723,15 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   const TcParams* first = resolve(blockIdx.x).prm;  // every tile of a launch shares n and parity mode
   const int n = (int)first->p.g.n;
   const bool par = first->parity[0] != 0;
-  const TcShape S = tc_shape(n, par);
-  const TcSmemLayout L = tc_layout(n, par);
+  const TcShape S = tc_shape(n, par, BF);
+  const TcSmemLayout L = tc_layout(n, par, BF);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars);
   uint64_t* dbar = bars + 2 * kStages;  // MMAs of a fill completed (the work warps drain)
   uint64_t* freebar = dbar + 1;         // the work warps drained a fill (regions free again)
   uint64_t* bready = dbar + 2;          // the B operand of the next matrix is written
-  float* bhi = reinterpret_cast<float*>(sm + L.bhi);
-  float* blo = reinterpret_cast<float*>(sm + L.blo);
+  float* bhi = reinterpret_cast<float*>(sm + L.bhi);  // also the FP32 output staging
+  unsigned char* bhb = sm + L.bhi;                    // B operand images (hi, lo)
+  unsigned char* blb = sm + L.blo;
 
   if (tid == 0) {
     for (int k = 0; k < 2 * kStages; ++k) mbar_init(bars + k, 1);  // full[], empty[]
@@ -720,7 +752,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   if (warp == kWorkThreads / 32) {
     if (lane == 0) tma_producer(resolve, total, S, sm0, L, &s_fail);
   } else if (warp == kWorkThreads / 32 + 1) {
-    if (lane == 0) mma_issuer(resolve, total, S, sm0, L, tmem, &s_fail);
+    if (lane == 0) mma_issuer<BF>(resolve, total, S, sm0, L, tmem, &s_fail);
   } else {
     // ================= work warps
     const int lg = warp & 3, up = warp >> 2;
@@ -734,7 +766,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
     const int c0 = S.mh == 2 ? 0 : (kVals / 2) * up;  // complex column of v[0..1] (plain)
     const uint32_t lane_base = tmem + ((uint32_t)(lg * 32) << 16);
     constexpr int kLd = kVals / 32;  // 16-column loads per half of a thread's columns (even / odd form)
-    const uint32_t bhw = L.bhalf / 4;  // words between the two B halves
+    const uint32_t bhb2 = L.bhalf;  // bytes between the two B halves
     float* stg = bhi;  // output staging reuses the B_hi area once the last GEMM is done
     uint32_t drains = 0;
     const TcParams* cur = nullptr;
@@ -792,15 +824,15 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         const int mo = tp.mat_op[0];
         unsigned long long* lm = (tid == 0 && tp.trace) ? tp.trace + tile * kTraceSlots + TR_LOADED : nullptr;
         if (k0 == 1)
-          prologue_vec<2, 4, 1>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc, lm);
+          prologue_vec<2, 4, 1, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, bhb2, L.sbo_b, acc, lm);
         else if (k0 == 2)
-          prologue_vec<2, 8, 2>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, bhw, L.sbo_b, acc, lm);
+          prologue_vec<2, 8, 2, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, bhb2, L.sbo_b, acc, lm);
         else if (n / G == 16)
-          prologue_vec<4, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
+          prologue_vec<4, 4, 0, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, 0, L.sbo_b, acc, lm);
         else if (n / G == 8)
-          prologue_vec<2, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
+          prologue_vec<2, 4, 0, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, 0, L.sbo_b, acc, lm);
         else
-          prologue_vec<1, 4, 0>(p, tabs, mo, psi, base, c, h, G, n, bhi, blo, 0, L.sbo_b, acc, lm);
+          prologue_vec<1, 4, 0, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, 0, L.sbo_b, acc, lm);
         if (tid == 0) trace_mark(tp, tile, TR_STORED);
         fence_proxy_async();
         mbar_arrive(bready);
@@ -871,9 +903,9 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             if (last)
               stage_row<kVals / 2>(x, c0, jr, stg, S.stage_row);
             else if (next == 2)
-              write_b_row<kVals / 2>(x, c0, jr >> 1, bhi + (jr & 1) * bhw, blo + (jr & 1) * bhw, L.sbo_b);
+              write_b_row<kVals / 2, BF>(x, c0, jr >> 1, bhb + (jr & 1) * bhb2, blb + (jr & 1) * bhb2, L.sbo_b);
             else
-              write_b_row<kVals / 2>(x, c0, jr, bhi, blo, L.sbo_b);
+              write_b_row<kVals / 2, BF>(x, c0, jr, bhb, blb, L.sbo_b);
           }
         } else {
           // even / odd matrix: psi_i = E + O, psi_{n-1-i} = E - O
@@ -895,13 +927,13 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             float2 sd[kVals / 4];
 #pragma unroll
             for (int u = 0; u < kVals / 4; ++u) sd[u] = {xa[u].x + xb[u].x, xa[u].y + xb[u].y};
-            write_b_row<kVals / 4>(sd, cc0, i, bhi, blo, L.sbo_b);
+            write_b_row<kVals / 4, BF>(sd, cc0, i, bhb, blb, L.sbo_b);
 #pragma unroll
             for (int u = 0; u < kVals / 4; ++u) sd[u] = {xa[u].x - xb[u].x, xa[u].y - xb[u].y};
-            write_b_row<kVals / 4>(sd, cc0, i, bhi + bhw, blo + bhw, L.sbo_b);
+            write_b_row<kVals / 4, BF>(sd, cc0, i, bhb + bhb2, blb + bhb2, L.sbo_b);
           } else {
-            write_b_row<kVals / 4>(xa, cc0, ja >> 1, bhi + (ja & 1) * bhw, blo + (ja & 1) * bhw, L.sbo_b);
-            write_b_row<kVals / 4>(xb, cc0, jb >> 1, bhi + (jb & 1) * bhw, blo + (jb & 1) * bhw, L.sbo_b);
+            write_b_row<kVals / 4, BF>(xa, cc0, ja >> 1, bhb + (ja & 1) * bhb2, blb + (ja & 1) * bhb2, L.sbo_b);
+            write_b_row<kVals / 4, BF>(xb, cc0, jb >> 1, bhb + (jb & 1) * bhb2, blb + (jb & 1) * bhb2, L.sbo_b);
           }
         }
         if (!last) {
@@ -972,14 +1004,16 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
+template <bool BF>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel(const __grid_constant__ TcParams tp) {
   const TcParams* prm = &tp;
-  tc_persistent([prm](int64_t t) { return TileRef{prm, t}; }, tp.p.g.tiles);
+  tc_persistent<BF>([prm](int64_t t) { return TileRef{prm, t}; }, tp.p.g.tiles);
 }
 
 // Many propagations' lane-matrix passes in one launch (all with the same lane extent):
 // global tile b is tile (b - offsets[i]) of params[i], offsets[i] <= b < offsets[i + 1];
 // offsets[count] is the total.
+template <bool BF>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel_batched(const TcParams* __restrict__ params,
                                                                         const int64_t* __restrict__ offsets,
                                                                         int count) {
@@ -994,11 +1028,11 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel_batche
     }
     return TileRef{params + lo, b - offsets[lo]};
   };
-  tc_persistent(resolve, offsets[count]);
+  tc_persistent<BF>(resolve, offsets[count]);
 }
 
 // ------------------------------------------------------------------ host side
-size_t angular_tc_smem_bytes(int n, bool par) { return tc_layout(n, par).total; }
+size_t angular_tc_smem_bytes(int n, bool par, bool bf) { return tc_layout(n, par, bf).total; }
 
 int angular_tc_columns(int n) { return tc_shape(n).bn; }
 
@@ -1022,11 +1056,12 @@ void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const floa
 static size_t tc_max_dynamic_smem() {
   size_t m = 0;
   for (int n = 32; n <= 256; n *= 2)
-    for (int par = 0; par < 2; ++par) m = tc_layout(n, par).total > m ? tc_layout(n, par).total : m;
+    for (int par = 0; par < 2; ++par)
+      for (int bf = 0; bf < 2; ++bf) m = tc_layout(n, par, bf).total > m ? tc_layout(n, par, bf).total : m;
   return m;
 }
 
-// one persistent CTA per SM, with the whole shared-memory carveout
+// persistent CTAs with the whole shared-memory carveout
 static bool configure_once(const void* kern, bool& flag) {
   if (flag) return true;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_max_dynamic_smem()) !=
@@ -1053,12 +1088,16 @@ static unsigned persistent_grid(int64_t tiles) {
 }
 
 cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,
-                                      size_t smem, cudaStream_t s) {
-  static bool configured = false;
-  if (!configure_once((const void*)angular_tc_kernel_batched, configured)) return cudaGetLastError();
+                                      size_t smem, bool bf, cudaStream_t s) {
+  static bool configured[2] = {false, false};
+  const void* kern = bf ? (const void*)angular_tc_kernel_batched<true> : (const void*)angular_tc_kernel_batched<false>;
+  if (!configure_once(kern, configured[bf ? 1 : 0])) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
-  angular_tc_kernel_batched<<<persistent_grid(blocks), kThreads, smem, s>>>(
-      reinterpret_cast<const TcParams*>(params_dev), offsets_dev, count);
+  const TcParams* prm = reinterpret_cast<const TcParams*>(params_dev);
+  if (bf)
+    angular_tc_kernel_batched<true><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, offsets_dev, count);
+  else
+    angular_tc_kernel_batched<false><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, offsets_dev, count);
   count_launch();
   return cudaGetLastError();
 }
@@ -1075,11 +1114,12 @@ bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis) {
   return across <= kColtSlots;
 }
 
-// Chunk images of the 3xTF32 A operand: rows x kdim values a(r, k), per K chunk 8 KB of
-// tf32-exact high parts then 8 KB of tf32-exact remainders, each in the K-major
-// core-matrix order (row-group stride sbo_a, K core-matrix stride 128 B).
+// Chunk images of the A operand: rows x kdim values a(r, k); per K chunk 8 KB of high
+// parts then 8 KB of remainders, both exact in the operand format, each in the K-major
+// core-matrix order (row-group stride sbo_a, K core-matrix stride 128 B).  3xTF32: tf32
+// values in 4-byte words; split-BF16x3: bf16 values in 2-byte halves of the same buffer.
 template <typename F>
-static void tc_images(const TcShape& S, F a, std::vector<float>& out) {
+static void tc_images(const TcShape& S, bool bf, F a, std::vector<float>& out) {
   const int rows = 128 * S.mh;
   out.assign((size_t)S.nk * 2 * (kChunkBytes / 4), 0.0f);
   auto tf32 = [](float x) {
@@ -1090,24 +1130,45 @@ static void tc_images(const TcShape& S, F a, std::vector<float>& out) {
     std::memcpy(&r, &b, 4);
     return r;
   };
+  auto bf16 = [](float x) -> uint16_t {  // round to nearest even (finite inputs)
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    b += 0x7FFFu + ((b >> 16) & 1u);
+    return (uint16_t)(b >> 16);
+  };
+  auto bf16_value = [](uint16_t h) {
+    const uint32_t b = (uint32_t)h << 16;
+    float r;
+    std::memcpy(&r, &b, 4);
+    return r;
+  };
   for (int q = 0; q < S.nk; ++q) {
-    float* hi = out.data() + (size_t)q * 2 * (kChunkBytes / 4);
-    float* lo = hi + kChunkBytes / 4;
+    unsigned char* hi = reinterpret_cast<unsigned char*>(out.data() + (size_t)q * 2 * (kChunkBytes / 4));
+    unsigned char* lo = hi + kChunkBytes;
     for (int r = 0; r < rows; ++r)
       for (int kk = 0; kk < S.chunk_k; ++kk) {
         const double v = a(r, q * S.chunk_k + kk);
-        const float h = tf32((float)v);
-        const float l = tf32((float)(v - (double)h));  // the tensor core would truncate an unrounded remainder
-        const size_t off = (size_t)(r >> 3) * (S.sbo_a / 4) + (size_t)(kk >> 2) * 32 + (size_t)(r & 7) * 4 + (kk & 3);
-        hi[off] = h;
-        lo[off] = l;
+        const size_t off = (size_t)(r >> 3) * S.sbo_a + (size_t)(kk / S.kc) * 128 + (size_t)(r & 7) * 16 +
+                           (size_t)(kk % S.kc) * (bf ? 2 : 4);
+        if (bf) {
+          const uint16_t h = bf16((float)v);
+          const uint16_t l = bf16((float)(v - (double)bf16_value(h)));
+          std::memcpy(hi + off, &h, 2);
+          std::memcpy(lo + off, &l, 2);
+        } else {
+          const float h = tf32((float)v);
+          const float l = tf32((float)(v - (double)h));  // the tensor core would truncate an unrounded remainder
+          std::memcpy(hi + off, &h, 4);
+          std::memcpy(lo + off, &l, 4);
+        }
       }
   }
 }
 
 // One real n x n matrix (row-major FP64: out[r] = sum_k m[r][k] in[k]), zero-padded to M.
-void angular_tc_images(const double* m, int n, std::vector<float>& out) {
-  tc_images(tc_shape(n), [&](int r, int k) { return (r < n && k < n) ? m[(size_t)r * n + k] : 0.0; }, out);
+void angular_tc_images(const double* m, int n, bool bf, std::vector<float>& out) {
+  tc_images(tc_shape(n, false, bf), bf, [&](int r, int k) { return (r < n && k < n) ? m[(size_t)r * n + k] : 0.0; },
+            out);
 }
 
 // Parity structure of a lane matrix for the split form (n = 256 only):
@@ -1133,18 +1194,20 @@ int angular_tc_parity(const double* m, int n) {
 
 // A images of the split form: rows 0..127 the first half (even l, or E), rows 128..255
 // the second (odd l, or O), K = n / 2.
-void angular_tc_parity_images(const double* m, int n, int kind, std::vector<float>& out) {
+void angular_tc_parity_images(const double* m, int n, int kind, bool bf, std::vector<float>& out) {
   const int hn = n / 2;
+  const TcShape S = tc_shape(n, true, bf);
   if (kind == 1)
-    tc_images(tc_shape(n, true), [&](int r, int k) { return m[(size_t)(2 * (r % hn) + r / hn) * n + k]; }, out);
+    tc_images(S, bf, [&](int r, int k) { return m[(size_t)(2 * (r % hn) + r / hn) * n + k]; }, out);
   else
-    tc_images(tc_shape(n, true), [&](int r, int k) { return m[(size_t)(r % hn) * n + 2 * k + r / hn]; }, out);
+    tc_images(S, bf, [&](int r, int k) { return m[(size_t)(r % hn) * n + 2 * k + r / hn]; }, out);
 }
 
 int angular_tc_trace_slots() { return kTraceSlots; }
 
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
-                              int error_slot, const int* parity, cudaStream_t s, unsigned long long* trace) {
+                              int error_slot, const int* parity, bool bf, cudaStream_t s,
+                              unsigned long long* trace) {
   TcParams tp{};
   tp.trace = trace;
   tp.p = p;
@@ -1155,11 +1218,15 @@ cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, 
     tp.parity[i] = parity ? parity[i] : 0;
   }
   tp.error_slot = error_slot;
-  const size_t smem = angular_tc_smem_bytes((int)p.g.n, tp.parity[0] != 0);
-  static bool configured = false;
-  if (!configure_once((const void*)angular_tc_kernel, configured)) return cudaGetLastError();
+  const size_t smem = angular_tc_smem_bytes((int)p.g.n, tp.parity[0] != 0, bf);
+  static bool configured[2] = {false, false};
+  const void* kern = bf ? (const void*)angular_tc_kernel<true> : (const void*)angular_tc_kernel<false>;
+  if (!configure_once(kern, configured[bf ? 1 : 0])) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
-  angular_tc_kernel<<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
+  if (bf)
+    angular_tc_kernel<true><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
+  else
+    angular_tc_kernel<false><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
   count_launch();
   return cudaGetLastError();
 }

@@ -84,6 +84,7 @@ struct PassParams {
   int32_t resident;             // 1: single CTA owns the whole array, scalars are immediate
   int32_t nonfinite_slot;       // slot set to 1 if a norm is not finite
   int32_t one_buffer;           // 1: no op needs the second tile buffer (FFT stages run in place)
+  int32_t sweep;                // 1: only point-wise ops, norms, scalars and power-of-two FFTs
   DevOp ops[kMaxOps];
 };
 
@@ -92,7 +93,7 @@ cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);
 cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s);
 size_t pass_smem_bytes(const PassParams& p, bool fp64);
 int pass_threads(const Geometry& g);
-// sets p.one_buffer from the pass's ops and geometry (call once p.ops, p.nops, p.g are set)
+// sets p.one_buffer and p.sweep from the pass's ops and geometry (call once p.ops, p.nops, p.g are set)
 void pass_choose_buffers(PassParams& p, bool fp64);
 
 // Tensor-core angular sweep (angular_tc.cu): FP32 state, real lane matrices as 3xTF32.
@@ -100,25 +101,27 @@ int angular_tc_columns(int n);  // complex columns of the inner axis per CTA til
 bool angular_tc_eligible(const Geometry& g);
 // the pass's point-wise ops fit the per-tile tables of the tensor-core kernel
 bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis);
-size_t angular_tc_smem_bytes(int n, bool par = false);
-void angular_tc_images(const double* m, int n, std::vector<float>& out);
+size_t angular_tc_smem_bytes(int n, bool par = false, bool bf = false);
+// A-operand chunk images (bf: split-BF16x3 bf16 parts; else 3xTF32 tf32 parts), raw bytes in a float vector
+void angular_tc_images(const double* m, int n, bool bf, std::vector<float>& out);
 // parity structure of a real n x n lane matrix (0 none, 1 row signs, 2 column signs; n = 256 only)
 int angular_tc_parity(const double* m, int n);
-void angular_tc_parity_images(const double* m, int n, int kind, std::vector<float>& out);
+void angular_tc_parity_images(const double* m, int n, int kind, bool bf, std::vector<float>& out);
 // parity: per matrix 0 / 1 / 2 (all 0, or all non-zero with the split images); trace: optional
 // per-tile phase timestamps (angular_tc_trace_slots() per tile), nullptr: off
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
-                              int error_slot, const int* parity, cudaStream_t s, unsigned long long* trace = nullptr);
+                              int error_slot, const int* parity, bool bf, cudaStream_t s,
+                              unsigned long long* trace = nullptr);
 int angular_tc_trace_slots();
 
 // Batched launches over many propagations' passes (block -> (instance, tile) by offsets)
-cudaError_t launch_pass_batched(bool fp64, const PassParams* params_dev, const int64_t* offsets_dev, int count,
-                                int64_t blocks, int threads, size_t smem, cudaStream_t s);
+cudaError_t launch_pass_batched(bool fp64, bool sweep, const PassParams* params_dev, const int64_t* offsets_dev,
+                                int count, int64_t blocks, int threads, size_t smem, cudaStream_t s);
 size_t tc_params_bytes();
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
                     const int* parity, void* out);
 cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,
-                                      size_t smem, cudaStream_t s);
+                                      size_t smem, bool bf, cudaStream_t s);
 
 // Auxiliary kernels (aux_kernels.cu)
 cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);

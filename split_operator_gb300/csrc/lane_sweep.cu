@@ -376,7 +376,10 @@ __device__ void run_scalar(const PassParams& p, const DevOp& op, const double* t
 template <typename C>
 __host__ __device__ constexpr int load_batch() { return 64 / (int)sizeof(C); }
 
-template <typename R, int RMAX>
+// SWEEP: the pass has only point-wise ops, norms, scalar bookkeeping and power-of-two FFTs
+// (16 or more points): the lane-matrix, direct-DFT and overlap paths are compiled out,
+// which keeps the kernel small (instruction-cache misses stalled the general interpreter).
+template <typename R, int RMAX, bool SWEEP>
 __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t tile) {
   using C = typename Cx<R>::T;
   constexpr bool kF64 = sizeof(R) == 8;
@@ -537,16 +540,17 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
           break;
         }
         case OP_FFT:
-          if (pow2 && n >= 16)
+          if (SWEEP || (pow2 && n >= 16))
             fft_stockham<RMAX>(buf, alt, g, op.dir, tw);
-          else
+          else if constexpr (!SWEEP)
             dft_direct(buf, alt, g, op.dir, tw);
           break;
         case OP_MAT:
-          mat_apply(buf, alt, g, op, nullptr);
+          if constexpr (!SWEEP) mat_apply(buf, alt, g, op, nullptr);
           break;
         case OP_MAT_LANE:
         case OP_MAT_SLICE: {
+          if constexpr (!SWEEP) {
           for (int l = tid; l < L; l += T) {
             int64_t idx;
             if (op.kind == OP_MAT_SLICE) {
@@ -566,6 +570,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
           }
           __syncthreads();
           mat_apply(buf, alt, g, op, lane_sel);
+          }
           break;
         }
         case OP_NORM:
@@ -685,14 +690,14 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
   }
 }
 
-template <typename R, int RMAX>
+template <typename R, int RMAX, bool SWEEP>
 __global__ void __launch_bounds__(512, 2) pass_kernel(const __grid_constant__ PassParams p) {
-  pass_tile<R, RMAX>(p, blockIdx.x);
+  pass_tile<R, RMAX, SWEEP>(p, blockIdx.x);
 }
 
 // Many propagations' passes in one launch: block b runs tile (b - offsets[i]) of
 // params[i], offsets[i] <= b < offsets[i + 1].
-template <typename R, int RMAX>
+template <typename R, int RMAX, bool SWEEP>
 __global__ void __launch_bounds__(512, 2) pass_kernel_batched(const PassParams* __restrict__ params,
                                                            const int64_t* __restrict__ offsets, int count) {
   const int64_t b = blockIdx.x;
@@ -710,13 +715,13 @@ __global__ void __launch_bounds__(512, 2) pass_kernel_batched(const PassParams* 
   for (int k = threadIdx.x; k < (int)(sizeof(PassParams) / 4); k += blockDim.x)
     reinterpret_cast<uint32_t*>(&sp)[k] = reinterpret_cast<const uint32_t*>(params + lo)[k];
   __syncthreads();
-  pass_tile<R, RMAX>(sp, b - offsets[lo]);
+  pass_tile<R, RMAX, SWEEP>(sp, b - offsets[lo]);
 }
 
-template <typename R, int RMAX>
+template <typename R, int RMAX, bool SWEEP>
 static cudaError_t launch_batched_impl(const PassParams* params_dev, const int64_t* offsets_dev, int count,
                                        int64_t blocks, int threads, size_t smem, cudaStream_t s) {
-  auto kern = pass_kernel_batched<R, RMAX>;
+  auto kern = pass_kernel_batched<R, RMAX, SWEEP>;
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
@@ -729,10 +734,13 @@ static cudaError_t launch_batched_impl(const PassParams* params_dev, const int64
   return cudaGetLastError();
 }
 
-cudaError_t launch_pass_batched(bool fp64, const PassParams* params_dev, const int64_t* offsets_dev, int count,
-                                int64_t blocks, int threads, size_t smem, cudaStream_t s) {
-  return fp64 ? launch_batched_impl<double, 8>(params_dev, offsets_dev, count, blocks, threads, smem, s)
-              : launch_batched_impl<float, 16>(params_dev, offsets_dev, count, blocks, threads, smem, s);
+cudaError_t launch_pass_batched(bool fp64, bool sweep, const PassParams* params_dev, const int64_t* offsets_dev,
+                                int count, int64_t blocks, int threads, size_t smem, cudaStream_t s) {
+  if (fp64)
+    return sweep ? launch_batched_impl<double, 8, true>(params_dev, offsets_dev, count, blocks, threads, smem, s)
+                 : launch_batched_impl<double, 8, false>(params_dev, offsets_dev, count, blocks, threads, smem, s);
+  return sweep ? launch_batched_impl<float, 16, true>(params_dev, offsets_dev, count, blocks, threads, smem, s)
+               : launch_batched_impl<float, 16, false>(params_dev, offsets_dev, count, blocks, threads, smem, s);
 }
 
 size_t pass_smem_bytes(const PassParams& p, bool fp64) {
@@ -749,6 +757,14 @@ size_t pass_smem_bytes(const PassParams& p, bool fp64) {
 void pass_choose_buffers(PassParams& p, bool fp64) {
   (void)fp64;
   p.one_buffer = 0;  // every pass keeps the ping-pong pair of tile buffers
+  const Geometry& g = p.g;
+  bool sweep = true;
+  for (int i = 0; i < p.nops; ++i) {
+    const int k = p.ops[i].kind;
+    if (k == OP_MAT || k == OP_MAT_LANE || k == OP_MAT_SLICE || k == OP_DOT) sweep = false;
+    if (k == OP_FFT && !((g.n & (g.n - 1)) == 0 && g.n >= 16)) sweep = false;
+  }
+  p.sweep = sweep ? 1 : 0;
 }
 
 int pass_threads(const Geometry& g) {
@@ -760,10 +776,10 @@ int pass_threads(const Geometry& g) {
   return (int)t;
 }
 
-template <typename R, int RMAX>
+template <typename R, int RMAX, bool SWEEP>
 static cudaError_t launch_impl(const PassParams& p, cudaStream_t s) {
   const size_t smem = pass_smem_bytes(p, sizeof(R) == 8);
-  auto kern = pass_kernel<R, RMAX>;
+  auto kern = pass_kernel<R, RMAX, SWEEP>;
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
@@ -777,7 +793,11 @@ static cudaError_t launch_impl(const PassParams& p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s) { return launch_impl<double, 8>(p, s); }
-cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s) { return launch_impl<float, 16>(p, s); }
+cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s) {
+  return p.sweep ? launch_impl<double, 8, true>(p, s) : launch_impl<double, 8, false>(p, s);
+}
+cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s) {
+  return p.sweep ? launch_impl<float, 16, true>(p, s) : launch_impl<float, 16, false>(p, s);
+}
 
 }  // namespace so

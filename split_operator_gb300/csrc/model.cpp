@@ -306,17 +306,17 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
   }
   c.version = version;
   c.real = real;
-  if (!fp64 && tc_tf32 && real && count == 1 && (n == 32 || n == 64 || n == 128 || n == 256)) {
+  if (!fp64 && (tc_tf32 || tc_bf16) && real && count == 1 && (n == 32 || n == 64 || n == 128 || n == 256)) {
     std::vector<double> md(n * n);
     for (size_t i = 0; i < n * n; ++i) md[i] = m[i].real();
     std::vector<float> img;
-    angular_tc_images(md.data(), (int)n, img);
+    angular_tc_images(md.data(), (int)n, tc_bf16, img);
     upload(c.tc_images, img, stream);
     tc_images_by_matrix_[c.buf.ptr] = c.tc_images.as<float>();
     // the parity-split form as well, when the matrix has the structure (Legendre pairs)
     const int kind = angular_tc_parity(md.data(), (int)n);
     if (kind) {
-      angular_tc_parity_images(md.data(), (int)n, kind, img);
+      angular_tc_parity_images(md.data(), (int)n, kind, tc_bf16, img);
       upload(c.tc_par_images, img, stream);
       tc_parity_by_matrix_[c.buf.ptr] = {kind, c.tc_par_images.as<float>()};
     } else {
@@ -372,13 +372,15 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
     p.partials = partials_.as<double>();
   }
-  std::string name = std::string(par ? "f32 tc3xtf32 parity axis" : "f32 tc3xtf32 axis") + std::to_string(axis) + ":";
+  std::string name = std::string(tc_bf16 ? "f32 tcbf16x3" : "f32 tc3xtf32") + (par ? " parity axis" : " axis") +
+                     std::to_string(axis) + ":";
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
-    // threads: the lane extent and the parity mode (one batched launch serves one of each;
-    // the kernel's thread count is fixed)
+    // threads: the lane extent, the parity mode and the operand format (one batched launch
+    // serves one of each; the kernel's thread count is fixed)
     RecordedPass r{RecordedPass::TensorCore, false, p, std::vector<unsigned char>(tc_params_bytes()),
-                   (int)g.n | (par ? 1 << 16 : 0), angular_tc_smem_bytes((int)g.n, par), name, pass_bytes(ops, g)};
+                   (int)g.n | (par ? 1 << 16 : 0) | (tc_bf16 ? 1 << 17 : 0), angular_tc_smem_bytes((int)g.n, par, tc_bf16),
+                   name, pass_bytes(ops, g)};
     make_tc_params(p, mats, nmat, images, timeout_slot, parity, r.tcp.data());
     recording->push_back(std::move(r));
     return true;
@@ -394,7 +396,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     trace = DeviceBuffer((size_t)g.tiles * angular_tc_trace_slots() * sizeof(unsigned long long));
     cuda_check(cudaMemsetAsync(trace.ptr, 0, trace.bytes, stream), "trace clear");
   }
-  cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, parity, stream,
+  cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, parity, tc_bf16, stream,
                                trace_path ? trace.as<unsigned long long>() : nullptr),
              "tensor-core pass launch");
   if (trace_path) {
@@ -459,7 +461,7 @@ void Engine::submit(const Action& a) {
   }
   const int need = k == OP_NORM ? 1 : (k == OP_DOT ? 2 : 0);
   if ((int)cur_.size() >= kMaxOps || cur_red_ + need > kMaxRed) flush();
-  if (k == OP_MAT && tc_tf32) {
+  if (k == OP_MAT && (tc_tf32 || tc_bf16)) {
     // the tensor-core pass holds at most two lane-matrix products
     int mats = 0;
     for (const DevOp& o : cur_) mats += o.kind == OP_MAT;
@@ -502,7 +504,7 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   p.nred = nred;
   if (fft) p.twiddle = twiddle((size_t)p.g.n);
   pass_choose_buffers(p, fp64);
-  if (!fp64 && tc_tf32 && !resident && try_launch_tc(ops, axis, p)) return;
+  if (!fp64 && (tc_tf32 || tc_bf16) && !resident && try_launch_tc(ops, axis, p)) return;
   if (!resident && (size_t)p.g.tiles > partials_cap_) {
     partials_cap_ = (size_t)p.g.tiles;
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
@@ -1039,6 +1041,7 @@ Propagation::Propagation(WaveFunction& src, so_time_grid time, std::shared_ptr<O
   const bool fp64 = prec == SO_PRECISION_FP64;
   wf_ = std::make_unique<WaveFunction>(src.shape, src.grids, choose_perm(src.shape.size(), *stack_), fp64);
   wf_->eng->tc_tf32 = prec == SO_PRECISION_FP32_TF32X3;
+  wf_->eng->tc_bf16 = prec == SO_PRECISION_FP32_BF16X3;
   wf_->last_grid_names = src.last_grid_names;
   wf_->possible_norm_change = src.possible_norm_change;
   wf_->eng->write_slot(wf_->cache_slot, src.eng->read_slot(src.cache_slot));
@@ -1333,8 +1336,10 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
     const size_t pb = g.kind == RecordedPass::TensorCore ? tc_params_bytes() : sizeof(PassParams);
     std::vector<unsigned char> params(pb * v.size());
     g.bytes = 0.0;
+    g.sweep = true;  // the compact kernel only when every member's pass allows it
     for (size_t i = 0; i < v.size(); ++i) {
       off[i + 1] = off[i] + v[i]->p.g.tiles;
+      g.sweep = g.sweep && v[i]->p.sweep;
       if (g.kind == RecordedPass::TensorCore)
         std::memcpy(params.data() + i * pb, v[i]->tcp.data(), pb);
       else
@@ -1363,11 +1368,12 @@ void Batch::run_groups(std::vector<Group>& gs) {
       cuda_check(cudaEventRecord(t.a, stream_), "event record");
     }
     if (g.kind == RecordedPass::TensorCore)
-      cuda_check(launch_angular_tc_batched(g.params.ptr, g.offsets.as<int64_t>(), g.count, g.blocks, g.smem, stream_),
+      cuda_check(launch_angular_tc_batched(g.params.ptr, g.offsets.as<int64_t>(), g.count, g.blocks, g.smem,
+                                           (g.threads >> 17) & 1, stream_),
                  "batched tensor-core pass");
     else
-      cuda_check(launch_pass_batched(g.fp64, g.params.as<PassParams>(), g.offsets.as<int64_t>(), g.count, g.blocks,
-                                     g.threads, g.smem, stream_),
+      cuda_check(launch_pass_batched(g.fp64, g.sweep, g.params.as<PassParams>(), g.offsets.as<int64_t>(), g.count,
+                                     g.blocks, g.threads, g.smem, stream_),
                  "batched pass");
     if (timing_) {
       cuda_check(cudaEventRecord(t.b, stream_), "event record");

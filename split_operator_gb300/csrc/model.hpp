@@ -125,6 +125,7 @@ class Engine {
   int nonfinite_slot = 0;
   int timeout_slot = 0;
   bool tc_tf32 = false;  // real lane matrices on the tensor cores (3xTF32); FP32 state only
+  bool tc_bf16 = false;  // the same as split-BF16x3
 
   size_t points() const;
   size_t elem_bytes() const { return fp64 ? 16 : 8; }
@@ -428,6 +429,7 @@ class Batch {
   struct Group {
     RecordedPass::Kind kind;
     bool fp64;
+    bool sweep = false;  // lane-sweep groups: every member's pass runs the compact sweep kernel
     int threads;
     size_t smem;
     int64_t blocks;

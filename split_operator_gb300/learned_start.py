@@ -174,12 +174,19 @@ class LearnedStart:
         self.mean = None
         self.std = None
 
-    def fit(self, params, states, steps=3000, lr=1e-3):
+    def fit(self, params, states, steps=3000, lr=1e-3, lr_end=None, segments=10):
+        """Full-batch Adam; with lr_end the rate falls geometrically from lr to lr_end
+        over `segments` equal parts (the optimiser's moments carry across them)."""
         coef = np.stack([self.basis.coefficients(s).ravel() for s in states])
         self.mean = coef.mean(axis=0)
         self.std = coef.std(axis=0) + 1e-12 * np.abs(coef).max()
         y = ((coef - self.mean) / self.std).astype(np.float32)
-        return self.net.train(scale_params(params), y, steps=steps, lr=lr)
+        x = scale_params(params)
+        if lr_end is None or segments <= 1:
+            return self.net.train(x, y, steps=steps, lr=lr)
+        per = max(1, steps // segments)
+        rates = lr * (lr_end / lr) ** (np.arange(segments) / (segments - 1))
+        return np.concatenate([self.net.train(x, y, steps=per, lr=float(r)) for r in rates])
 
     def predict(self, params):
         y = self.net.forward(scale_params(params)).astype(np.float64)
@@ -192,12 +199,15 @@ def evaluate(model: LearnedStart, params, g: Grid2D, every=5, max_steps=20000, t
     _, e_star, steps_plain_full = ground_states(params, g, tol=tol, every=20, max_steps=max_steps)
     gauss = [problem(p, g) for p in params]
     _, steps_g, wall_g = relax(gauss, every=every, max_steps=max_steps, target=e_star)
+    t0 = time.perf_counter()
     starts = model.predict(params)
+    t_predict = time.perf_counter() - t0
     learned = [problem(p, g, psi0=s) for p, s in zip(params, starts)]
     _, steps_l, wall_l = relax(learned, every=every, max_steps=max_steps, target=e_star)
+    wall_l += t_predict  # the network's forward pass and the basis sum are part of the learned start
     return {"heldout": len(params), "energy_star_mean": float(np.mean(e_star)),
             "steps_gaussian_mean": float(np.mean(steps_g)), "steps_learned_mean": float(np.mean(steps_l)),
-            "wall_s_gaussian": wall_g, "wall_s_learned": wall_l,
+            "wall_s_gaussian": wall_g, "wall_s_learned": wall_l, "predict_s": t_predict,
             "wall_ratio_learned_over_gaussian": wall_l / wall_g,
             "steps_ratio_learned_over_gaussian": float(np.mean(steps_l) / np.mean(steps_g)),
             "converged_gaussian": int(np.sum(steps_g < max_steps)), "converged_learned": int(np.sum(steps_l < max_steps))}
@@ -211,6 +221,8 @@ def main():
     ap.add_argument("--nth", type=int, default=64)
     ap.add_argument("--modes", type=int, default=64)
     ap.add_argument("--epochs", type=int, default=3000)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr-end", type=float, default=None)
     ap.add_argument("--out", default="learned_start.json")
     a = ap.parse_args()
     g = Grid2D(a.nr, a.nth)
@@ -220,10 +232,13 @@ def main():
     t_data = time.perf_counter() - t0
     basis = RadialBasis(states, g, a.modes)
     model = LearnedStart(basis)
-    losses = model.fit(ptrain, states, steps=a.epochs)
+    t0 = time.perf_counter()
+    losses = model.fit(ptrain, states, steps=a.epochs, lr=a.lr, lr_end=a.lr_end)
+    t_fit = time.perf_counter() - t0
     res = evaluate(model, param_sets(a.heldout, 6), g)
     res.update({"train": a.train, "grid": [a.nr, a.nth], "modes": a.modes, "train_loss_first": float(losses[0]),
-                "train_loss_last": float(losses[-1]), "data_generation_s": t_data,
+                "train_loss_last": float(losses[-1]), "data_generation_s": t_data, "fit_s": t_fit,
+                "epochs": a.epochs, "lr": a.lr, "lr_end": a.lr_end,
                 "train_steps_mean": float(np.mean(nsteps))})
     with open(a.out, "w") as f:
         json.dump(res, f, indent=1)

@@ -5,8 +5,10 @@ dt = 0.5, border damping with a loss checker), 10^4 real-time steps.
   (propagation.rs:134-182 step order): relative L2 <= 1e-9 after 10^4 steps, norm and
   accumulated loss to the same order.
 * Each FP32 mode against the FP64 GPU path: one step from the same state within
-  relative L2 1e-6; the accumulated error at 10^2, 10^3 and 10^4 steps is reported
-  (written to precision_report.json in $SO_REPORT_DIR when set).
+  relative L2 1e-6 (FP32 SIMT and 3xTF32) or 2e-5 (split-BF16x3: a bf16 pair keeps
+  16 significand bits, so each operand carries a relative error up to 2^-17 ~ 7.6e-6);
+  the accumulated error at 10^2, 10^3 and 10^4 steps is reported (written to
+  precision_report.json in $SO_REPORT_DIR when set).
 """
 import json
 import os
@@ -22,6 +24,7 @@ pytestmark = pytest.mark.gpu
 NR, NTH = 4096, 128
 CHECKPOINTS = (100, 1000, 10000)
 FP32_MODES = ("fp32_simt", "fp32_tf32x3", "fp32_bf16x3")
+ONE_STEP_TOL = {"fp32_simt": 1e-6, "fp32_tf32x3": 1e-6, "fp32_bf16x3": 2e-5}
 
 
 def _norm(psi, wr, wth):
@@ -81,7 +84,7 @@ def test_long_run_fp64_vs_cpu_restatement_and_fp32_modes(tmp_path):
     print(json.dumps(report))
 
     for m, e in one.items():
-        assert e <= 1e-6, (m, e)
+        assert e <= ONE_STEP_TOL[m], (m, e)
     last = rows[-1]
     assert rows[0]["fp64_vs_cpu_rel_l2"] <= 1e-10
     assert last["fp64_vs_cpu_rel_l2"] <= 1e-9

@@ -146,3 +146,25 @@ def test_parity_split_legendre_pair_matches_plain_form(so, monkeypatch):
     # FP32 state: about 3e-7 per step against FP64
     assert e_split < 1e-5 and e_plain < 1e-5, (e_split, e_plain)
     assert rel_l2(out["1"], out["0"]) < 1e-5
+
+
+@pytest.mark.parametrize("n,nr", [(128, 256), (32, 64), (256, 256)])
+def test_real_lane_matrix_split_bf16x3(so, n, nr):
+    """Split-BF16x3 tensor-core form (x = bf16(x) + bf16(remainder), three products, FP32
+    accumulation): about 16 significant bits, so a few 1e-6 per product."""
+    rng = np.random.default_rng(7 * n + nr)
+    psi = rng.standard_normal((nr, n)) + 1j * rng.standard_normal((nr, n))
+    t = rng.standard_normal((n, n)) / np.sqrt(n)
+    g0 = so.Grid.new_linear_continuos("r", 0.0, 1.0, nr, 0)
+    g1 = so.Grid.new_linear_countable("th", 0.0, 1.0, n, 1)
+    wf = so.WaveFunction(psi, [g0, g1])
+    mt = so.MatrixTransformation(g1, so.Grid.new_linear_countable("l", 0.0, 1.0, n, 1))
+    mt.set_diagonalization_matrix(t.astype(np.complex128), np.eye(n, dtype=np.complex128))
+    st = so.OperationStack()
+    st.add_transformation(mt, so.NORMAL)
+    prop = so.Propagation(wf, so.TimeGrid(1.0, 3), st, "fp32_bf16x3")
+    prop.set_timing(True)
+    prop.steps(1)
+    assert any("tcbf16x3" in k[0] for k in prop.kernel_times())
+    err = rel_l2(prop.get_array(), psi @ t.T)
+    assert err < 3e-5, err
