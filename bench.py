@@ -333,28 +333,58 @@ def run_ours(a):
         return
 
     # end to end through the C ABI: pinned FP64 host state in, one step, state out
-    e2e_steps = 3
+    e2e_steps = 5
     hosts = [torch.empty(int(np.prod(p.wave_function_shape())) * 2, dtype=torch.float64).pin_memory()
              for p in props]
     outs = [torch.empty_like(h).pin_memory() for h in hosts]
     for p, h in zip(props, hosts):
         h.numpy()[:] = p.get_array().view(np.float64).ravel()
+    in_ptrs, out_ptrs = [h.data_ptr() for h in hosts], [o.data_ptr() for o in outs]
+
+    def e2e_step():
+        if single:
+            props[0].set_array_ptr(in_ptrs[0])
+            props[0].steps(1)
+            props[0].get_array_ptr(out_ptrs[0])
+        else:
+            batch.steps_host_ptr(in_ptrs, out_ptrs, 1)
+
+    e2e_step()  # warm-up
     torch.cuda.synchronize()
+    barrier(world)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for p, h in zip(props, hosts):
-            p.set_array_ptr(h.data_ptr())
-        if single:
-            props[0].steps(1)
-        else:
-            batch.steps(1)
-        for p, o in zip(props, outs):
-            p.get_array_ptr(o.data_ptr())
+        e2e_step()
     e2e_s = allmax(world, time.perf_counter() - t0)
+    # one more step as three separate calls (each waited on), for the breakdown only
+    ph = []
+    t = time.perf_counter()
+    if single:
+        props[0].set_array_ptr(in_ptrs[0])
+    else:
+        batch.set_arrays_ptr(in_ptrs)
+    torch.cuda.synchronize()
+    ph.append(time.perf_counter() - t)
+    t = time.perf_counter()
+    props[0].steps(1) if single else batch.steps(1)
+    torch.cuda.synchronize()
+    ph.append(time.perf_counter() - t)
+    t = time.perf_counter()
+    if single:
+        props[0].get_array_ptr(out_ptrs[0])
+    else:
+        batch.get_arrays_ptr(out_ptrs)
+    ph.append(time.perf_counter() - t)
     e2e = {"value": points * e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": points * 16,
            "d2h_bytes_per_step": points * 16, "steps": e2e_steps,
-           "note": "every step: so_propagation_set_array from pinned FP64 host buffers for all instances, one step, "
-                   "so_propagation_get_array into pinned host buffers"}
+           "unpipelined_phase_ms": {"set_arrays": ph[0] * 1e3, "steps": ph[1] * 1e3, "get_arrays": ph[2] * 1e3},
+           "host_link_gbs": {"h2d": 211, "d2h": 193, "source": "cudaMemcpyAsync of 1 GiB pinned, measured on this "
+                                                               "GPU model"},
+           "note": ("every step: one so_batch_steps_host call: pinned FP64 host states of all instances in, one "
+                    "step, states out to pinned host buffers, pipelined over 4 instance chunks on their own "
+                    "streams (copy engines both ways)") if not single else
+                   "every step: so_propagation_set_array from a pinned FP64 host buffer, one step, "
+                   "so_propagation_get_array into a pinned host buffer"}
 
     acc = {}
     if rank == 0:

@@ -250,7 +250,11 @@ int so_propagation_reset_savers_state(so_propagation p); /* propagation.rs:116-1
 int so_propagation_savers_save(so_propagation p);        /* propagation.rs:234-243 */
 /* wave_function() (propagation.rs:111-113): a stand-alone FP64 copy of the current state */
 int so_propagation_wave_function(so_propagation p, so_wave_function* out);
-/* host copy of the current array (logical row-major, complex128) and its replacement */
+/* host copy of the current array (logical row-major, complex128) and its replacement.
+ * get returns once `out` is written.  A page-locked `in` is read on the propagation's
+ * stream after set returns (the layout kernel reads it directly): keep it unchanged until
+ * a later call that waits on the stream (get_array, norm, steps).  Pageable `in` is copied
+ * before set returns. */
 int so_propagation_get_array(so_propagation p, double* out);
 int so_propagation_set_array(so_propagation p, const double* in);
 /* norm of the current state with the current representation's weights */
@@ -283,6 +287,17 @@ int so_batch_set_timing(so_batch b, int enabled);
 int so_batch_kernel_times(so_batch b, char* buf, size_t cap);
 /* launches of the repeated part of one step (after the first) */
 int so_batch_launches_per_step(so_batch b, size_t* out);
+/* Every member's state from / to host arrays (count == the batch size; array i is the
+ * logical row-major complex128 state of propagation i, as so_propagation_set_array /
+ * so_propagation_get_array).  Page-locked host arrays are read and written by the
+ * layout kernels directly; get queues every export and waits once. */
+int so_batch_set_arrays(so_batch b, const double* const* in, size_t count);
+int so_batch_get_arrays(so_batch b, double* const* out, size_t count);
+/* so_batch_set_arrays(in), so_batch_steps(steps), so_batch_get_arrays(out) as one call,
+ * pipelined: the members are split into up to four chunks on streams of their own, each
+ * copied in (copy engines), stepped and copied out, so the host link's two directions
+ * and the chunks' steps overlap.  `in` and `out` may be the same arrays. */
+int so_batch_steps_host(so_batch b, const double* const* in, double* const* out, size_t count, uint64_t steps);
 void so_batch_free(so_batch b);
 
 /* ---- Learned starting states (no counterpart in the reference) ----

@@ -135,6 +135,9 @@ SIGNATURES = {
     "so_batch_set_timing": [_P, _I],
     "so_batch_kernel_times": [_P, C.c_char_p, _S],
     "so_batch_launches_per_step": [_P, _SP],
+    "so_batch_set_arrays": [_P, _PP, _S],
+    "so_batch_get_arrays": [_P, _PP, _S],
+    "so_batch_steps_host": [_P, _PP, _PP, _S, C.c_uint64],
     "so_mlp_new": [C.POINTER(C.c_int), _S, C.c_uint64, _PP],
     "so_mlp_num_params": [_P, _SP],
     "so_mlp_get_params": [_P, C.POINTER(C.c_float)],

@@ -685,6 +685,37 @@ class Batch(_Handle):
         call("so_batch_launches_per_step", self._h, C.byref(v))
         return v.value
 
+    def set_arrays_ptr(self, host_ptrs: Sequence[int]):
+        """Every member's state from host addresses (logical complex128 each; page-locked
+        buffers are read by the layout kernels directly)."""
+        arr = (C.c_void_p * len(host_ptrs))(*host_ptrs)
+        call("so_batch_set_arrays", self._h, C.cast(arr, C.POINTER(C.c_void_p)), len(host_ptrs))
+
+    def get_arrays_ptr(self, host_ptrs: Sequence[int]):
+        """Every member's state into host addresses; returns when all are written."""
+        arr = (C.c_void_p * len(host_ptrs))(*host_ptrs)
+        call("so_batch_get_arrays", self._h, C.cast(arr, C.POINTER(C.c_void_p)), len(host_ptrs))
+
+    def steps_host_ptr(self, in_ptrs: Sequence[int], out_ptrs: Sequence[int], n: int):
+        """States in from host addresses, n steps, states out to host addresses: one
+        pipelined call (chunks of members overlap their copies and steps)."""
+        a = (C.c_void_p * len(in_ptrs))(*in_ptrs)
+        b = (C.c_void_p * len(out_ptrs))(*out_ptrs)
+        call("so_batch_steps_host", self._h, C.cast(a, C.POINTER(C.c_void_p)), C.cast(b, C.POINTER(C.c_void_p)),
+             len(in_ptrs), n)
+
+    def set_arrays(self, arrays):
+        arrs = [np.ascontiguousarray(a, dtype=np.complex128) for a in arrays]
+        for a, p in zip(arrs, self._props):
+            if a.shape != tuple(p.wave_function_shape()):
+                raise ValueError("state shape differs from the propagation's grid")
+        self.set_arrays_ptr([a.ctypes.data for a in arrs])
+
+    def get_arrays(self):
+        outs = [np.empty(tuple(p.wave_function_shape()), dtype=np.complex128) for p in self._props]
+        self.get_arrays_ptr([o.ctypes.data for o in outs])
+        return outs
+
 
 def _fp(a):
     return a.ctypes.data_as(C.POINTER(C.c_float))

@@ -960,6 +960,27 @@ int so_batch_launches_per_step(so_batch b, size_t* out) {
     *out = b->b->launches_per_step();
   });
 }
+int so_batch_set_arrays(so_batch b, const double* const* in, size_t count) {
+  return guard([&] {
+    need(b && in, "null argument");
+    need(count == b->b->size(), "count differs from the batch size");
+    b->b->set_arrays(in);
+  });
+}
+int so_batch_get_arrays(so_batch b, double* const* out, size_t count) {
+  return guard([&] {
+    need(b && out, "null argument");
+    need(count == b->b->size(), "count differs from the batch size");
+    b->b->get_arrays(out);
+  });
+}
+int so_batch_steps_host(so_batch b, const double* const* in, double* const* out, size_t count, uint64_t steps) {
+  return guard([&] {
+    need(b && in && out, "null argument");
+    need(count == b->b->size(), "count differs from the batch size");
+    b->b->steps_host(in, out, steps);
+  });
+}
 void so_batch_free(so_batch b) { delete b; }
 
 }  // extern "C"

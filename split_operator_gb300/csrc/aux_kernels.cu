@@ -100,6 +100,66 @@ __global__ void density_kernel(double* dst, const S* src, Perm P, int64_t total)
   }
 }
 
+// Two-axis layouts whose storage order is the transpose of the logical order (the radial
+// FFT axis, logical axis 0, stored last): a 32 x 32 tile is read along the source's
+// contiguous axis and written along the destination's, through shared memory, so both
+// sides are coalesced.  This matters most when one side is pinned host memory read or
+// written directly by the kernel over the host link.
+//   import: logical [a0][a1] (complex128)  ->  storage [a1][a0] (D)
+//   export: storage [a1][a0] (S)           ->  logical [a0][a1] (complex128)
+constexpr int kTT = 32;
+
+template <typename D>
+__global__ void __launch_bounds__(256) import_transpose_kernel(D* __restrict__ dst, const double2* __restrict__ src,
+                                                               int64_t n0, int64_t n1) {
+  __shared__ double2 tile[kTT][kTT + 1];
+  const int64_t a1 = blockIdx.x * (int64_t)kTT, a0 = blockIdx.y * (int64_t)kTT;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int i = ty; i < kTT; i += 8) {
+    const int64_t r = a0 + i, c = a1 + tx;
+    if (r < n0 && c < n1) tile[i][tx] = src[r * n1 + c];
+  }
+  __syncthreads();
+  for (int i = ty; i < kTT; i += 8) {
+    const int64_t c = a1 + i, r = a0 + tx;
+    if (r < n0 && c < n1) {
+      const double2 v = tile[tx][i];
+      dst[c * n0 + r] = D{(decltype(dst->x))v.x, (decltype(dst->x))v.y};
+    }
+  }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256) export_transpose_kernel(double2* __restrict__ dst, const S* __restrict__ src,
+                                                               int64_t n0, int64_t n1) {
+  __shared__ double2 tile[kTT][kTT + 1];
+  const int64_t a1 = blockIdx.x * (int64_t)kTT, a0 = blockIdx.y * (int64_t)kTT;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int i = ty; i < kTT; i += 8) {
+    const int64_t c = a1 + i, r = a0 + tx;
+    if (r < n0 && c < n1) {
+      const S v = src[c * n0 + r];
+      tile[tx][i] = double2{(double)v.x, (double)v.y};
+    }
+  }
+  __syncthreads();
+  for (int i = ty; i < kTT; i += 8) {
+    const int64_t r = a0 + i, c = a1 + tx;
+    if (r < n0 && c < n1) dst[r * n1 + c] = tile[i][tx];
+  }
+}
+
+bool layout_is_transpose2(const Geometry& g) { return g.ndim == 2 && g.perm[0] == 1 && g.perm[1] == 0; }
+bool layout_is_identity(const Geometry& g) {
+  for (int q = 0; q < g.ndim; ++q)
+    if (g.perm[q] != q) return false;
+  return true;
+}
+
+static dim3 transpose_grid(const Geometry& g) {  // g.sshape = {n1, n0}
+  return dim3((unsigned)((g.sshape[0] + kTT - 1) / kTT), (unsigned)((g.sshape[1] + kTT - 1) / kTT));
+}
+
 static int64_t total_of(const Geometry& g) {
   int64_t t = 1;
   for (int q = 0; q < g.ndim; ++q) t *= g.sshape[q];
@@ -115,6 +175,18 @@ static unsigned blocks_for(int64_t total) {
 
 cudaError_t launch_import(void* dst, bool dst_fp64, const double* src, const Geometry& g, cudaStream_t st) {
   const int64_t total = total_of(g);
+  if (layout_is_transpose2(g)) {
+    const dim3 grid = transpose_grid(g), block(kTT, 8);
+    if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
+    if (dst_fp64)
+      import_transpose_kernel<double2><<<grid, block, 0, st>>>((double2*)dst, (const double2*)src, g.sshape[1],
+                                                               g.sshape[0]);
+    else
+      import_transpose_kernel<float2><<<grid, block, 0, st>>>((float2*)dst, (const double2*)src, g.sshape[1],
+                                                              g.sshape[0]);
+    count_launch();
+    return cudaGetLastError();
+  }
   const Perm P = make_perm(g);
   if (dst_fp64)
     import_kernel<double2><<<blocks_for(total), 256, 0, st>>>((double2*)dst, (const double2*)src, P, total);
@@ -126,6 +198,18 @@ cudaError_t launch_import(void* dst, bool dst_fp64, const double* src, const Geo
 
 cudaError_t launch_export(double* dst, const void* src, bool src_fp64, const Geometry& g, cudaStream_t st) {
   const int64_t total = total_of(g);
+  if (layout_is_transpose2(g)) {
+    const dim3 grid = transpose_grid(g), block(kTT, 8);
+    if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
+    if (src_fp64)
+      export_transpose_kernel<double2><<<grid, block, 0, st>>>((double2*)dst, (const double2*)src, g.sshape[1],
+                                                               g.sshape[0]);
+    else
+      export_transpose_kernel<float2><<<grid, block, 0, st>>>((double2*)dst, (const float2*)src, g.sshape[1],
+                                                              g.sshape[0]);
+    count_launch();
+    return cudaGetLastError();
+  }
   const Perm P = make_perm(g);
   if (src_fp64)
     export_kernel<double2><<<blocks_for(total), 256, 0, st>>>((double2*)dst, (const double2*)src, P, total);

@@ -76,7 +76,8 @@ struct PassParams {
   double* slots;
   double* partials;             // [kMaxRed][tiles]
   unsigned int* counter;        // last-block ticket (reset by the last block)
-  const void* twiddle;          // exp(-2 pi i j / n), j < n, in the state precision
+  const void* twiddle;          // n entries, state precision: stage-major (stage_twiddle_exponent) for
+                                // power-of-two n >= 16, else exp(-2 pi i j / n) at j
   double* record;
   int32_t nops;
   int32_t nred;
@@ -87,6 +88,30 @@ struct PassParams {
   int32_t sweep;                // 1: only point-wise ops, norms, scalars and power-of-two FFTs
   DevOp ops[kMaxOps];
 };
+
+// Twiddle table of a power-of-two lane FFT (n >= 16) in stage-major order: the Stockham
+// stages run radix rmax (16 FP32, 8 FP64) and one smaller closing radix; stage (RS, p)
+// with p > 1 owns (RS - 1) * p consecutive entries, entry (r - 1) * p + k holding
+// w^(r k n / (RS p)), w = exp(-2 pi i / n).  Threads of a stage read consecutive k, so the
+// shared-memory reads are free of bank conflicts.  Returns the exponent of entry e
+// (0 past the end of the table; the table occupies at most n entries).
+__host__ __device__ inline int64_t stage_twiddle_exponent(int64_t e, int64_t n, int rmax) {
+  int64_t p = 1, off = 0;
+  while (p < n) {
+    const int64_t rs = n / p >= rmax ? rmax : n / p;
+    if (p > 1) {
+      const int64_t cnt = (rs - 1) * p;
+      if (e < off + cnt) {
+        const int64_t q = e - off, r = q / p + 1, k = q - (r - 1) * p;
+        return r * k * (n / (rs * p));
+      }
+      off += cnt;
+    }
+    p *= rs;
+  }
+  return 0;
+}
+__host__ __device__ inline bool stage_twiddles(int64_t n) { return n >= 16 && (n & (n - 1)) == 0; }
 
 // Host launchers (lane_sweep.cu)
 cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);
@@ -127,6 +152,10 @@ cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* off
 cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);
 // dst (storage order, precision of dst) <- src (logical row-major complex128)
 cudaError_t launch_import(void* dst, bool dst_fp64, const double* src, const Geometry& g, cudaStream_t s);
+// storage order is the logical order / the transpose of a two-axis logical order (the
+// layouts whose import and export stay coalesced on both sides)
+bool layout_is_identity(const Geometry& g);
+bool layout_is_transpose2(const Geometry& g);
 // dst (logical row-major complex128) <- src (storage order)
 cudaError_t launch_export(double* dst, const void* src, bool src_fp64, const Geometry& g, cudaStream_t s);
 // density |psi|^2 in logical order, and its weighted marginal along one logical axis

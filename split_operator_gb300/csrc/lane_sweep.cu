@@ -192,7 +192,6 @@ __device__ __forceinline__ void stockham_stage(const C* __restrict__ src, C* __r
                                                int p, int dir, const C* __restrict__ tw, bool last, R sc) {
   const int nb = n / RS;
   const int total = L * nb;
-  const int estride = n / (RS * p);
   for (int b = threadIdx.x; b < total; b += blockDim.x) {
     const int l = b / nb, i = b - l * nb;
     const int k = i & (p - 1);
@@ -201,7 +200,7 @@ __device__ __forceinline__ void stockham_stage(const C* __restrict__ src, C* __r
     for (int r = 0; r < RS; ++r) {
       C x = src[sidx(l, i + r * nb, ls)];
       if (r > 0 && k > 0) {
-        C w = tw[r * k * estride];  // shared-memory copy of the table
+        C w = tw[(r - 1) * p + k];  // this stage's part of the shared-memory table
         if (dir > 0) w.y = -w.y;
         x = cmul(x, w);
       }
@@ -235,22 +234,26 @@ __device__ void fft_stockham(C*& buf, C*& alt, const Geometry& g, int dir, const
   using R = decltype(buf[0].x);
   const int n = (int)g.n, L = g.lanes_per_tile, ls = g.lane_stride;
   const R scale = inv_sqrt_pow2<R>(__ffs(n) - 1);
-  int p = 1;
+  int p = 1, off = 0;  // off: the stage's first entry in the stage-major table
   while (p < n) {
     const int rem = n / p;
+    const C* ts = tw + off;
+    int rs;
     if (rem >= RMAX) {
-      stockham_stage<RMAX>(buf, alt, L, n, ls, p, dir, tw, rem == RMAX, scale);
-      p *= RMAX;
+      stockham_stage<RMAX>(buf, alt, L, n, ls, p, dir, ts, rem == RMAX, scale);
+      rs = RMAX;
     } else if (rem == 8) {
-      stockham_stage<8>(buf, alt, L, n, ls, p, dir, tw, true, scale);
-      p *= 8;
+      stockham_stage<8>(buf, alt, L, n, ls, p, dir, ts, true, scale);
+      rs = 8;
     } else if (rem == 4) {
-      stockham_stage<4>(buf, alt, L, n, ls, p, dir, tw, true, scale);
-      p *= 4;
+      stockham_stage<4>(buf, alt, L, n, ls, p, dir, ts, true, scale);
+      rs = 4;
     } else {
-      stockham_stage<2>(buf, alt, L, n, ls, p, dir, tw, true, scale);
-      p *= 2;
+      stockham_stage<2>(buf, alt, L, n, ls, p, dir, ts, true, scale);
+      rs = 2;
     }
+    if (p > 1) off += (rs - 1) * p;
+    p *= rs;
     C* t = buf;
     buf = alt;
     alt = t;
@@ -474,7 +477,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
       }
     }
   }
-  // twiddles in shared memory: the butterflies read them at scattered indices
+  // twiddles in shared memory (stage-major for the Stockham stages: consecutive reads)
   const C* tw = reinterpret_cast<const C*>(p.twiddle);
   if (tw) {
     for (int k = tid; k < n; k += T) tw_s[k] = tw[k];

@@ -443,7 +443,13 @@ const void* Engine::twiddle(size_t n) {
   auto it = twiddles_.find(n);
   if (it != twiddles_.end()) return it->second.ptr;
   DeviceBuffer b;
-  upload_complex(b, twiddles(n), fp64, stream);
+  std::vector<cplx> tw = twiddles(n);
+  if (stage_twiddles((int64_t)n)) {  // the Stockham stages' order (same values, permuted)
+    std::vector<cplx> st(n, cplx(0.0, 0.0));
+    for (size_t e = 0; e < n; ++e) st[e] = tw[(size_t)stage_twiddle_exponent((int64_t)e, (int64_t)n, fp64 ? 8 : 16)];
+    tw.swap(st);
+  }
+  upload_complex(b, tw, fp64, stream);
   const void* p = b.ptr;
   twiddles_.emplace(n, std::move(b));
   return p;
@@ -665,29 +671,59 @@ static bool identity_perm(const std::vector<int>& p) {
   return true;
 }
 
-void Engine::import_host(const double* host) {
+// Device address of a page-locked, mapped host range (nullptr for pageable memory or a
+// range that leaves the mapped allocation): kernels read and write such buffers directly
+// over the host link, with no staging copy in device memory.
+static char* mapped_range(const void* host, size_t bytes) {
+  auto dev = [](const void* p) -> char* {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+      cudaGetLastError();  // clear the error of an unknown pointer
+      return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? static_cast<char*>(at.devicePointer) : nullptr;
+  };
+  if (bytes == 0) return nullptr;
+  char* d0 = dev(host);
+  char* d1 = d0 ? dev(static_cast<const char*>(host) + bytes - 1) : nullptr;
+  return d0 && d1 == d0 + bytes - 1 ? d0 : nullptr;
+}
+
+void Engine::import_host(const double* host, bool copy_engine) {
   flush();
   const size_t b = points() * 16;
+  const Geometry g = flat_geometry(*this);
   if (fp64 && identity_perm(perm)) {
     cuda_check(cudaMemcpyAsync(psi.ptr, host, b, cudaMemcpyHostToDevice, stream), "import copy");
     return;
   }
+  if (!copy_engine && (identity_perm(perm) || layout_is_transpose2(g))) {
+    if (const char* d = mapped_range(host, b)) {
+      cuda_check(launch_import(psi.ptr, fp64, reinterpret_cast<const double*>(d), g, stream), "import");
+      return;
+    }
+  }
   if (staging_.bytes < b) staging_ = DeviceBuffer(b);
   cuda_check(cudaMemcpyAsync(staging_.ptr, host, b, cudaMemcpyHostToDevice, stream), "import copy");
-  cuda_check(launch_import(psi.ptr, fp64, staging_.as<double>(), flat_geometry(*this), stream), "import");
+  cuda_check(launch_import(psi.ptr, fp64, staging_.as<double>(), g, stream), "import");
 }
 
-void Engine::export_host(double* host) {
+void Engine::export_host(double* host, bool sync, bool copy_engine) {
   flush();
   const size_t b = points() * 16;
+  const Geometry g = flat_geometry(*this);
+  char* d = nullptr;
   if (fp64 && identity_perm(perm)) {
     cuda_check(cudaMemcpyAsync(host, psi.ptr, b, cudaMemcpyDeviceToHost, stream), "export copy");
+  } else if (!copy_engine && (identity_perm(perm) || layout_is_transpose2(g)) &&
+             (d = mapped_range(host, b)) != nullptr) {
+    cuda_check(launch_export(reinterpret_cast<double*>(d), psi.ptr, fp64, g, stream), "export");
   } else {
     if (staging_.bytes < b) staging_ = DeviceBuffer(b);
-    cuda_check(launch_export(staging_.as<double>(), psi.ptr, fp64, flat_geometry(*this), stream), "export");
+    cuda_check(launch_export(staging_.as<double>(), psi.ptr, fp64, g, stream), "export");
     cuda_check(cudaMemcpyAsync(host, staging_.ptr, b, cudaMemcpyDeviceToHost, stream), "export copy");
   }
-  cuda_check(cudaStreamSynchronize(stream), "export sync");
+  if (sync) cuda_check(cudaStreamSynchronize(stream), "export sync");
 }
 
 // ----------------------------------------------------------------- WaveFunction
@@ -1237,10 +1273,10 @@ void Propagation::savers_save() {
     if (auto* s = dynamic_cast<StateSaver*>(e.op.get())) s->save();
 }
 
-void Propagation::get_array(double* out) { wf_->eng->export_host(out); }
+void Propagation::get_array(double* out, bool sync, bool copy_engine) { wf_->eng->export_host(out, sync, copy_engine); }
 
-void Propagation::set_array(const double* in) {
-  wf_->eng->import_host(in);
+void Propagation::set_array(const double* in, bool copy_engine) {
+  wf_->eng->import_host(in, copy_engine);
   wf_->possible_norm_change = true;
 }
 
@@ -1303,6 +1339,11 @@ Batch::Batch(std::vector<Propagation*> props) : props_(std::move(props)) {
 }
 
 Batch::~Batch() {
+  for (Chunk& ch : chunks_) {
+    ch.batch.reset();
+    cudaStreamSynchronize(ch.stream);
+    cudaStreamDestroy(ch.stream);
+  }
   for (Timed& t : timed_) {
     cudaEventDestroy(t.a);
     cudaEventDestroy(t.b);
@@ -1382,9 +1423,16 @@ void Batch::run_groups(std::vector<Group>& gs) {
   }
 }
 
-void Batch::steps(uint64_t n) {
+void Batch::steps(uint64_t n, bool wait) {
   if (n == 0) return;
-  for (Propagation* p : props_) p->engine().sync();
+  {
+    std::vector<cudaStream_t> seen;  // each member's queued work, then one wait per stream
+    for (Propagation* p : props_) {
+      p->engine().flush();
+      if (std::find(seen.begin(), seen.end(), p->engine().stream) == seen.end()) seen.push_back(p->engine().stream);
+    }
+    for (cudaStream_t st : seen) cuda_check(cudaStreamSynchronize(st), "stream sync");
+  }
   // Host logic of two steps per propagation: passes [head, period..., tail] where the
   // period (the middle passes) repeats for every further step.
   std::vector<std::vector<RecordedPass>> rec;
@@ -1414,8 +1462,20 @@ void Batch::steps(uint64_t n) {
                                             std::to_string(off) + " of " + std::to_string(np) +
                                             " passes); run these propagations one by one");
       }
-  std::vector<std::vector<Group>> pos(np);
-  for (size_t i = 0; i < np; ++i) pos[i] = build_groups(rec, i);
+  // the launch groups (device parameter blocks) of the last call are reused when every
+  // recorded pass has the same parameters: consecutive calls of a steady propagation
+  bool reuse = cached_rec_.size() == rec.size();
+  for (size_t i = 0; reuse && i < rec.size(); ++i) {
+    reuse = cached_rec_[i].size() == rec[i].size();
+    for (size_t j = 0; reuse && j < rec[i].size(); ++j) reuse = same_params(rec[i][j], cached_rec_[i][j]);
+  }
+  if (!reuse) {
+    cached_pos_.clear();
+    cached_pos_.resize(np);
+    for (size_t i = 0; i < np; ++i) cached_pos_[i] = build_groups(rec, i);
+    cached_rec_ = std::move(rec);
+  }
+  std::vector<std::vector<Group>>& pos = cached_pos_;
   launches_per_step_ = 0;
   for (size_t i = per0; i < per0 + m; ++i) launches_per_step_ += pos[i].size();
   // first step (head)
@@ -1432,6 +1492,7 @@ void Batch::steps(uint64_t n) {
       cuda_check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
       for (uint64_t r = 0; r < reps; ++r) cuda_check(cudaGraphLaunch(exec, stream_), "graph launch");
       count_launch(launches_per_step_ * (reps - 1));  // the capture counted the period once
+      cuda_check(cudaStreamSynchronize(stream_), "batch sync");  // before the graph is destroyed
       cudaGraphExecDestroy(exec);
       cudaGraphDestroy(graph);
     } else {
@@ -1442,7 +1503,89 @@ void Batch::steps(uint64_t n) {
   // tail: the last step's closing passes (merged form only)
   if (merged)
     for (size_t i = m + 1; i < np; ++i) run_groups(pos[i]);
-  cuda_check(cudaStreamSynchronize(stream_), "batch sync");
+  if (wait) cuda_check(cudaStreamSynchronize(stream_), "batch sync");
+}
+
+void Batch::set_arrays(const double* const* in) {
+  for (size_t i = 0; i < props_.size(); ++i)
+    if (!in[i]) throw Error(SO_ERR_INVALID, "null state array in batch");
+  for (size_t i = 0; i < props_.size(); ++i) props_[i]->set_array(in[i]);
+}
+
+void Batch::get_arrays(double* const* out) {
+  for (size_t i = 0; i < props_.size(); ++i)
+    if (!out[i]) throw Error(SO_ERR_INVALID, "null state array in batch");
+  // every export is queued first; one wait per distinct stream at the end
+  for (size_t i = 0; i < props_.size(); ++i) props_[i]->get_array(out[i], false);
+  std::vector<cudaStream_t> done;
+  for (Propagation* p : props_) {
+    cudaStream_t s = p->engine().stream;
+    if (std::find(done.begin(), done.end(), s) != done.end()) continue;
+    done.push_back(s);
+    cuda_check(cudaStreamSynchronize(s), "batch export sync");
+  }
+}
+
+void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) {
+  const size_t m = props_.size();
+  for (size_t i = 0; i < m; ++i)
+    if (!in[i] || !out[i]) throw Error(SO_ERR_INVALID, "null state array in batch");
+  if (chunks_.empty()) {
+    // up to four chunks of consecutive members with about equal points, each a batch of
+    // its own on its own stream
+    double total = 0.0;
+    for (Propagation* p : props_) total += (double)p->engine().points();
+    const size_t k = std::min<size_t>(4, m);
+    size_t first = 0;
+    double acc = 0.0;
+    for (size_t c = 0; c < k; ++c) {
+      size_t last = first;
+      const double goal = total * (double)(c + 1) / (double)k;
+      while (last < m && (c + 1 == k || acc < goal || last == first)) acc += (double)props_[last++]->engine().points();
+      if (last == first) break;
+      Chunk ch;
+      ch.first = first;
+      ch.count = last - first;
+      cuda_check(cudaStreamCreateWithFlags(&ch.stream, cudaStreamNonBlocking), "chunk stream");
+      std::vector<Propagation*> sub(props_.begin() + first, props_.begin() + last);
+      std::vector<cudaStream_t> saved;
+      for (Propagation* p : sub) {
+        saved.push_back(p->engine().stream);
+        p->engine().stream = ch.stream;
+      }
+      ch.batch = std::make_unique<Batch>(sub);  // its launches go to ch.stream
+      for (size_t i = 0; i < sub.size(); ++i) sub[i]->engine().stream = saved[i];
+      chunks_.push_back(std::move(ch));
+      first = last;
+    }
+  }
+  // members' own streams: everything queued there before this call completes first
+  std::vector<cudaStream_t> own;
+  for (Propagation* p : props_) {
+    p->engine().flush();
+    own.push_back(p->engine().stream);
+  }
+  for (size_t i = 0; i < m; ++i)
+    if (std::find(own.begin(), own.begin() + i, own[i]) == own.begin() + i)
+      cuda_check(cudaStreamSynchronize(own[i]), "stream sync");
+  for (Chunk& ch : chunks_)
+    for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->engine().stream = ch.stream;
+  try {
+    // imports on the copy engines (host link H2D) for every chunk, then per chunk its steps
+    // and its exports (copy engines, D2H), all queued on the chunk's stream: chunk c's steps
+    // run while later chunks arrive and earlier ones leave
+    for (Chunk& ch : chunks_)
+      for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->set_array(in[i], true);
+    for (Chunk& ch : chunks_) {
+      ch.batch->steps(n, false);  // queued; the host moves on to the next chunk
+      for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->get_array(out[i], false, true);
+    }
+    for (Chunk& ch : chunks_) cuda_check(cudaStreamSynchronize(ch.stream), "chunk sync");
+  } catch (...) {
+    for (size_t i = 0; i < m; ++i) props_[i]->engine().stream = own[i];
+    throw;
+  }
+  for (size_t i = 0; i < m; ++i) props_[i]->engine().stream = own[i];
 }
 
 std::string Batch::kernel_times() {

@@ -152,8 +152,10 @@ class Engine {
   void flush();
   void run_resident(const std::vector<Action>& prog, int repeat);
   void sync();
-  void import_host(const double* host);   // logical complex128 -> storage
-  void export_host(double* host);         // storage -> logical complex128 (synchronizes)
+  // logical complex128 -> storage; copy_engine: staged cudaMemcpyAsync even for page-locked
+  // memory (no SMs busy on the host link, so the copy overlaps kernels of other streams)
+  void import_host(const double* host, bool copy_engine = false);
+  void export_host(double* host, bool sync = true, bool copy_engine = false);  // storage -> logical complex128
   void check_nonfinite();
 
   std::vector<ScalarState*> bound;
@@ -390,8 +392,9 @@ class Propagation {
   std::vector<double> losses(bool include_controls);
   void reset_losses();
   std::unique_ptr<WaveFunction> snapshot();
-  void get_array(double* out);
-  void set_array(const double* in);
+  // sync false: queued on the engine stream; copy_engine: staged through cudaMemcpyAsync
+  void get_array(double* out, bool sync = true, bool copy_engine = false);
+  void set_array(const double* in, bool copy_engine = false);
   double norm();
   std::string describe();
   void set_stream(cudaStream_t s) { wf_->eng->stream = s; }
@@ -420,10 +423,17 @@ class Batch {
  public:
   explicit Batch(std::vector<Propagation*> props);
   ~Batch();
-  void steps(uint64_t n);
+  // wait false: return once the launches are queued (the batch's stream runs them)
+  void steps(uint64_t n, bool wait = true);
   void set_timing(bool on) { timing_ = on; }
   std::string kernel_times();
   size_t launches_per_step() const { return launches_per_step_; }
+  size_t size() const { return props_.size(); }
+  // every member's state from / to host arrays (logical complex128); get waits once at the end
+  void set_arrays(const double* const* in);
+  void get_arrays(double* const* out);
+  // set_arrays, steps(n), get_arrays as one pipeline over member chunks on separate streams
+  void steps_host(const double* const* in, double* const* out, uint64_t n);
 
  private:
   struct Group {
@@ -439,6 +449,14 @@ class Batch {
     double bytes;
   };
   std::vector<Group> build_groups(const std::vector<std::vector<RecordedPass>>& rec, size_t pos);
+  std::vector<std::vector<RecordedPass>> cached_rec_;  // the passes the cached groups were built from
+  std::vector<std::vector<Group>> cached_pos_;
+  struct Chunk {
+    size_t first = 0, count = 0;
+    cudaStream_t stream = nullptr;
+    std::unique_ptr<Batch> batch;
+  };
+  std::vector<Chunk> chunks_;  // steps_host pipeline (built on first use)
   void run_groups(std::vector<Group>& gs);
   std::vector<Propagation*> props_;
   cudaStream_t stream_ = nullptr;

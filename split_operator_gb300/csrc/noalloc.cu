@@ -37,11 +37,13 @@ struct DeviceScratch {
 };
 DeviceScratch g_dev[kMaxDevices];
 
-// exp(-2 pi i j / n) from sincospi (exact at multiples of a quarter turn)
+// exp(-2 pi i m / n) from sincospi (exact at multiples of a quarter turn); m = j, or the
+// stage-major exponent of entry j for the FP64 Stockham stages of power-of-two n >= 16
 __global__ void twiddle_kernel(double2* tw, int64_t n) {
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = stage_twiddles(n) ? stage_twiddle_exponent(j, n, 8) : j;
     double s, c;
-    sincospi(2.0 * (double)j / (double)n, &s, &c);
+    sincospi(2.0 * (double)m / (double)n, &s, &c);
     tw[j] = make_double2(c, -s);
   }
 }

@@ -12,7 +12,10 @@ No counterpart in the reference crate.  Pipeline:
    until successive energies differ by <= 1e-10.  Many instances run together
    through the batched executor.
 3. A radial basis per l: the leading `modes` left singular vectors of the training
-   ground states' radial functions at that l (eigenvectors of their covariance).
+   ground states' radial functions at that l (eigenvectors of their covariance), each
+   sampled in the scaled coordinate xi = (r - re) (m omega)^(1/2) of the harmonic
+   approximation of its well (cubic splines to and from the radial grid), so that the
+   network predicts the shape of the state, not its position and width.
 4. A multilayer perceptron (5 -> 256 -> 256 -> 256 -> Ntheta*modes, BF16 weights, FP32
    accumulation) trained on the library's own CUDA kernels to map the scaled
    parameters to the standardised basis coefficients.
@@ -42,6 +45,28 @@ def param_sets(count, seed):
 
 def scale_params(p):
     return (2.0 * (np.asarray(p) - PARAM_LO) / (PARAM_HI - PARAM_LO) - 1.0).astype(np.float32)
+
+
+def physics_features(p):
+    """Five inputs that set the ground state's shape in the well's scaled frame:
+    ln lambda (lambda = (2 m D)^(1/2) / a, the Morse anharmonicity: the radial shape in xi
+    depends on it alone), ln(1 + q) with q = beta e^(-re/2) 2 m re^2 (the P2 coupling over
+    the rotational constant at re: the angular shape), re, ln m and a; each mapped to
+    [-1, 1] over the sampled parameter box."""
+    p = np.atleast_2d(np.asarray(p, dtype=np.float64))
+    d, a, re, beta, m = p.T
+
+    def raw(d, a, re, beta, m):
+        lam = np.sqrt(2.0 * m * d) / a
+        q = beta * np.exp(-re / 2.0) * 2.0 * m * re * re
+        return np.stack([np.log(lam), np.log1p(q), re, np.log(m), a], axis=1)
+
+    # bounds of each feature over the parameter box (its corners hold the extremes:
+    # every feature is monotone in each parameter)
+    corners = np.array(np.meshgrid(*[[lo, hi] for lo, hi in zip(PARAM_LO, PARAM_HI)])).reshape(5, -1).T
+    fc = raw(*corners.T)
+    lo, hi = fc.min(axis=0), fc.max(axis=0)
+    return (2.0 * (raw(d, a, re, beta, m) - lo) / (hi - lo) - 1.0).astype(np.float32)
 
 
 class Grid2D:
@@ -142,33 +167,57 @@ def ground_states(params, g: Grid2D, tol=1e-10, every=20, max_steps=20000, chunk
     return states, energies, nsteps
 
 
+def well_frame(prm):
+    """Centre and inverse width of the harmonic approximation of the Morse well:
+    xi = (r - re) * s with s = (m omega)^(1/2), omega = a (2 D / m)^(1/2).  In xi the
+    ground states of all parameter sets have nearly the same shape."""
+    d, a, re, _, mass = [float(v) for v in prm]
+    return re, math.sqrt(a * math.sqrt(2.0 * d * mass))
+
+
 class RadialBasis:
-    """Per l: the leading `modes` left singular vectors of the training radial functions."""
+    """Per l: the leading `modes` left singular vectors of the training radial functions,
+    sampled in the well's scaled coordinate xi (well_frame) on a fixed grid, so that the
+    basis describes the shape of a ground state rather than its position and width."""
 
-    def __init__(self, states, g: Grid2D, modes=64):
-        self.modes = modes
-        nl = g.nth
-        psil = np.stack([g.to_l(s.astype(np.float64)) for s in states])  # [count, nr, nl]
-        self.u = np.empty((nl, g.nr, modes))
-        for l in range(nl):
-            x = psil[:, :, l].T  # [nr, count]
-            cov = x @ x.T
-            evals, evecs = np.linalg.eigh(cov)
+    def __init__(self, states, params, g: Grid2D, modes=64, nxi=1024, xi_max=10.0):
+        self.modes, self.g = modes, g
+        self.xi = np.linspace(-xi_max, xi_max, nxi)
+        psil = np.stack([self.to_xi(g.to_l(s.astype(np.float64)), p) for s, p in zip(states, params)])
+        self.u = np.empty((g.nth, nxi, modes))
+        for l in range(g.nth):
+            x = psil[:, :, l].T  # [nxi, count]
+            evals, evecs = np.linalg.eigh(x @ x.T)
             self.u[l] = evecs[:, ::-1][:, :modes]
-        self.g = g
 
-    def coefficients(self, state):
-        psil = self.g.to_l(np.asarray(state, dtype=np.float64))
-        return np.einsum("lrm,rl->lm", self.u, psil)
+    def to_xi(self, psil, prm):  # [nr, nl] on the radial grid -> [nxi, nl] on the xi grid
+        from scipy.interpolate import CubicSpline
+        re, sc = well_frame(prm)
+        r = re + self.xi / sc
+        out = CubicSpline(self.g.r, psil, axis=0)(np.clip(r, self.g.r_min, self.g.r_max))
+        out[(r < self.g.r_min) | (r > self.g.r_max)] = 0.0
+        return out
 
-    def state(self, coef):
-        psil = np.einsum("lrm,lm->rl", self.u, coef)
-        return self.g.to_theta(psil)
+    def from_xi(self, psixi, prm):  # [nxi, nl] -> [nr, nl]
+        from scipy.interpolate import CubicSpline
+        re, sc = well_frame(prm)
+        xi = (self.g.r - re) * sc
+        out = CubicSpline(self.xi, psixi, axis=0)(np.clip(xi, self.xi[0], self.xi[-1]))
+        out[(xi < self.xi[0]) | (xi > self.xi[-1])] = 0.0
+        return out
+
+    def coefficients(self, state, prm):
+        psil = self.to_xi(self.g.to_l(np.asarray(state, dtype=np.float64)), prm)
+        return np.einsum("lxm,xl->lm", self.u, psil)
+
+    def state(self, coef, prm):
+        return self.g.to_theta(self.from_xi(np.einsum("lxm,lm->xl", self.u, coef), prm))
 
 
 class LearnedStart:
-    def __init__(self, basis: RadialBasis, hidden=(256, 256, 256), seed=0):
+    def __init__(self, basis: RadialBasis, hidden=(256, 256, 256), seed=0, features=False):
         self.basis = basis
+        self.inputs = physics_features if features else scale_params
         nout = basis.g.nth * basis.modes
         self.net = so.Mlp([5, *hidden, nout], seed=seed)
         self.mean = None
@@ -177,26 +226,33 @@ class LearnedStart:
     def fit(self, params, states, steps=3000, lr=1e-3, lr_end=None, segments=10):
         """Full-batch Adam; with lr_end the rate falls geometrically from lr to lr_end
         over `segments` equal parts (the optimiser's moments carry across them)."""
-        coef = np.stack([self.basis.coefficients(s).ravel() for s in states])
+        coef = np.stack([self.basis.coefficients(s, p).ravel() for s, p in zip(states, params)])
         self.mean = coef.mean(axis=0)
         self.std = coef.std(axis=0) + 1e-12 * np.abs(coef).max()
         y = ((coef - self.mean) / self.std).astype(np.float32)
-        x = scale_params(params)
+        x = self.inputs(params)
         if lr_end is None or segments <= 1:
             return self.net.train(x, y, steps=steps, lr=lr)
         per = max(1, steps // segments)
         rates = lr * (lr_end / lr) ** (np.arange(segments) / (segments - 1))
         return np.concatenate([self.net.train(x, y, steps=per, lr=float(r)) for r in rates])
 
+    def standardized(self, params, states):
+        """Network output and target, both standardized, for held-out checks."""
+        coef = np.stack([self.basis.coefficients(s, p).ravel() for s, p in zip(states, params)])
+        return self.net.forward(self.inputs(params)).astype(np.float64), (coef - self.mean) / self.std
+
     def predict(self, params):
-        y = self.net.forward(scale_params(params)).astype(np.float64)
+        y = self.net.forward(self.inputs(params)).astype(np.float64)
         coef = y * self.std + self.mean
-        return [self.basis.state(c.reshape(self.basis.g.nth, self.basis.modes)) for c in coef]
+        return [self.basis.state(c.reshape(self.basis.g.nth, self.basis.modes), p) for c, p in zip(coef, params)]
 
 
-def evaluate(model: LearnedStart, params, g: Grid2D, every=5, max_steps=20000, tol=1e-10):
-    """Held-out comparison: plain solver energies E* first, then both starts to |E - E*| <= 1e-8."""
-    _, e_star, steps_plain_full = ground_states(params, g, tol=tol, every=20, max_steps=max_steps)
+def evaluate(model: LearnedStart, params, g: Grid2D, every=5, max_steps=20000, tol=1e-10, diagnose=False):
+    """Held-out comparison: plain solver energies E* first, then both starts to |E - E*| <= 1e-8.
+    diagnose: also relax from the held-out ground states projected on the radial basis (the
+    best start the basis can represent) to separate basis truncation from network error."""
+    true_states, e_star, steps_plain_full = ground_states(params, g, tol=tol, every=20, max_steps=max_steps)
     gauss = [problem(p, g) for p in params]
     _, steps_g, wall_g = relax(gauss, every=every, max_steps=max_steps, target=e_star)
     t0 = time.perf_counter()
@@ -205,7 +261,24 @@ def evaluate(model: LearnedStart, params, g: Grid2D, every=5, max_steps=20000, t
     learned = [problem(p, g, psi0=s) for p, s in zip(params, starts)]
     _, steps_l, wall_l = relax(learned, every=every, max_steps=max_steps, target=e_star)
     wall_l += t_predict  # the network's forward pass and the basis sum are part of the learned start
-    return {"heldout": len(params), "energy_star_mean": float(np.mean(e_star)),
+    extra = {}
+    if diagnose:
+        proj = [model.basis.state(model.basis.coefficients(t, p), p) for t, p in zip(true_states, params)]
+        _, steps_p, wall_p = relax([problem(p, g, psi0=s) for p, s in zip(params, proj)], every=every,
+                                   max_steps=max_steps, target=e_star)
+        err = [np.linalg.norm(s - t) / np.linalg.norm(t) for s, t in zip(starts, true_states)]
+        perr = [np.linalg.norm(s - t) / np.linalg.norm(t) for s, t in zip(proj, true_states)]
+        yh, th = model.standardized(params, true_states)
+        # the isotropic (l = 0) and the anisotropic (l >= 1) parts of the start's error
+        g = model.basis.g
+        iso = [np.linalg.norm(g.to_l(s - t)[:, 0]) / np.linalg.norm(t) for s, t in zip(starts, true_states)]
+        ani = [np.linalg.norm(g.to_l(s - t)[:, 1:]) / np.linalg.norm(t) for s, t in zip(starts, true_states)]
+        extra = {"steps_projection_mean": float(np.mean(steps_p)), "wall_s_projection": wall_p,
+                 "start_rel_l2_learned_median": float(np.median(err)),
+                 "start_rel_l2_projection_median": float(np.median(perr)),
+                 "start_rel_l2_l0_median": float(np.median(iso)), "start_rel_l2_l_ge_1_median": float(np.median(ani)),
+                 "heldout_loss": float(np.mean((yh - th) ** 2))}
+    return {**extra, "heldout": len(params), "energy_star_mean": float(np.mean(e_star)),
             "steps_gaussian_mean": float(np.mean(steps_g)), "steps_learned_mean": float(np.mean(steps_l)),
             "wall_s_gaussian": wall_g, "wall_s_learned": wall_l, "predict_s": t_predict,
             "wall_ratio_learned_over_gaussian": wall_l / wall_g,
@@ -223,6 +296,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=3000)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--lr-end", type=float, default=None)
+    ap.add_argument("--diagnose", action="store_true")
+    ap.add_argument("--features", action="store_true", help="physics features as the network's inputs")
     ap.add_argument("--out", default="learned_start.json")
     a = ap.parse_args()
     g = Grid2D(a.nr, a.nth)
@@ -230,15 +305,15 @@ def main():
     ptrain = param_sets(a.train, 5)
     states, energies, nsteps = ground_states(ptrain, g)
     t_data = time.perf_counter() - t0
-    basis = RadialBasis(states, g, a.modes)
-    model = LearnedStart(basis)
+    basis = RadialBasis(states, ptrain, g, a.modes)
+    model = LearnedStart(basis, features=a.features)
     t0 = time.perf_counter()
     losses = model.fit(ptrain, states, steps=a.epochs, lr=a.lr, lr_end=a.lr_end)
     t_fit = time.perf_counter() - t0
-    res = evaluate(model, param_sets(a.heldout, 6), g)
+    res = evaluate(model, param_sets(a.heldout, 6), g, diagnose=a.diagnose)
     res.update({"train": a.train, "grid": [a.nr, a.nth], "modes": a.modes, "train_loss_first": float(losses[0]),
                 "train_loss_last": float(losses[-1]), "data_generation_s": t_data, "fit_s": t_fit,
-                "epochs": a.epochs, "lr": a.lr, "lr_end": a.lr_end,
+                "epochs": a.epochs, "lr": a.lr, "lr_end": a.lr_end, "features": a.features,
                 "train_steps_mean": float(np.mean(nsteps))})
     with open(a.out, "w") as f:
         json.dump(res, f, indent=1)

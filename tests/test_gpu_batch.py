@@ -66,3 +66,99 @@ def test_batch_graph_path_long_run(so):
     so.Batch(props).steps(steps)
     solo.steps(steps)
     assert rel_l2(props[0].get_array(), solo.get_array()) == 0.0
+
+
+@pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp64"])
+def test_batch_host_arrays_pinned_and_pageable(so, precision):
+    """so_batch_set_arrays / so_batch_get_arrays: page-locked buffers (read and written by
+    the layout kernels directly) and pageable ones (staged copies) give the same states as
+    the per-propagation calls, bit for bit."""
+    torch = pytest.importorskip("torch")
+    from split_operator_gb300 import workloads as W
+    shapes = [(256, 32), (512, 64), (128, 128), (256, 256)]
+    props = [W.radial_angular_2d(nr=nr, nth=nth, step_no=10, seed=300 + k, precision=precision)[0]
+             for k, (nr, nth) in enumerate(shapes)]
+    b = so.Batch(props)
+    rng = np.random.default_rng(11)
+    states = [rng.normal(size=s) + 1j * rng.normal(size=s) for s in shapes]
+
+    # pageable in, pageable out, against the single-propagation calls
+    b.set_arrays(states)
+    got = b.get_arrays()
+    for p, g in zip(props, got):
+        assert np.array_equal(g, p.get_array())
+    if precision == "fp64":
+        for g, s in zip(got, states):
+            assert np.array_equal(g, s)
+    else:
+        for g, s in zip(got, states):
+            assert np.array_equal(g, s.astype(np.complex64).astype(np.complex128))
+
+    # page-locked in and out: same bits
+    pins = [torch.from_numpy(s.view(np.float64).ravel().copy()).pin_memory() for s in states]
+    outs = [torch.empty_like(t).pin_memory() for t in pins]
+    b.set_arrays_ptr([t.data_ptr() for t in pins])
+    b.get_arrays_ptr([t.data_ptr() for t in outs])
+    for o, g in zip(outs, got):
+        assert np.array_equal(o.numpy().view(np.complex128).reshape(g.shape), g)
+
+    # and a step from a pinned start equals a step from a pageable start
+    b.set_arrays_ptr([t.data_ptr() for t in pins])
+    b.steps(2)
+    after_pinned = b.get_arrays()
+    b.set_arrays(states)
+    b.steps(2)
+    for a, c in zip(after_pinned, b.get_arrays()):
+        assert np.array_equal(a, c)
+    with pytest.raises(Exception):
+        b.set_arrays_ptr([t.data_ptr() for t in pins[:-1]])  # count differs from the batch size
+
+
+@pytest.mark.parametrize("precision", ["fp32_simt", "fp64"])
+def test_single_host_array_ragged_transpose_tiles(so, precision):
+    """A radial x angular state whose extents are not multiples of the 32 x 32 transpose
+    tile: pinned and pageable buffers through so_propagation_set_array / get_array."""
+    torch = pytest.importorskip("torch")
+    from split_operator_gb300 import workloads as W
+    nr, nth = 300, 17
+    p = W.radial_angular_2d(nr=nr, nth=nth, step_no=10, seed=5, precision=precision)[0]
+    rng = np.random.default_rng(12)
+    s = rng.normal(size=(nr, nth)) + 1j * rng.normal(size=(nr, nth))
+    want = s if precision == "fp64" else s.astype(np.complex64).astype(np.complex128)
+    p.set_array(s)
+    assert np.array_equal(p.get_array(), want)
+    pin = torch.from_numpy(s.view(np.float64).ravel().copy()).pin_memory()
+    out = torch.zeros_like(pin).pin_memory()
+    p.set_array(np.zeros_like(s))
+    p.set_array_ptr(pin.data_ptr())
+    p.get_array_ptr(out.data_ptr())
+    assert np.array_equal(out.numpy().view(np.complex128).reshape(nr, nth), want)
+
+
+def test_batch_steps_host_pipeline_equals_separate_calls(so):
+    """so_batch_steps_host (chunked, overlapped copies) gives the same states and losses as
+    set_arrays + steps + get_arrays, bit for bit; in and out may be the same buffers."""
+    torch = pytest.importorskip("torch")
+    from split_operator_gb300 import workloads as W
+    shapes = [(256, 32), (512, 64), (128, 128), (256, 256), (512, 32), (256, 64)]
+    mk = lambda: [W.radial_angular_2d(nr=nr, nth=nth, step_no=10, seed=400 + k, precision="fp32_tf32x3")[0]
+                  for k, (nr, nth) in enumerate(shapes)]
+    pa, pb = mk(), mk()
+    ba, bb = so.Batch(pa), so.Batch(pb)
+    rng = np.random.default_rng(13)
+    states = [rng.normal(size=s) + 1j * rng.normal(size=s) for s in shapes]
+    pins = [torch.from_numpy(s.view(np.float64).ravel().copy()).pin_memory() for s in states]
+    outs = [torch.empty_like(t).pin_memory() for t in pins]
+    ba.steps_host_ptr([t.data_ptr() for t in pins], [t.data_ptr() for t in outs], 3)
+    bb.set_arrays(states)
+    bb.steps(3)
+    want = bb.get_arrays()
+    for o, w in zip(outs, want):
+        assert np.array_equal(o.numpy().view(np.complex128).reshape(w.shape), w)
+    for x, y in zip(pa, pb):
+        assert x.all_losses() == y.all_losses()
+    # in place: the outputs of one call are the inputs of the next
+    ba.steps_host_ptr([t.data_ptr() for t in outs], [t.data_ptr() for t in outs], 2)
+    bb.steps(2)
+    for o, w in zip(outs, bb.get_arrays()):
+        assert np.array_equal(o.numpy().view(np.complex128).reshape(w.shape), w)
