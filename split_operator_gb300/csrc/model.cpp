@@ -3,6 +3,9 @@
 // norm cache, loss bookkeeping and representation swaps happen exactly where
 // the reference does them; every array touch becomes an emitted device op.
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -1425,6 +1428,10 @@ void Batch::run_groups(std::vector<Group>& gs) {
 
 void Batch::steps(uint64_t n, bool wait) {
   if (n == 0) return;
+  static const bool trace = std::getenv("SO_PIPE_TRACE") != nullptr;
+  const auto t0 = std::chrono::steady_clock::now();
+  auto ms = [&] { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); };
+  double t_sync = 0.0, t_rec = 0.0, t_groups = 0.0;
   {
     std::vector<cudaStream_t> seen;  // each member's queued work, then one wait per stream
     for (Propagation* p : props_) {
@@ -1433,10 +1440,12 @@ void Batch::steps(uint64_t n, bool wait) {
     }
     for (cudaStream_t st : seen) cuda_check(cudaStreamSynchronize(st), "stream sync");
   }
+  t_sync = ms();
   // Host logic of two steps per propagation: passes [head, period..., tail] where the
   // period (the middle passes) repeats for every further step.
   std::vector<std::vector<RecordedPass>> rec;
   for (Propagation* p : props_) rec.push_back(p->record_steps(2));
+  t_rec = ms();
   const size_t np = rec[0].size();
   for (const auto& r : rec)
     if (r.size() != np || np < 2)
@@ -1476,6 +1485,7 @@ void Batch::steps(uint64_t n, bool wait) {
     cached_rec_ = std::move(rec);
   }
   std::vector<std::vector<Group>>& pos = cached_pos_;
+  t_groups = ms();
   launches_per_step_ = 0;
   for (size_t i = per0; i < per0 + m; ++i) launches_per_step_ += pos[i].size();
   // first step (head)
@@ -1503,6 +1513,9 @@ void Batch::steps(uint64_t n, bool wait) {
   // tail: the last step's closing passes (merged form only)
   if (merged)
     for (size_t i = m + 1; i < np; ++i) run_groups(pos[i]);
+  if (trace)
+    std::fprintf(stderr, "batch steps(%llu) of %zu: sync %.3f record %.3f groups%s %.3f launched %.3f ms\n",
+                 (unsigned long long)n, props_.size(), t_sync, t_rec, reuse ? " (reused)" : "", t_groups, ms());
   if (wait) cuda_check(cudaStreamSynchronize(stream_), "batch sync");
 }
 
@@ -1570,22 +1583,41 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
       cuda_check(cudaStreamSynchronize(own[i]), "stream sync");
   for (Chunk& ch : chunks_)
     for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->engine().stream = ch.stream;
+  // SO_PIPE_TRACE=1: host-side time of each phase of the call on stderr
+  static const bool trace = std::getenv("SO_PIPE_TRACE") != nullptr;
+  auto now = [] { return std::chrono::steady_clock::now(); };
+  std::vector<std::pair<std::string, double>> marks;
+  const auto t0 = now();
+  auto mark = [&](const std::string& what) {
+    if (trace) marks.emplace_back(what, std::chrono::duration<double, std::milli>(now() - t0).count());
+  };
   try {
     // imports on the copy engines (host link H2D) for every chunk, then per chunk its steps
     // and its exports (copy engines, D2H), all queued on the chunk's stream: chunk c's steps
     // run while later chunks arrive and earlier ones leave
     for (Chunk& ch : chunks_)
       for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->set_array(in[i], true);
+    mark("imports queued");
     for (Chunk& ch : chunks_) {
       ch.batch->steps(n, false);  // queued; the host moves on to the next chunk
+      mark("chunk steps queued");
       for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->get_array(out[i], false, true);
+      mark("chunk exports queued");
     }
-    for (Chunk& ch : chunks_) cuda_check(cudaStreamSynchronize(ch.stream), "chunk sync");
+    for (Chunk& ch : chunks_) {
+      cuda_check(cudaStreamSynchronize(ch.stream), "chunk sync");
+      mark("chunk done");
+    }
   } catch (...) {
     for (size_t i = 0; i < m; ++i) props_[i]->engine().stream = own[i];
     throw;
   }
   for (size_t i = 0; i < m; ++i) props_[i]->engine().stream = own[i];
+  if (trace) {
+    std::string line = "steps_host:";
+    for (const auto& mk : marks) line += " " + mk.first + " " + std::to_string(mk.second) + " ms;";
+    std::fprintf(stderr, "%s\n", line.c_str());
+  }
 }
 
 std::string Batch::kernel_times() {

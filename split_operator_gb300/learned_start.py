@@ -215,9 +215,10 @@ class RadialBasis:
 
 
 class LearnedStart:
-    def __init__(self, basis: RadialBasis, hidden=(256, 256, 256), seed=0, features=False):
+    def __init__(self, basis: RadialBasis, hidden=(256, 256, 256), seed=0, features=False, scaling="channel"):
         self.basis = basis
         self.inputs = physics_features if features else scale_params
+        self.scaling = scaling
         nout = basis.g.nth * basis.modes
         self.net = so.Mlp([5, *hidden, nout], seed=seed)
         self.mean = None
@@ -228,7 +229,15 @@ class LearnedStart:
         over `segments` equal parts (the optimiser's moments carry across them)."""
         coef = np.stack([self.basis.coefficients(s, p).ravel() for s, p in zip(states, params)])
         self.mean = coef.mean(axis=0)
-        self.std = coef.std(axis=0) + 1e-12 * np.abs(coef).max()
+        if self.scaling == "channel":
+            # one scale per l channel (the RMS spread of its modes): within a channel the
+            # modes keep their physical weights, so the loss does not inflate modes that only
+            # carry rounding noise of the training states
+            sd = coef.std(axis=0).reshape(self.basis.g.nth, self.basis.modes)
+            self.std = np.repeat(np.sqrt(np.mean(sd ** 2, axis=1)), self.basis.modes)
+        else:
+            self.std = coef.std(axis=0)
+        self.std = self.std + 1e-12 * np.abs(coef).max()
         y = ((coef - self.mean) / self.std).astype(np.float32)
         x = self.inputs(params)
         if lr_end is None or segments <= 1:
@@ -298,6 +307,8 @@ def main():
     ap.add_argument("--lr-end", type=float, default=None)
     ap.add_argument("--diagnose", action="store_true")
     ap.add_argument("--features", action="store_true", help="physics features as the network's inputs")
+    ap.add_argument("--scaling", default="channel", choices=["channel", "coef"],
+                    help="standardise the targets per l channel or per coefficient")
     ap.add_argument("--out", default="learned_start.json")
     a = ap.parse_args()
     g = Grid2D(a.nr, a.nth)
@@ -306,14 +317,14 @@ def main():
     states, energies, nsteps = ground_states(ptrain, g)
     t_data = time.perf_counter() - t0
     basis = RadialBasis(states, ptrain, g, a.modes)
-    model = LearnedStart(basis, features=a.features)
+    model = LearnedStart(basis, features=a.features, scaling=a.scaling)
     t0 = time.perf_counter()
     losses = model.fit(ptrain, states, steps=a.epochs, lr=a.lr, lr_end=a.lr_end)
     t_fit = time.perf_counter() - t0
     res = evaluate(model, param_sets(a.heldout, 6), g, diagnose=a.diagnose)
     res.update({"train": a.train, "grid": [a.nr, a.nth], "modes": a.modes, "train_loss_first": float(losses[0]),
                 "train_loss_last": float(losses[-1]), "data_generation_s": t_data, "fit_s": t_fit,
-                "epochs": a.epochs, "lr": a.lr, "lr_end": a.lr_end, "features": a.features,
+                "epochs": a.epochs, "lr": a.lr, "lr_end": a.lr_end, "features": a.features, "scaling": a.scaling,
                 "train_steps_mean": float(np.mean(nsteps))})
     with open(a.out, "w") as f:
         json.dump(res, f, indent=1)
