@@ -112,6 +112,12 @@ __host__ __device__ inline int64_t stage_twiddle_exponent(int64_t e, int64_t n, 
   return 0;
 }
 __host__ __device__ inline bool stage_twiddles(int64_t n) { return n >= 16 && (n & (n - 1)) == 0; }
+// A pass copies its twiddle table into shared memory, except for power-of-two lanes in tiles
+// of fewer than 4 lanes: there the copy would cost a load and a store per point, and the
+// stages read their consecutive table slices straight through L1 / L2 instead.
+__host__ __device__ inline bool twiddles_in_smem(const Geometry& g) {
+  return !(stage_twiddles(g.n) && g.lanes_per_tile < 4);
+}
 
 // Host launchers (lane_sweep.cu)
 cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);

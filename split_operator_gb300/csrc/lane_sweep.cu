@@ -477,9 +477,10 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
       }
     }
   }
-  // twiddles in shared memory (stage-major for the Stockham stages: consecutive reads)
+  // twiddles in shared memory (stage-major for the Stockham stages: consecutive reads), or
+  // read from the cached global table when the tile has few lanes
   const C* tw = reinterpret_cast<const C*>(p.twiddle);
-  if (tw) {
+  if (tw && twiddles_in_smem(g)) {
     for (int k = tid; k < n; k += T) tw_s[k] = tw[k];
     tw = tw_s;
   }
@@ -753,7 +754,7 @@ size_t pass_smem_bytes(const PassParams& p, bool fp64) {
   size_t b = (p.one_buffer ? 1 : 2) * (((size_t)g.lanes_per_tile * g.lane_stride * cs + 15) & ~(size_t)15);
   b += (size_t)g.lanes_per_tile * (sizeof(int64_t) + sizeof(double) + kMaxDims * sizeof(int) + sizeof(int));
   b = (b + 15) & ~(size_t)15;
-  if (fft) b += (size_t)g.n * cs;
+  if (fft && twiddles_in_smem(g)) b += (size_t)g.n * cs;
   return b;
 }
 

@@ -729,6 +729,38 @@ void Engine::export_host(double* host, bool sync, bool copy_engine) {
   if (sync) cuda_check(cudaStreamSynchronize(stream), "export sync");
 }
 
+// The two halves of a staged copy-engine import / export, for callers that order the
+// copies (copy engines) and the layout kernels (SMs) separately.
+void Engine::stage_in(const double* host) {
+  flush();
+  const size_t b = points() * 16;
+  if (fp64 && identity_perm(perm)) {
+    cuda_check(cudaMemcpyAsync(psi.ptr, host, b, cudaMemcpyHostToDevice, stream), "import copy");
+    return;
+  }
+  if (staging_.bytes < b) staging_ = DeviceBuffer(b);
+  cuda_check(cudaMemcpyAsync(staging_.ptr, host, b, cudaMemcpyHostToDevice, stream), "import copy");
+}
+
+void Engine::unstage_in() {
+  if (fp64 && identity_perm(perm)) return;
+  cuda_check(launch_import(psi.ptr, fp64, staging_.as<double>(), flat_geometry(*this), stream), "import");
+}
+
+void Engine::stage_out() {
+  flush();
+  if (fp64 && identity_perm(perm)) return;
+  const size_t b = points() * 16;
+  if (staging_.bytes < b) staging_ = DeviceBuffer(b);
+  cuda_check(launch_export(staging_.as<double>(), psi.ptr, fp64, flat_geometry(*this), stream), "export");
+}
+
+void Engine::unstage_out(double* host) {
+  const size_t b = points() * 16;
+  const void* src = (fp64 && identity_perm(perm)) ? psi.ptr : staging_.ptr;
+  cuda_check(cudaMemcpyAsync(host, src, b, cudaMemcpyDeviceToHost, stream), "export copy");
+}
+
 // ----------------------------------------------------------------- WaveFunction
 WaveFunction::WaveFunction(const std::vector<size_t>& shp, const std::vector<Grid>& g, const std::vector<int>& perm,
                            bool fp64)
@@ -1346,6 +1378,9 @@ Batch::~Batch() {
     ch.batch.reset();
     cudaStreamSynchronize(ch.stream);
     cudaStreamDestroy(ch.stream);
+    cudaEventDestroy(ch.in_done);
+    cudaEventDestroy(ch.out_done);
+    cudaEventDestroy(ch.sm_done);
   }
   for (Timed& t : timed_) {
     cudaEventDestroy(t.a);
@@ -1426,7 +1461,7 @@ void Batch::run_groups(std::vector<Group>& gs) {
   }
 }
 
-void Batch::steps(uint64_t n, bool wait) {
+void Batch::steps(uint64_t n, bool wait, bool sync_members) {
   if (n == 0) return;
   static const bool trace = std::getenv("SO_PIPE_TRACE") != nullptr;
   const auto t0 = std::chrono::steady_clock::now();
@@ -1438,7 +1473,12 @@ void Batch::steps(uint64_t n, bool wait) {
       p->engine().flush();
       if (std::find(seen.begin(), seen.end(), p->engine().stream) == seen.end()) seen.push_back(p->engine().stream);
     }
-    for (cudaStream_t st : seen) cuda_check(cudaStreamSynchronize(st), "stream sync");
+    // members on the batch's own stream are ordered by the stream itself
+    if (sync_members)
+      for (cudaStream_t st : seen) cuda_check(cudaStreamSynchronize(st), "stream sync");
+    else
+      for (cudaStream_t st : seen)
+        if (st != stream_) cuda_check(cudaStreamSynchronize(st), "stream sync");
   }
   t_sync = ms();
   // Host logic of two steps per propagation: passes [head, period..., tail] where the
@@ -1560,6 +1600,9 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
       ch.first = first;
       ch.count = last - first;
       cuda_check(cudaStreamCreateWithFlags(&ch.stream, cudaStreamNonBlocking), "chunk stream");
+      cuda_check(cudaEventCreateWithFlags(&ch.in_done, cudaEventDisableTiming), "chunk event");
+      cuda_check(cudaEventCreateWithFlags(&ch.out_done, cudaEventDisableTiming), "chunk event");
+      cuda_check(cudaEventCreateWithFlags(&ch.sm_done, cudaEventDisableTiming), "chunk event");
       std::vector<Propagation*> sub(props_.begin() + first, props_.begin() + last);
       std::vector<cudaStream_t> saved;
       for (Propagation* p : sub) {
@@ -1592,17 +1635,34 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
     if (trace) marks.emplace_back(what, std::chrono::duration<double, std::milli>(now() - t0).count());
   };
   try {
-    // imports on the copy engines (host link H2D) for every chunk, then per chunk its steps
-    // and its exports (copy engines, D2H), all queued on the chunk's stream: chunk c's steps
-    // run while later chunks arrive and earlier ones leave
-    for (Chunk& ch : chunks_)
-      for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->set_array(in[i], true);
-    mark("imports queued");
-    for (Chunk& ch : chunks_) {
-      ch.batch->steps(n, false);  // queued; the host moves on to the next chunk
+    // Copy engines: every chunk's states in (host link H2D), in chunk order; later each
+    // chunk's states out (D2H), in chunk order.  SMs, in chunk order: the chunk's layout
+    // kernels in, its steps, its layout kernels out.  So chunk c computes while later
+    // chunks arrive and earlier ones leave, and the link carries both directions at once.
+    // (Interleaved copies would make every chunk arrive only when all had; a layout kernel
+    // queued between two copies would hold the copy engine behind the SMs.)
+    for (size_t c = 0; c < chunks_.size(); ++c) {
+      Chunk& ch = chunks_[c];
+      if (c > 0) cuda_check(cudaStreamWaitEvent(ch.stream, chunks_[c - 1].in_done, 0), "chunk order");
+      for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->engine().stage_in(in[i]);
+      cuda_check(cudaEventRecord(ch.in_done, ch.stream), "chunk event");
+    }
+    mark("copies in queued");
+    for (size_t c = 0; c < chunks_.size(); ++c) {
+      Chunk& ch = chunks_[c];
+      if (c > 0) cuda_check(cudaStreamWaitEvent(ch.stream, chunks_[c - 1].sm_done, 0), "chunk order");
+      for (size_t i = ch.first; i < ch.first + ch.count; ++i) {
+        props_[i]->engine().unstage_in();
+        props_[i]->state_replaced();
+      }
+      ch.batch->steps(n, false, false);  // queued behind the chunk's imports; no host wait
+      for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->engine().stage_out();
+      cuda_check(cudaEventRecord(ch.sm_done, ch.stream), "chunk event");
       mark("chunk steps queued");
-      for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->get_array(out[i], false, true);
-      mark("chunk exports queued");
+      if (c > 0) cuda_check(cudaStreamWaitEvent(ch.stream, chunks_[c - 1].out_done, 0), "chunk order");
+      for (size_t i = ch.first; i < ch.first + ch.count; ++i) props_[i]->engine().unstage_out(out[i]);
+      cuda_check(cudaEventRecord(ch.out_done, ch.stream), "chunk event");
+      mark("chunk copies out queued");
     }
     for (Chunk& ch : chunks_) {
       cuda_check(cudaStreamSynchronize(ch.stream), "chunk sync");

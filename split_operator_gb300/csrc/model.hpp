@@ -155,6 +155,11 @@ class Engine {
   // logical complex128 -> storage; copy_engine: staged cudaMemcpyAsync even for page-locked
   // memory (no SMs busy on the host link, so the copy overlaps kernels of other streams)
   void import_host(const double* host, bool copy_engine = false);
+  // import_host / export_host split at the staging buffer: copy engine and SM halves
+  void stage_in(const double* host);
+  void unstage_in();
+  void stage_out();
+  void unstage_out(double* host);
   void export_host(double* host, bool sync = true, bool copy_engine = false);  // storage -> logical complex128
   void check_nonfinite();
 
@@ -395,6 +400,7 @@ class Propagation {
   // sync false: queued on the engine stream; copy_engine: staged through cudaMemcpyAsync
   void get_array(double* out, bool sync = true, bool copy_engine = false);
   void set_array(const double* in, bool copy_engine = false);
+  void state_replaced() { wf_->possible_norm_change = true; }  // after a direct engine import
   double norm();
   std::string describe();
   void set_stream(cudaStream_t s) { wf_->eng->stream = s; }
@@ -424,7 +430,8 @@ class Batch {
   explicit Batch(std::vector<Propagation*> props);
   ~Batch();
   // wait false: return once the launches are queued (the batch's stream runs them)
-  void steps(uint64_t n, bool wait = true);
+  // sync_members false: members whose stream is the batch's are not waited on by the host
+  void steps(uint64_t n, bool wait = true, bool sync_members = true);
   void set_timing(bool on) { timing_ = on; }
   std::string kernel_times();
   size_t launches_per_step() const { return launches_per_step_; }
@@ -454,6 +461,8 @@ class Batch {
   struct Chunk {
     size_t first = 0, count = 0;
     cudaStream_t stream = nullptr;
+    // the chunk's copies in, its SM work (layout kernels, steps) and its copies out are done
+    cudaEvent_t in_done = nullptr, sm_done = nullptr, out_done = nullptr;
     std::unique_ptr<Batch> batch;
   };
   std::vector<Chunk> chunks_;  // steps_host pipeline (built on first use)
