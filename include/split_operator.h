@@ -70,6 +70,11 @@ const char* so_last_error(void);
 int so_version(void);
 /* Kernels this library has launched since load (all devices, all handles). */
 int so_launch_count(uint64_t* out);
+/* Failure-detection self-test (no reference counterpart): one CTA waits on a tensor-core
+ * pipeline barrier that nothing completes, with the kernel's two bounded wait forms and a
+ * limit of limit_ns each.  out[0], out[1]: 1 if the wait gave up as intended; out[2]: the
+ * elapsed device time in ns.  The context stays usable afterwards. */
+int so_selftest_bounded_wait(uint64_t limit_ns, uint64_t* out);
 
 /* ---- Grid: grid.rs:14-89 ------------------------------------------------ */
 /* grid.rs:24-48 */

@@ -34,6 +34,7 @@ _STR = C.c_char_p
 SIGNATURES = {
     "so_version": [],
     "so_launch_count": [C.POINTER(C.c_uint64)],
+    "so_selftest_bounded_wait": [C.c_uint64, C.POINTER(C.c_uint64)],
     "so_grid_new_linear_continuos": [_STR, _D, _D, _S, _S, _PP],
     "so_grid_new_linear_countable": [_STR, _D, _D, _S, _S, _PP],
     "so_grid_new_custom": [_STR, _DP, _DP, _S, _S, _PP],

@@ -767,6 +767,14 @@ class Mlp(_Handle):
         return losses
 
 
+def selftest_bounded_wait(limit_ns: int):
+    """(try_wait form timed out, polling form timed out, elapsed ns) of a device wait on a
+    barrier that nothing completes."""
+    out = (C.c_uint64 * 3)()
+    call("so_selftest_bounded_wait", limit_ns, out)
+    return bool(out[0]), bool(out[1]), int(out[2])
+
+
 def launch_count() -> int:
     v = C.c_uint64()
     call("so_launch_count", C.byref(v))

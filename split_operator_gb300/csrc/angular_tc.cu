@@ -1205,6 +1205,42 @@ void angular_tc_parity_images(const double* m, int n, int kind, bool bf, std::ve
 
 int angular_tc_trace_slots() { return kTraceSlots; }
 
+// Self-test of the bounded waits: one CTA waits on an mbarrier that nothing arrives at, with
+// both wait forms of the tensor-core kernel (suspend-hinted try_wait and plain polling), and
+// reports whether each gave up: out[0], out[1] = 1 when the wait timed out as intended,
+// out[2] = elapsed ns.  The barrier is completed afterwards, so nothing is left waiting.
+__global__ void bounded_wait_selftest_kernel(uint64_t limit_ns, unsigned long long* out) {
+  using namespace tc;
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint64_t t0 = globaltimer_ns();
+    const bool a = mbar_wait(&bar, 0u, limit_ns);
+    const bool b = mbar_poll(&bar, 0u, limit_ns);
+    out[0] = a ? 0ull : 1ull;
+    out[1] = b ? 0ull : 1ull;
+    out[2] = globaltimer_ns() - t0;
+    mbar_arrive(&bar);
+  }
+  __syncthreads();
+}
+
+cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_out) {
+  unsigned long long* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, 3 * sizeof(unsigned long long));
+  if (e != cudaSuccess) return e;
+  bounded_wait_selftest_kernel<<<1, 32>>>(limit_ns, d);
+  count_launch();
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e;
+}
+
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
                               int error_slot, const int* parity, bool bf, cudaStream_t s,
                               unsigned long long* trace) {

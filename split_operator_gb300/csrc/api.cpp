@@ -106,6 +106,15 @@ int so_launch_count(uint64_t* out) {
     *out = so::launch_count();
   });
 }
+int so_selftest_bounded_wait(uint64_t limit_ns, uint64_t* out) {
+  return guard([&] {
+    need(out, "null out");
+    need(limit_ns > 0 && limit_ns <= 1000000000ull, "limit must be in (0, 1 s]");
+    unsigned long long r[3] = {0, 0, 0};
+    so::cuda_check(so::bounded_wait_selftest(limit_ns, r), "bounded-wait self-test");
+    for (int k = 0; k < 3; ++k) out[k] = r[k];
+  });
+}
 
 // ---------------------------------------------------------------------- grid
 int so_grid_new_linear_continuos(const char* name, double start, double end, size_t n, size_t dim, so_grid* out) {

@@ -144,6 +144,9 @@ cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, 
                               int error_slot, const int* parity, bool bf, cudaStream_t s,
                               unsigned long long* trace = nullptr);
 int angular_tc_trace_slots();
+// one CTA waits (limit_ns, both wait forms) on an mbarrier nothing completes; out[3]:
+// timed out (try_wait form), timed out (polling form), elapsed ns
+cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_out);
 
 // Batched launches over many propagations' passes (block -> (instance, tile) by offsets)
 cudaError_t launch_pass_batched(bool fp64, bool sweep, const PassParams* params_dev, const int64_t* offsets_dev,
