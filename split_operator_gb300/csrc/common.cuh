@@ -86,28 +86,50 @@ struct PassParams {
   int32_t nonfinite_slot;       // slot set to 1 if a norm is not finite
   int32_t one_buffer;           // 1: no op needs the second tile buffer (FFT stages run in place)
   int32_t sweep;                // 1: only point-wise ops, norms, scalars and power-of-two FFTs
+  int32_t fused;                // 1: an FFT pair with point-wise ops, run by fft_pair_kernel
   DevOp ops[kMaxOps];
 };
 
-// Twiddle table of a power-of-two lane FFT (n >= 16) in stage-major order: the Stockham
-// stages run radix rmax (16 FP32, 8 FP64) and one smaller closing radix; stage (RS, p)
+// Radix sequence of the Stockham stages of a power-of-two lane FFT: rmax while at least
+// rmax points remain, then one smaller closing radix; `reversed` lists it backwards.
+// Returns the number of stages (at most 13).
+__host__ __device__ inline int fft_radices(int64_t n, int rmax, bool reversed, int* rs) {
+  int c = 0;
+  for (int64_t p = 1; p < n;) {
+    const int64_t r = n / p >= rmax ? rmax : n / p;
+    rs[c++] = (int)r;
+    p *= r;
+  }
+  if (reversed)
+    for (int a = 0, b = c - 1; a < b; ++a, --b) {
+      const int t = rs[a];
+      rs[a] = rs[b];
+      rs[b] = t;
+    }
+  return c;
+}
+
+// Twiddle table of a power-of-two lane FFT (n >= 16) in stage-major order: stage (RS, p)
 // with p > 1 owns (RS - 1) * p consecutive entries, entry (r - 1) * p + k holding
 // w^(r k n / (RS p)), w = exp(-2 pi i / n).  Threads of a stage read consecutive k, so the
-// shared-memory reads are free of bank conflicts.  Returns the exponent of entry e
-// (0 past the end of the table; the table occupies at most n entries).
-__host__ __device__ inline int64_t stage_twiddle_exponent(int64_t e, int64_t n, int rmax) {
+// shared-memory reads are free of bank conflicts.  Returns the exponent of entry e for the
+// stages in fft_radices order (0 past the end: a table occupies at most n entries).  The
+// device table holds the forward order in entries [0, n) and the reversed order in [n, 2n).
+__host__ __device__ inline int64_t stage_twiddle_exponent(int64_t e, int64_t n, int rmax, bool reversed = false) {
+  int rs[16];
+  const int c = fft_radices(n, rmax, reversed, rs);
   int64_t p = 1, off = 0;
-  while (p < n) {
-    const int64_t rs = n / p >= rmax ? rmax : n / p;
+  for (int s = 0; s < c; ++s) {
+    const int64_t r_s = rs[s];
     if (p > 1) {
-      const int64_t cnt = (rs - 1) * p;
+      const int64_t cnt = (r_s - 1) * p;
       if (e < off + cnt) {
         const int64_t q = e - off, r = q / p + 1, k = q - (r - 1) * p;
-        return r * k * (n / (rs * p));
+        return r * k * (n / (r_s * p));
       }
       off += cnt;
     }
-    p *= rs;
+    p *= r_s;
   }
   return 0;
 }
@@ -118,6 +140,12 @@ __host__ __device__ inline bool stage_twiddles(int64_t n) { return n >= 16 && (n
 __host__ __device__ inline bool twiddles_in_smem(const Geometry& g) {
   return !(stage_twiddles(g.n) && g.lanes_per_tile < 4);
 }
+
+// FFT pair pass (lane_sweep.cu): [FFT] [DIAG1D along / DIAGND]* [FFT] [DIAG1D along / DIAGND]*
+// over contiguous power-of-two FP32 lanes, every thread holding 16 values in registers.
+// fft_pair_plan checks the pass and sets its tiling (lanes per tile, tiles) and p.fused.
+bool fft_pair_plan(PassParams& p, bool fp64, bool resident);
+int fft_pair_threads(const Geometry& g);
 
 // Host launchers (lane_sweep.cu)
 cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);
@@ -149,8 +177,9 @@ int angular_tc_trace_slots();
 cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_out);
 
 // Batched launches over many propagations' passes (block -> (instance, tile) by offsets)
-cudaError_t launch_pass_batched(bool fp64, bool sweep, const PassParams* params_dev, const int64_t* offsets_dev,
-                                int count, int64_t blocks, int threads, size_t smem, cudaStream_t s);
+cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassParams* params_dev,
+                                const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
+                                cudaStream_t s);
 size_t tc_params_bytes();
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
                     const int* parity, void* out);

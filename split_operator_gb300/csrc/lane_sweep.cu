@@ -694,6 +694,249 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
   }
 }
 
+// ------------------------------------------------------------------ FFT pair pass
+// [FFT] [point-wise ops] [FFT] [point-wise ops] over L contiguous FP32 lanes of n points
+// (power of two, 16 .. 8192): the 2-D step's radial pass (F, K, F^-1, Rot/2).  Every
+// thread holds kPairV = 16 values (L n = 16 T) and runs 16 / RS butterflies of each
+// radix-RS stage, b = t + j T, so a stage can run in place in one shared buffer (read,
+// barrier, compute, write, barrier).  The first FFT's first stage (p = 1) reads global
+// memory directly, its last stage keeps its outputs in registers (index k + q p_last of
+// butterfly k), the point-wise ops between the FFTs run on them, and the second FFT runs
+// its radices in the reverse order, so that its first stage's inputs (i + r nb, nb = n /
+// RS) are exactly those registers.  Its last stage applies the closing point-wise ops and
+// writes global memory directly.  Twiddles come from the stage-major table (forward order
+// in [0, n), reversed order in [n, 2n)) through L1.  Compared with the general pass this
+// drops the tile load and store through shared memory, the shared-memory round trips of
+// both FFTs' outer stages and of the point-wise ops, and the second tile buffer.
+constexpr int kPairV = 16;
+
+template <int RS>
+__device__ __forceinline__ void pair_load_smem(float2 (&v)[kPairV], const float2* buf, int t, int T, int lgnb,
+                                               int ls) {
+  const int nb = 1 << lgnb;
+#pragma unroll
+  for (int j = 0; j < kPairV / RS; ++j) {
+    const int b = t + j * T, l = b >> lgnb, i = b & (nb - 1);
+#pragma unroll
+    for (int r = 0; r < RS; ++r) v[j * RS + r] = buf[sidx(l, i + r * nb, ls)];
+  }
+}
+
+template <int RS>
+__device__ __forceinline__ void pair_store_smem(const float2 (&v)[kPairV], float2* buf, int t, int T, int lgnb,
+                                                int p, int ls) {
+  const int nb = 1 << lgnb;
+#pragma unroll
+  for (int j = 0; j < kPairV / RS; ++j) {
+    const int b = t + j * T, l = b >> lgnb, i = b & (nb - 1), k = i & (p - 1);
+    const int base = (i - k) * RS + k;
+#pragma unroll
+    for (int q = 0; q < RS; ++q) buf[sidx(l, base + q * p, ls)] = v[j * RS + q];
+  }
+}
+
+// first stage (p = 1) inputs straight from the lanes in global memory (invalid lanes: 0)
+// (psi: the tile's first lane; nl: its valid lanes; offsets within a tile fit 32 bits)
+template <int RS>
+__device__ __forceinline__ void pair_load_global(float2 (&v)[kPairV], const float2* __restrict__ psi, int t, int T,
+                                                 int lgnb, int nl, int n) {
+  const int nb = 1 << lgnb;
+#pragma unroll
+  for (int j = 0; j < kPairV / RS; ++j) {
+    const int b = t + j * T, l = b >> lgnb, i = b & (nb - 1);
+    const int o = l * n + i;
+#pragma unroll
+    for (int r = 0; r < RS; ++r) v[j * RS + r] = l < nl ? psi[o + r * nb] : float2{0.f, 0.f};
+  }
+}
+
+template <int RS>
+__device__ __forceinline__ void pair_butterflies(float2 (&v)[kPairV], int t, int T, int lgnb, int p, int dir,
+                                                 const float2* __restrict__ tw) {
+  const int nb = 1 << lgnb;
+#pragma unroll
+  for (int j = 0; j < kPairV / RS; ++j) {
+    const int b = t + j * T, i = b & (nb - 1), k = i & (p - 1);
+    if (k > 0) {
+#pragma unroll
+      for (int r = 1; r < RS; ++r) {
+        float2 w = __ldg(tw + (r - 1) * p + k);
+        if (dir > 0) w.y = -w.y;
+        v[j * RS + r] = cmul(v[j * RS + r], w);
+      }
+    }
+    dft_r<RS>(&v[j * RS], dir);
+  }
+}
+
+// point-wise ops [ob, oe) on the outputs of a last stage: value j RS + q sits at lane
+// b >> lgnb, point x = k + q p with k = b & (p - 1), p = 2^lgnb
+template <int RS>
+__device__ __forceinline__ void pair_pointwise(float2 (&v)[kPairV], const PassParams& pp, int ob, int oe, int t,
+                                               int T, int lgnb, int64_t lane0, int nl, float sc) {
+  const int p = 1 << lgnb, n = (int)pp.g.n;
+#pragma unroll
+  for (int e = 0; e < kPairV; ++e) v[e] = float2{v[e].x * sc, v[e].y * sc};
+  for (int oi = ob; oi < oe; ++oi) {
+    const DevOp& op = pp.ops[oi];
+    const bool nd = op.kind == OP_DIAGND;
+    // DIAGND: the tile's rows of the full table; DIAG1D along the lane: the lane table
+    const float2* tab = reinterpret_cast<const float2*>(op.ptr) + (nd ? lane0 * n : 0);
+#pragma unroll
+    for (int j = 0; j < kPairV / RS; ++j) {
+      const int b = t + j * T, l = b >> lgnb, k = b & (p - 1);
+      if (!nd || l < nl) {
+        const int row = nd ? l * n : 0;
+#pragma unroll
+        for (int q = 0; q < RS; ++q) v[j * RS + q] = cmul(v[j * RS + q], __ldg(tab + row + k + q * p));
+      }
+    }
+  }
+}
+
+template <int RS>
+__device__ __forceinline__ void pair_store_global(const float2 (&v)[kPairV], float2* __restrict__ psi, int t, int T,
+                                                  int lgnb, int nl, int n) {
+  const int p = 1 << lgnb;
+#pragma unroll
+  for (int j = 0; j < kPairV / RS; ++j) {
+    const int b = t + j * T, l = b >> lgnb, k = b & (p - 1);
+    if (l < nl) {
+      const int o = l * n + k;
+#pragma unroll
+      for (int q = 0; q < RS; ++q) psi[o + q * p] = v[j * RS + q];
+    }
+  }
+}
+
+// one stage of radix rs (a runtime value: 2, 4, 8 or 16) in one of the pair's forms
+enum PairIn { PIN_GLOBAL, PIN_SMEM, PIN_REGS };
+enum PairOut { POUT_SMEM, POUT_REGS, POUT_GLOBAL };
+
+template <int RS>
+__device__ __forceinline__ void pair_stage_rs(float2 (&v)[kPairV], float2* buf, const PassParams& pp, int in,
+                                              int out, int p, int dir, const float2* tw, int ob, int oe,
+                                              int64_t lane0, float sc) {
+  const Geometry& g = pp.g;
+  const int t = threadIdx.x, T = blockDim.x, n = (int)g.n, ls = g.lane_stride;
+  const int lgnb = __ffs(n / RS) - 1;
+  const int64_t rem = g.outer - lane0;
+  const int nl = rem < g.lanes_per_tile ? (int)rem : g.lanes_per_tile;  // valid lanes of the tile
+  float2* tile_psi = reinterpret_cast<float2*>(pp.psi) + lane0 * n;
+  if (in == PIN_GLOBAL) {
+    pair_load_global<RS>(v, tile_psi, t, T, lgnb, nl, n);
+  } else if (in == PIN_SMEM) {
+    pair_load_smem<RS>(v, buf, t, T, lgnb, ls);
+    __syncthreads();  // every read of the stage before any write (in place)
+  }
+  pair_butterflies<RS>(v, t, T, lgnb, p, dir, tw);
+  if (out == POUT_SMEM) {
+    pair_store_smem<RS>(v, buf, t, T, lgnb, p, ls);
+    __syncthreads();
+  } else {
+    // a last stage: p = n / RS = nb, outputs at k + q p
+    pair_pointwise<RS>(v, pp, ob, oe, t, T, lgnb, lane0, nl, sc);
+    if (out == POUT_GLOBAL) pair_store_global<RS>(v, tile_psi, t, T, lgnb, nl, n);
+  }
+}
+
+__device__ __forceinline__ void pair_stage(int rs, float2 (&v)[kPairV], float2* buf, const PassParams& pp, int in,
+                                           int out, int p, int dir, const float2* tw, int ob, int oe, int64_t lane0,
+                                           float sc) {
+  switch (rs) {
+    case 16: pair_stage_rs<16>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
+    case 8: pair_stage_rs<8>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
+    case 4: pair_stage_rs<4>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
+    default: pair_stage_rs<2>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
+  }
+}
+
+__device__ __forceinline__ void fft_pair_tile(const PassParams& pp, int64_t tile) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* buf = reinterpret_cast<float2*>(smem_raw);
+  const Geometry& g = pp.g;
+  const int n = (int)g.n;
+  const int64_t lane0 = tile * g.lanes_per_tile;
+  const float2* tw = reinterpret_cast<const float2*>(pp.twiddle);
+  const float sc = inv_sqrt_pow2<float>(__ffs(n) - 1);
+  int f1 = 1;
+  while (f1 < pp.nops && pp.ops[f1].kind != OP_FFT) ++f1;
+  // the radices of fft_radices(n, 16, ...): S - 1 stages of 16 and the closing radix rl
+  // (the forward order ends with it, the reversed order starts with it)
+  const int lg = __ffs(n) - 1, S = (lg + 3) / 4, rl = 1 << (lg - 4 * (S - 1));
+  float2 v[kPairV];
+  int p = 1, off = 0;
+  for (int s = 0; s < S; ++s) {
+    const int rs = s + 1 < S ? 16 : rl;
+    const int in = s == 0 ? PIN_GLOBAL : PIN_SMEM, out = s + 1 < S ? POUT_SMEM : POUT_REGS;
+    pair_stage(rs, v, buf, pp, in, out, p, pp.ops[0].dir, tw + off, 1, f1, lane0, sc);
+    if (p > 1) off += (rs - 1) * p;
+    p *= rs;
+  }
+  p = 1;
+  off = 0;
+  for (int s = 0; s < S; ++s) {
+    const int rs = s == 0 ? rl : 16;
+    const int in = s == 0 ? PIN_REGS : PIN_SMEM, out = s + 1 < S ? POUT_SMEM : POUT_GLOBAL;
+    pair_stage(rs, v, buf, pp, in, out, p, pp.ops[f1].dir, tw + n + off, f1 + 1, pp.nops, lane0, sc);
+    if (p > 1) off += (rs - 1) * p;
+    p *= rs;
+  }
+}
+
+__global__ void __launch_bounds__(512, 2) fft_pair_kernel(const __grid_constant__ PassParams p) {
+  fft_pair_tile(p, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(512, 2) fft_pair_kernel_batched(const PassParams* __restrict__ params,
+                                                                  const int64_t* __restrict__ offsets, int count) {
+  const int64_t b = blockIdx.x;
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (offsets[mid] <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  __shared__ __align__(16) PassParams sp;
+  for (int k = threadIdx.x; k < (int)(sizeof(PassParams) / 4); k += blockDim.x)
+    reinterpret_cast<uint32_t*>(&sp)[k] = reinterpret_cast<const uint32_t*>(params + lo)[k];
+  __syncthreads();
+  fft_pair_tile(sp, b - offsets[lo]);
+}
+
+int fft_pair_threads(const Geometry& g) { return g.n >= 8192 ? 512 : 256; }
+
+bool fft_pair_plan(PassParams& p, bool fp64, bool resident) {
+  Geometry& g = p.g;
+  if (fp64 || resident || g.inner != 1 || !stage_twiddles(g.n) || g.n > 8192 || p.twiddle == nullptr) return false;
+  if (p.nops < 2 || p.ops[0].kind != OP_FFT) return false;
+  int ffts = 0;
+  for (int i = 0; i < p.nops; ++i) {
+    const DevOp& op = p.ops[i];
+    if (op.kind == OP_FFT) {
+      ++ffts;
+    } else if (op.kind == OP_DIAGND || (op.kind == OP_DIAG1D && op.axis == g.sweep_axis)) {
+      // point-wise, in registers
+    } else {
+      return false;
+    }
+  }
+  if (ffts != 2) return false;
+  const int T = fft_pair_threads(g);
+  const int64_t L = (int64_t)kPairV * T / g.n;
+  g.lanes_per_tile = (int32_t)L;
+  g.tiles_per_outer = 1;
+  g.tiles = (g.outer + L - 1) / L;
+  p.fused = 1;
+  return true;
+}
+
+static size_t fft_pair_smem(const Geometry& g) {
+  return ((size_t)g.lanes_per_tile * g.lane_stride * sizeof(float2) + 15) & ~(size_t)15;
+}
+
 template <typename R, int RMAX, bool SWEEP>
 __global__ void __launch_bounds__(512, 2) pass_kernel(const __grid_constant__ PassParams p) {
   pass_tile<R, RMAX, SWEEP>(p, blockIdx.x);
@@ -738,8 +981,22 @@ static cudaError_t launch_batched_impl(const PassParams* params_dev, const int64
   return cudaGetLastError();
 }
 
-cudaError_t launch_pass_batched(bool fp64, bool sweep, const PassParams* params_dev, const int64_t* offsets_dev,
-                                int count, int64_t blocks, int threads, size_t smem, cudaStream_t s) {
+cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassParams* params_dev,
+                                const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
+                                cudaStream_t s) {
+  if (fused) {
+    if (fp64 || smem > 220 * 1024 || threads > 512) return cudaErrorInvalidValue;
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(fft_pair_kernel_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           220 * 1024);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    fft_pair_kernel_batched<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
+    count_launch();
+    return cudaGetLastError();
+  }
   if (fp64)
     return sweep ? launch_batched_impl<double, 8, true>(params_dev, offsets_dev, count, blocks, threads, smem, s)
                  : launch_batched_impl<double, 8, false>(params_dev, offsets_dev, count, blocks, threads, smem, s);
@@ -749,6 +1006,7 @@ cudaError_t launch_pass_batched(bool fp64, bool sweep, const PassParams* params_
 
 size_t pass_smem_bytes(const PassParams& p, bool fp64) {
   const Geometry& g = p.g;
+  if (p.fused) return fft_pair_smem(g);
   const bool fft = p.twiddle != nullptr;
   const size_t cs = fp64 ? 16 : 8;
   size_t b = (p.one_buffer ? 1 : 2) * (((size_t)g.lanes_per_tile * g.lane_stride * cs + 15) & ~(size_t)15);
@@ -801,6 +1059,20 @@ cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s) {
   return p.sweep ? launch_impl<double, 8, true>(p, s) : launch_impl<double, 8, false>(p, s);
 }
 cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s) {
+  if (p.fused) {
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e =
+          cudaFuncSetAttribute(fft_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    const size_t smem = fft_pair_smem(p.g);
+    if (smem > 220 * 1024) return cudaErrorInvalidValue;
+    fft_pair_kernel<<<(unsigned)p.g.tiles, fft_pair_threads(p.g), smem, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+  }
   return p.sweep ? launch_impl<float, 16, true>(p, s) : launch_impl<float, 16, false>(p, s);
 }
 

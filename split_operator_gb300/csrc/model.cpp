@@ -447,9 +447,15 @@ const void* Engine::twiddle(size_t n) {
   if (it != twiddles_.end()) return it->second.ptr;
   DeviceBuffer b;
   std::vector<cplx> tw = twiddles(n);
-  if (stage_twiddles((int64_t)n)) {  // the Stockham stages' order (same values, permuted)
-    std::vector<cplx> st(n, cplx(0.0, 0.0));
-    for (size_t e = 0; e < n; ++e) st[e] = tw[(size_t)stage_twiddle_exponent((int64_t)e, (int64_t)n, fp64 ? 8 : 16)];
+  if (stage_twiddles((int64_t)n)) {
+    // the Stockham stages' order (same values, permuted): forward radix order in [0, n),
+    // reversed radix order (the FFT pair pass's second transform) in [n, 2n)
+    std::vector<cplx> st(2 * n, cplx(0.0, 0.0));
+    const int rmax = fp64 ? 8 : 16;
+    for (size_t e = 0; e < n; ++e) {
+      st[e] = tw[(size_t)stage_twiddle_exponent((int64_t)e, (int64_t)n, rmax, false)];
+      st[n + e] = tw[(size_t)stage_twiddle_exponent((int64_t)e, (int64_t)n, rmax, true)];
+    }
     tw.swap(st);
   }
   upload_complex(b, tw, fp64, stream);
@@ -492,6 +498,7 @@ void Engine::submit(const Action& a) {
 
 void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int repeat) {
   PassParams p{};
+  const char* name_tag = "";
   p.g = geometry(axis, resident);
   p.psi = psi.ptr;
   p.slots = slots();
@@ -514,17 +521,20 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   if (fft) p.twiddle = twiddle((size_t)p.g.n);
   pass_choose_buffers(p, fp64);
   if (!fp64 && (tc_tf32 || tc_bf16) && !resident && try_launch_tc(ops, axis, p)) return;
+  if (fft_pair && fft_pair_plan(p, fp64, resident)) name_tag = " fftpair";
   if (!resident && (size_t)p.g.tiles > partials_cap_) {
     partials_cap_ = (size_t)p.g.tiles;
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
     p.partials = partials_.as<double>();
   }
-  std::string name = std::string(fp64 ? "f64" : "f32") + (resident ? " resident" : " sweep") + " axis" +
+  std::string name = std::string(fp64 ? "f64" : "f32") + (resident ? " resident" : " sweep") + name_tag + " axis" +
                      std::to_string(axis) + ":";
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
+    // fused FFT pairs: bit 16 of the thread count (their own launch group and kernel)
+    const int threads = p.fused ? (fft_pair_threads(p.g) | (1 << 16)) : pass_threads(p.g);
     RecordedPass r{resident ? RecordedPass::Resident : RecordedPass::Generic, fp64, p, {},
-                   pass_threads(p.g), pass_smem_bytes(p, fp64), name, pass_bytes(ops, p.g)};
+                   threads, pass_smem_bytes(p, fp64), name, pass_bytes(ops, p.g)};
     recording->push_back(std::move(r));
     return;
   }
@@ -1113,6 +1123,10 @@ Propagation::Propagation(WaveFunction& src, so_time_grid time, std::shared_ptr<O
   wf_ = std::make_unique<WaveFunction>(src.shape, src.grids, choose_perm(src.shape.size(), *stack_), fp64);
   wf_->eng->tc_tf32 = prec == SO_PRECISION_FP32_TF32X3;
   wf_->eng->tc_bf16 = prec == SO_PRECISION_FP32_BF16X3;
+  {
+    const char* fp = std::getenv("SO_FFT_PAIR");  // "0": FFT pairs run the general pass kernel
+    wf_->eng->fft_pair = !(fp && fp[0] == '0');
+  }
   wf_->last_grid_names = src.last_grid_names;
   wf_->possible_norm_change = src.possible_norm_change;
   wf_->eng->write_slot(wf_->cache_slot, src.eng->read_slot(src.cache_slot));
@@ -1451,8 +1465,8 @@ void Batch::run_groups(std::vector<Group>& gs) {
                                            (g.threads >> 17) & 1, stream_),
                  "batched tensor-core pass");
     else
-      cuda_check(launch_pass_batched(g.fp64, g.sweep, g.params.as<PassParams>(), g.offsets.as<int64_t>(), g.count,
-                                     g.blocks, g.threads, g.smem, stream_),
+      cuda_check(launch_pass_batched(g.fp64, g.sweep, (g.threads >> 16) & 1, g.params.as<PassParams>(),
+                                     g.offsets.as<int64_t>(), g.count, g.blocks, g.threads & 0xffff, g.smem, stream_),
                  "batched pass");
     if (timing_) {
       cuda_check(cudaEventRecord(t.b, stream_), "event record");

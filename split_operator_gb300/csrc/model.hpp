@@ -125,7 +125,8 @@ class Engine {
   int nonfinite_slot = 0;
   int timeout_slot = 0;
   bool tc_tf32 = false;  // real lane matrices on the tensor cores (3xTF32); FP32 state only
-  bool tc_bf16 = false;  // the same as split-BF16x3
+  bool tc_bf16 = false;
+  bool fft_pair = true;  // FP32 FFT-pair passes run the fused register kernel (SO_FFT_PAIR=0: the general pass)  // the same as split-BF16x3
 
   size_t points() const;
   size_t elem_bytes() const { return fp64 ? 16 : 8; }

@@ -161,3 +161,26 @@ def test_radial_angular_fp64_per_step_parity(so, nr, nth, steps):
     lg = h["damp"].loss()
     assert abs(lg - lo) <= 1e-12 + 1e-9 * abs(lo)
     assert prop.all_losses() == [lg]
+
+
+@pytest.mark.parametrize("nr,nth", [(16, 8), (32, 16), (512, 32), (1024, 64), (2048, 32), (4096, 32), (8192, 32)])
+def test_fft_pair_pass_matches_general_pass(nr, nth, monkeypatch):
+    """The fused FFT-pair kernel (registers at both FFTs' outer stages, reversed radix order
+    for the second transform) against the general lane-sweep pass on the same FP32
+    problem: same physics, different rounding order."""
+    ensure_built()
+    from split_operator_gb300 import workloads as W
+    kw = dict(nr=nr, nth=nth, step_no=20, seed=31, precision="fp32_simt")
+    fused = W.radial_angular_2d(**kw)[0]
+    monkeypatch.setenv("SO_FFT_PAIR", "0")
+    general = W.radial_angular_2d(**kw)[0]
+    monkeypatch.delenv("SO_FFT_PAIR")
+    fused.set_timing(True)
+    general.set_timing(True)
+    fused.steps(20)
+    general.steps(20)
+    assert any("fftpair" in k[0] for k in fused.kernel_times())
+    assert not any("fftpair" in k[0] for k in general.kernel_times())
+    a, b = fused.get_array(), general.get_array()
+    assert rel_l2(a, b) < 2e-6, rel_l2(a, b)
+    assert abs(fused.norm() - general.norm()) < 1e-6
