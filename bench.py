@@ -135,6 +135,8 @@ def kernel_of(group_name):
     """The CUDA kernel a batched group runs: its name carries the pass family."""
     if "tc3xtf32" in group_name or "tcbf16x3" in group_name:
         return "angular_tc_kernel_batched"
+    if "fftpair" in group_name:
+        return "fft_pair_kernel_batched"
     if "scalar" in group_name:
         return "scalar_program_kernel"
     return "pass_kernel_batched"
