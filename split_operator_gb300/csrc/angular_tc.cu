@@ -787,7 +787,10 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       float2* psi = reinterpret_cast<float2*>(p.psi);
       if (tid == 0) trace_mark(tp, tile, TR_START);
 
-      build_tile_tabs(p, tabs, o, i0, S.bn);
+      // a pass that starts with its matrix needs the tables only after the first GEMM: they
+      // are built while it runs (after the prologue) instead of ahead of the prologue
+      const bool late_tabs = tp.mat_op[0] == 0;
+      if (!late_tabs) build_tile_tabs(p, tabs, o, i0, S.bn);
       // full-size tables read after the first lane matrix: start their tile rows toward L2
       for (int oi = tp.mat_op[0] + 1; oi < p.nops; ++oi) {
         const DevOp& op = p.ops[oi];
@@ -838,6 +841,8 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         mbar_arrive(bready);
       }
       if (tid == 0) trace_mark(tp, tile, TR_PROLOGUE);
+      // (the first drain's barrier orders these writes before the epilogue reads them)
+      if (late_tabs) build_tile_tabs(p, tabs, o, i0, S.bn);
       // lane-axis weights of this thread's epilogue rows for the norms after the first
       // matrix, loaded now (they arrive while the GEMM runs)
       const float* rw_ptr = nullptr;
