@@ -1,5 +1,5 @@
 // CPU FP64 restatement of the split_operator propagation step (TEST AND
-// BASELINE INFRASTRUCTURE ONLY: imported by the test suite and by bench.py's
+// MEASUREMENT INFRASTRUCTURE ONLY: imported by the test suite and by bench.py's
 // CPU-baseline / reference leg, never by the product).
 //
 // It keeps the reference crate's structure and cost profile, not just its
