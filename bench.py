@@ -384,7 +384,7 @@ def run_ours(a):
            "host_link_gbs": {"h2d": 211, "d2h": 193, "source": "cudaMemcpyAsync of 1 GiB pinned, measured on this "
                                                                "GPU model"},
            "note": ("every step: one so_batch_steps_host call: pinned FP64 host states of all instances in, one "
-                    "step, states out to pinned host buffers, pipelined over 4 instance chunks on their own "
+                    "step, states out to pinned host buffers, pipelined over 8 instance chunks on their own "
                     "streams (copy engines both ways)") if not single else
                    "every step: so_propagation_set_array from a pinned FP64 host buffer, one step, "
                    "so_propagation_get_array into a pinned host buffer"}

@@ -1593,16 +1593,24 @@ void Batch::get_arrays(double* const* out) {
   }
 }
 
+// member chunks of the host-to-host pipeline (SO_HOST_CHUNKS overrides, 1..16)
+static size_t host_chunks() {
+  const char* e = std::getenv("SO_HOST_CHUNKS");
+  const long v = e ? std::strtol(e, nullptr, 10) : 8;
+  return (size_t)std::min<long>(16, std::max<long>(1, v));
+}
+
 void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) {
+  const size_t kHostChunks = host_chunks();
   const size_t m = props_.size();
   for (size_t i = 0; i < m; ++i)
     if (!in[i] || !out[i]) throw Error(SO_ERR_INVALID, "null state array in batch");
   if (chunks_.empty()) {
-    // up to four chunks of consecutive members with about equal points, each a batch of
-    // its own on its own stream
+    // chunks of consecutive members with about equal points, each a batch of its own on
+    // its own stream
     double total = 0.0;
     for (Propagation* p : props_) total += (double)p->engine().points();
-    const size_t k = std::min<size_t>(4, m);
+    const size_t k = std::min<size_t>(kHostChunks, m);
     size_t first = 0;
     double acc = 0.0;
     for (size_t c = 0; c < k; ++c) {
