@@ -184,3 +184,77 @@ def test_fft_pair_pass_matches_general_pass(nr, nth, monkeypatch):
     a, b = fused.get_array(), general.get_array()
     assert rel_l2(a, b) < 2e-6, rel_l2(a, b)
     assert abs(fused.norm() - general.norm()) < 1e-6
+
+
+# ------------------------------------------------------------ lane-matrix operators
+def _unitary(rng, n, count):
+    z = rng.standard_normal((count, n, n)) + 1j * rng.standard_normal((count, n, n))
+    return np.stack([np.linalg.qr(m)[0] for m in z])
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 2e-6)])
+@pytest.mark.parametrize("count", [40, 64])
+def test_non_diag_propagator_matches_oracle(so, precision, tol, count):
+    """NonDiagPropagator (non_diagonal_propagator.rs:9-66): a matrix per lane along axis 1,
+    lanes in ndarray lanes_mut order; with fewer matrices than lanes the rest stay as they
+    are (Iterator::zip)."""
+    nx, ny, steps = 64, 24, 3
+    rng = np.random.default_rng(count)
+    psi = rng.standard_normal((nx, ny)) + 1j * rng.standard_normal((nx, ny))
+    ops = _unitary(rng, ny, count)
+    gx = so.Grid.new_linear_continuos("x", -4.0, 4.0, nx, 0)
+    gy = so.Grid.new_linear_continuos("y", -2.0, 2.0, ny, 1)
+    ox = O.Grid.new_linear_continuos("x", -4.0, 4.0, nx, 0)
+    oy = O.Grid.new_linear_continuos("y", -2.0, 2.0, ny, 1)
+    v = np.sin(np.linspace(0.0, 3.0, nx))
+    tg, otg = so.TimeGrid(0.1, steps), O.TimeGrid(0.1, steps)
+    st, ost = so.OperationStack(), O.OperationStack()
+    nd = so.NonDiagPropagator(1)
+    nd.set_operators(ops)
+    ond = O.NonDiagPropagator(1)
+    ond.set_operators(list(ops))
+    st.add_propagator(so.one_dim_into_propagator(v, gx, tg, so.HALF))
+    st.add_propagator(nd)
+    ost.add_propagator(O.one_dim_into_propagator(v, ox, otg, O.HALF))
+    ost.add_propagator(ond)
+    prop = so.Propagation(so.WaveFunction(psi, [gx, gy]), tg, st, precision)
+    oprop = O.Propagation(O.WaveFunction(psi.copy(), [ox, oy]), otg, ost)
+    for k in range(steps):
+        prop.steps(1)
+        oprop.step()
+        assert rel_l2(prop.get_array(), oprop.wave_function.array) < tol * (k + 1)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 2e-6)])
+def test_state_matrix_transformation_matches_oracle(so, precision, tol):
+    """StateMatrixTransformation (state_matrix_transformation.rs:8-73): matrix i acts along
+    axis 0 on slice i of the dependent axis 1; transform in the first half-step, inverse in
+    the second, a diagonal propagator between them."""
+    nth, nom, steps = 16, 6, 3
+    rng = np.random.default_rng(5)
+    psi = rng.standard_normal((nth, nom)) + 1j * rng.standard_normal((nth, nom))
+    ts = _unitary(rng, nth, nom)
+    tinvs = np.conj(np.transpose(ts, (0, 2, 1)))
+    g0 = so.Grid.new_linear_countable("th", 0.0, 1.0, nth, 0)
+    g1 = so.Grid.new_linear_countable("om", 0.0, 1.0, nom, 1)
+    gl = so.Grid.new_linear_countable("l", 0.0, 1.0, nth, 0)
+    o0 = O.Grid.new_linear_countable("th", 0.0, 1.0, nth, 0)
+    o1 = O.Grid.new_linear_countable("om", 0.0, 1.0, nom, 1)
+    ol = O.Grid.new_linear_countable("l", 0.0, 1.0, nth, 0)
+    h = rng.standard_normal((nth, nom))
+    tg, otg = so.TimeGrid(0.05, steps), O.TimeGrid(0.05, steps)
+    smt = so.StateMatrixTransformation(1, g0, gl)
+    smt.set_diagonalization_matrices(ts, tinvs)
+    osmt = O.StateMatrixTransformation(1, o0, ol)
+    osmt.set_diagonalization_matrices(list(ts), list(tinvs))
+    st, ost = so.OperationStack(), O.OperationStack()
+    st.add_transformation(smt, so.NORMAL)
+    st.add_propagator(so.n_dim_into_propagator(h, tg, so.FULL))
+    ost.add_transformation(osmt, O.NORMAL)
+    ost.add_propagator(O.n_dim_into_propagator(h, otg, O.FULL))
+    prop = so.Propagation(so.WaveFunction(psi, [g0, g1]), tg, st, precision)
+    oprop = O.Propagation(O.WaveFunction(psi.copy(), [o0, o1]), otg, ost)
+    for k in range(steps):
+        prop.steps(1)
+        oprop.step()
+        assert rel_l2(prop.get_array(), oprop.wave_function.array) < tol * (k + 1)
