@@ -258,3 +258,53 @@ def test_state_matrix_transformation_matches_oracle(so, precision, tol):
         prop.steps(1)
         oprop.step()
         assert rel_l2(prop.get_array(), oprop.wave_function.array) < tol * (k + 1)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 3e-6)])
+def test_three_dim_two_fft_axes_matches_oracle(so, precision, tol):
+    """A 3-D state with FFTs along axes 0 and 2 (a power-of-two lane and a 24-point lane, so
+    the passes run strided lanes and the direct DFT), kinetic phases along both, and a full
+    3-D potential: the engine's storage permutation and lane-axis switches against the
+    oracle's straightforward ndarray arithmetic."""
+    nx, ny, nz, steps = 32, 6, 24, 4
+    rng = np.random.default_rng(3)
+    psi = rng.standard_normal((nx, ny, nz)) + 1j * rng.standard_normal((nx, ny, nz))
+    m = 1.7
+    g = [so.Grid.new_linear_continuos("x", -5.0, 5.0, nx, 0), so.Grid.new_linear_countable("y", 0.0, 1.0, ny, 1),
+         so.Grid.new_linear_continuos("z", -3.0, 3.0, nz, 2)]
+    o = [O.Grid.new_linear_continuos("x", -5.0, 5.0, nx, 0), O.Grid.new_linear_countable("y", 0.0, 1.0, ny, 1),
+         O.Grid.new_linear_continuos("z", -3.0, 3.0, nz, 2)]
+    v = 0.3 * rng.standard_normal((nx, ny, nz))
+    tg, otg = so.TimeGrid(0.02, steps), O.TimeGrid(0.02, steps)
+    st, ost = so.OperationStack(), O.OperationStack()
+    st.add_propagator(so.n_dim_into_propagator(v, tg, so.HALF))
+    st.add_transformation(so.FFTTransformation(g[0], "kx"), so.NORMAL)
+    st.add_transformation(so.FFTTransformation(g[2], "kz"), so.NORMAL)
+    st.add_propagator(so.one_dim_into_propagator(so.kinetic_hamiltonian(g[0], m), g[0], tg, so.FULL))
+    st.add_propagator(so.one_dim_into_propagator(so.kinetic_hamiltonian(g[2], m), g[2], tg, so.FULL))
+    ost.add_propagator(O.n_dim_into_propagator(v, otg, O.HALF))
+    ost.add_transformation(O.FFTTransformation(o[0], "kx"), O.NORMAL)
+    ost.add_transformation(O.FFTTransformation(o[2], "kz"), O.NORMAL)
+    ost.add_propagator(O.one_dim_into_propagator(O.kinetic_hamiltonian(o[0], m), o[0], otg, O.FULL))
+    ost.add_propagator(O.one_dim_into_propagator(O.kinetic_hamiltonian(o[2], m), o[2], otg, O.FULL))
+    prop = so.Propagation(so.WaveFunction(psi, g), tg, st, precision)
+    oprop = O.Propagation(O.WaveFunction(psi.copy(), o), otg, ost)
+    for k in range(steps):
+        prop.steps(1)
+        oprop.step()
+        assert rel_l2(prop.get_array(), oprop.wave_function.array) < tol * (k + 1)
+    assert abs(prop.norm() - oprop.wave_function.norm()) < 10 * tol * abs(oprop.wave_function.norm())
+
+
+@pytest.mark.parametrize("precision,n", [("fp32_simt", 16384), ("fp64", 8192)])
+def test_lanes_beyond_the_tile_limit_are_rejected(so, precision, n):
+    """A lane longer than a CTA tile holds (8192 FP32 / 4096 FP64 points) is refused with a
+    status before any kernel runs; the context stays usable."""
+    from split_operator_gb300 import workloads as W
+    with pytest.raises(so.SplitOperatorError) as e:
+        p = W.radial_angular_2d(nr=n, nth=8, step_no=2, precision=precision)[0]
+        p.steps(1)
+    assert "not supported" in str(e.value)
+    q = W.radial_angular_2d(nr=256, nth=8, step_no=2, precision=precision)[0]
+    q.steps(1)
+    assert np.isfinite(q.norm())
