@@ -308,3 +308,38 @@ def test_lanes_beyond_the_tile_limit_are_rejected(so, precision, n):
     q = W.radial_angular_2d(nr=256, nth=8, step_no=2, precision=precision)[0]
     q.steps(1)
     assert np.isfinite(q.norm())
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 3e-6)])
+def test_two_dim_savers_match_oracle(so, precision, tol):
+    """WaveFunctionSaver (|psi|^2 frames) and StateSaver (state_density along an axis) on a
+    2-D propagation, saved at the first half of every step_no / frames_no-th step
+    (wave_function_saver.rs:6-183): frames and their times against the oracle."""
+    nx, ny, steps, frames = 64, 12, 20, 5
+    rng = np.random.default_rng(8)
+    psi = rng.standard_normal((nx, ny)) + 1j * rng.standard_normal((nx, ny))
+    g = [so.Grid.new_linear_continuos("x", -6.0, 6.0, nx, 0), so.Grid.new_linear_continuos("y", -1.0, 1.0, ny, 1)]
+    o = [O.Grid.new_linear_continuos("x", -6.0, 6.0, nx, 0), O.Grid.new_linear_continuos("y", -1.0, 1.0, ny, 1)]
+    v = 0.2 * rng.standard_normal((nx, ny))
+    tg, otg = so.TimeGrid(0.05, steps), O.TimeGrid(0.05, steps)
+    wsave, osave = so.WaveFunctionSaver("w", tg, g[0], g[1], frames), O.WaveFunctionSaver("w", otg, o[0], o[1], frames)
+    ssave, ossave = so.StateSaver("s", tg, g[1], frames), O.StateSaver("s", otg, o[1], frames)
+    st, ost = so.OperationStack(), O.OperationStack()
+    st.add_saver(wsave, so.FIRST_HALF)
+    st.add_saver(ssave, so.FIRST_HALF)
+    st.add_propagator(so.n_dim_into_propagator(v, tg, so.HALF))
+    st.add_transformation(so.FFTTransformation(g[0], "kx"), so.NORMAL)
+    st.add_propagator(so.one_dim_into_propagator(so.kinetic_hamiltonian(g[0], 2.0), g[0], tg, so.FULL))
+    ost.add_saver(osave, O.FIRST_HALF)
+    ost.add_saver(ossave, O.FIRST_HALF)
+    ost.add_propagator(O.n_dim_into_propagator(v, otg, O.HALF))
+    ost.add_transformation(O.FFTTransformation(o[0], "kx"), O.NORMAL)
+    ost.add_propagator(O.one_dim_into_propagator(O.kinetic_hamiltonian(o[0], 2.0), o[0], otg, O.FULL))
+    prop = so.Propagation(so.WaveFunction(psi, g), tg, st, precision)
+    oprop = O.Propagation(O.WaveFunction(psi.copy(), o), otg, ost)
+    prop.propagate()
+    oprop.propagate()
+    assert rel_l2(wsave.data, osave.data) < tol * steps
+    assert rel_l2(ssave.data, ossave.data) < tol * steps
+    np.testing.assert_allclose(wsave.times, osave.times, rtol=1e-15)
+    np.testing.assert_allclose(ssave.times, ossave.times, rtol=1e-15)
