@@ -299,8 +299,8 @@ int so_batch_launches_per_step(so_batch b, size_t* out);
 int so_batch_set_arrays(so_batch b, const double* const* in, size_t count);
 int so_batch_get_arrays(so_batch b, double* const* out, size_t count);
 /* so_batch_set_arrays(in), so_batch_steps(steps), so_batch_get_arrays(out) as one call,
- * pipelined: the members are split into up to eight chunks (SO_HOST_CHUNKS: 1..16) on
- * streams of their own, each
+ * pipelined: the members are split into up to eight chunks (SO_HOST_CHUNKS: 1..16, read
+ * at the batch's first such call) on streams of their own, each
  * copied in (copy engines), stepped and copied out, so the host link's two directions
  * and the chunks' steps overlap.  `in` and `out` may be the same arrays. */
 int so_batch_steps_host(so_batch b, const double* const* in, double* const* out, size_t count, uint64_t steps);

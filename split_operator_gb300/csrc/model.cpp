@@ -1593,7 +1593,8 @@ void Batch::get_arrays(double* const* out) {
   }
 }
 
-// member chunks of the host-to-host pipeline (SO_HOST_CHUNKS overrides, 1..16)
+// member chunks of the host-to-host pipeline (SO_HOST_CHUNKS overrides, 1..16; the chunks
+// are formed at a batch's first steps_host call and kept)
 static size_t host_chunks() {
   const char* e = std::getenv("SO_HOST_CHUNKS");
   const long v = e ? std::strtol(e, nullptr, 10) : 8;
