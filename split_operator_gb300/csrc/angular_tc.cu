@@ -1057,6 +1057,10 @@ void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const floa
   std::memcpy(out, &tp, sizeof(TcParams));
 }
 
+void tc_params_set_trace(void* params, unsigned long long* trace) {
+  reinterpret_cast<TcParams*>(params)->trace = trace;
+}
+
 // the largest dynamic shared memory any supported lane extent asks for
 static size_t tc_max_dynamic_smem() {
   size_t m = 0;

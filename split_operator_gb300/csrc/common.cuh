@@ -181,6 +181,7 @@ cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassPar
                                 const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
                                 cudaStream_t s);
 size_t tc_params_bytes();
+void tc_params_set_trace(void* params, unsigned long long* trace);  // the TcParams' trace field
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
                     const int* parity, void* out);
 cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,

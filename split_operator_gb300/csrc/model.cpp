@@ -1388,6 +1388,20 @@ Batch::Batch(std::vector<Propagation*> props) : props_(std::move(props)) {
 }
 
 Batch::~Batch() {
+  if (const char* path = std::getenv("SO_TC_TRACE_BATCH")) {
+    cudaStreamSynchronize(stream_);
+    if (FILE* f = std::fopen(path, "a")) {
+      for (TraceBuf& tb : traces_) {
+        std::vector<unsigned long long> h(tb.buf.bytes / sizeof(unsigned long long));
+        if (cudaMemcpy(h.data(), tb.buf.ptr, tb.buf.bytes, cudaMemcpyDeviceToHost) != cudaSuccess) break;
+        std::fprintf(f, "pass %s tiles=%lld slots=%d\n", tb.name.c_str(), (long long)tb.tiles,
+                     angular_tc_trace_slots());
+        for (size_t i = 0; i < h.size(); ++i)
+          std::fprintf(f, "%llu%c", h[i], (i + 1) % angular_tc_trace_slots() == 0 ? '\n' : ' ');
+      }
+      std::fclose(f);
+    }
+  }
   for (Chunk& ch : chunks_) {
     ch.batch.reset();
     cudaStreamSynchronize(ch.stream);
@@ -1428,6 +1442,9 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
     std::vector<int64_t> off(v.size() + 1, 0);
     const size_t pb = g.kind == RecordedPass::TensorCore ? tc_params_bytes() : sizeof(PassParams);
     std::vector<unsigned char> params(pb * v.size());
+    // SO_TC_TRACE_BATCH=<file>: per-tile phase timestamps of every member's tensor-core pass
+    // (the last launch of each cached group), written when the batch is destroyed
+    static const char* trace_path = std::getenv("SO_TC_TRACE_BATCH");
     g.bytes = 0.0;
     g.sweep = true;  // the compact kernel only when every member's pass allows it
     for (size_t i = 0; i < v.size(); ++i) {
@@ -1435,6 +1452,15 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
       g.sweep = g.sweep && v[i]->p.sweep;
       if (g.kind == RecordedPass::TensorCore)
         std::memcpy(params.data() + i * pb, v[i]->tcp.data(), pb);
+        if (trace_path) {
+          TraceBuf tb;
+          tb.tiles = v[i]->p.g.tiles;
+          tb.name = v[i]->name + " member " + std::to_string(i);
+          tb.buf = DeviceBuffer((size_t)tb.tiles * angular_tc_trace_slots() * sizeof(unsigned long long));
+          cuda_check(cudaMemset(tb.buf.ptr, 0, tb.buf.bytes), "trace clear");
+          tc_params_set_trace(params.data() + i * pb, tb.buf.as<unsigned long long>());
+          traces_.push_back(std::move(tb));
+        }
       else
         std::memcpy(params.data() + i * pb, &v[i]->p, pb);
       g.bytes += v[i]->bytes;

@@ -467,6 +467,12 @@ class Batch {
     std::unique_ptr<Batch> batch;
   };
   std::vector<Chunk> chunks_;  // steps_host pipeline (built on first use)
+  struct TraceBuf {
+    DeviceBuffer buf;
+    int64_t tiles = 0;
+    std::string name;
+  };
+  std::vector<TraceBuf> traces_;  // SO_TC_TRACE_BATCH diagnostics
   void run_groups(std::vector<Group>& gs);
   std::vector<Propagation*> props_;
   cudaStream_t stream_ = nullptr;
