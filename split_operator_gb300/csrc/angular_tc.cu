@@ -1020,20 +1020,16 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel(const 
 // offsets[count] is the total.
 template <bool BF>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel_batched(const TcParams* __restrict__ params,
-                                                                        const int64_t* __restrict__ offsets,
-                                                                        int count) {
-  auto resolve = [params, offsets, count](int64_t b) {
-    int lo = 0, hi = count - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (offsets[mid] <= b)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    return TileRef{params + lo, b - offsets[lo]};
+                                                                        const uint2* __restrict__ owners,
+                                                                        int64_t total) {
+  // owners[b] = (pass index, tile within the pass) of global tile b, built on the host: one
+  // load per lookup (every warp looks up every tile it works on, the work warps also the
+  // next one; a binary search over the offsets would be a chain of dependent loads)
+  auto resolve = [params, owners](int64_t b) {
+    const uint2 o = __ldg(owners + b);
+    return TileRef{params + o.x, (int64_t)o.y};
   };
-  tc_persistent<BF>(resolve, offsets[count]);
+  tc_persistent<BF>(resolve, total);
 }
 
 // ------------------------------------------------------------------ host side
@@ -1096,17 +1092,18 @@ static unsigned persistent_grid(int64_t tiles) {
   return (unsigned)(tiles < slots ? tiles : slots);
 }
 
-cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,
-                                      size_t smem, bool bf, cudaStream_t s) {
+cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners_dev, int64_t blocks, size_t smem,
+                                      bool bf, cudaStream_t s) {
   static bool configured[2] = {false, false};
   const void* kern = bf ? (const void*)angular_tc_kernel_batched<true> : (const void*)angular_tc_kernel_batched<false>;
   if (!configure_once(kern, configured[bf ? 1 : 0])) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
   const TcParams* prm = reinterpret_cast<const TcParams*>(params_dev);
+  const uint2* own = reinterpret_cast<const uint2*>(owners_dev);
   if (bf)
-    angular_tc_kernel_batched<true><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, offsets_dev, count);
+    angular_tc_kernel_batched<true><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
   else
-    angular_tc_kernel_batched<false><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, offsets_dev, count);
+    angular_tc_kernel_batched<false><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
   count_launch();
   return cudaGetLastError();
 }

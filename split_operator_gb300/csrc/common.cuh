@@ -184,8 +184,9 @@ size_t tc_params_bytes();
 void tc_params_set_trace(void* params, unsigned long long* trace);  // the TcParams' trace field
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
                     const int* parity, void* out);
-cudaError_t launch_angular_tc_batched(const void* params_dev, const int64_t* offsets_dev, int count, int64_t blocks,
-                                      size_t smem, bool bf, cudaStream_t s);
+// owners_dev: blocks pairs (pass index, tile within the pass), uint32 each, in global tile order
+cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners_dev, int64_t blocks, size_t smem,
+                                      bool bf, cudaStream_t s);
 
 // Auxiliary kernels (aux_kernels.cu)
 cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);

@@ -1450,7 +1450,7 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
     for (size_t i = 0; i < v.size(); ++i) {
       off[i + 1] = off[i] + v[i]->p.g.tiles;
       g.sweep = g.sweep && v[i]->p.sweep;
-      if (g.kind == RecordedPass::TensorCore)
+      if (g.kind == RecordedPass::TensorCore) {
         std::memcpy(params.data() + i * pb, v[i]->tcp.data(), pb);
         if (trace_path) {
           TraceBuf tb;
@@ -1461,8 +1461,9 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
           tc_params_set_trace(params.data() + i * pb, tb.buf.as<unsigned long long>());
           traces_.push_back(std::move(tb));
         }
-      else
+      } else {
         std::memcpy(params.data() + i * pb, &v[i]->p, pb);
+      }
       g.bytes += v[i]->bytes;
     }
     g.blocks = off.back();
@@ -1471,6 +1472,19 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
     cuda_check(cudaMemcpy(g.params.ptr, params.data(), params.size(), cudaMemcpyHostToDevice), "batch params");
     cuda_check(cudaMemcpy(g.offsets.ptr, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice),
                "batch offsets");
+    if (g.kind == RecordedPass::TensorCore) {
+      // the tensor-core kernel looks tiles up directly: (pass index, tile within the pass)
+      if (g.blocks >= (int64_t)0xffffffff) throw Error(SO_ERR_UNSUPPORTED, "too many tiles in one batched pass");
+      std::vector<uint32_t> own((size_t)g.blocks * 2);
+      for (size_t i = 0; i + 1 < off.size(); ++i)
+        for (int64_t t = off[i]; t < off[i + 1]; ++t) {
+          own[(size_t)t * 2] = (uint32_t)i;
+          own[(size_t)t * 2 + 1] = (uint32_t)(t - off[i]);
+        }
+      g.owners = DeviceBuffer(own.size() * sizeof(uint32_t));
+      cuda_check(cudaMemcpy(g.owners.ptr, own.data(), own.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+                 "batch tile owners");
+    }
     out.push_back(std::move(g));
   }
   return out;
@@ -1487,7 +1501,7 @@ void Batch::run_groups(std::vector<Group>& gs) {
       cuda_check(cudaEventRecord(t.a, stream_), "event record");
     }
     if (g.kind == RecordedPass::TensorCore)
-      cuda_check(launch_angular_tc_batched(g.params.ptr, g.offsets.as<int64_t>(), g.count, g.blocks, g.smem,
+      cuda_check(launch_angular_tc_batched(g.params.ptr, g.owners.ptr, g.blocks, g.smem,
                                            (g.threads >> 17) & 1, stream_),
                  "batched tensor-core pass");
     else

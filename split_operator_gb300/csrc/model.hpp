@@ -453,6 +453,7 @@ class Batch {
     int64_t blocks;
     int count;
     DeviceBuffer params, offsets;
+    DeviceBuffer owners;  // tensor-core groups: (pass index, tile within the pass) per global tile
     std::string name;
     double bytes;
   };
