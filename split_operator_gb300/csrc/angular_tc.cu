@@ -800,7 +800,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         const float2* t = reinterpret_cast<const float2*>(op.ptr) + base;
         if (!seen && (reinterpret_cast<uintptr_t>(t) & 15u) == 0)
           for (int jj = tid; jj < n; jj += kWorkThreads)
-            prefetch_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * sizeof(float2)));
+            prefetch_lines_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * sizeof(float2)));
       }
       // the next tile's state rows toward L2 (its prologue loads then hit L2)
       if (gt + gridDim.x < total) {
@@ -810,7 +810,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         const float2* pn = reinterpret_cast<const float2*>(rn.prm->p.psi) + on * gn.n * gn.inner +
                            (rn.tile - on * gn.tiles_per_outer) * S.bn;
         for (int jj = tid; jj < n; jj += kWorkThreads)
-          prefetch_l2(pn + (int64_t)jj * gn.inner, (uint32_t)(S.bn * sizeof(float2)));
+          prefetch_lines_l2(pn + (int64_t)jj * gn.inner, (uint32_t)(S.bn * sizeof(float2)));
       }
       work_sync();  // tabs complete; the previous tile's staging has been stored
       if (tid == 0) trace_mark(tp, tile, TR_TABS);

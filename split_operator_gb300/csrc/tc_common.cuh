@@ -217,6 +217,12 @@ __device__ __forceinline__ void split_bf16(float x, uint16_t& hi, uint16_t& lo) 
 __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
+// the same through the load/store path, one 128-byte line per instruction: the bulk form
+// takes a slot of the SM's bulk-copy unit per row, which the A-chunk copies also use
+__device__ __forceinline__ void prefetch_lines_l2(const void* p, uint32_t bytes) {
+  const char* c = static_cast<const char*>(p);
+  for (uint32_t o = 0; o < bytes; o += 128u) asm volatile("prefetch.global.L2 [%0];" ::"l"(c + o));
+}
 
 }  // namespace tc
 }  // namespace so
