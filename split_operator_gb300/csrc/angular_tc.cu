@@ -802,16 +802,6 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
           for (int jj = tid; jj < n; jj += kWorkThreads)
             prefetch_lines_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * sizeof(float2)));
       }
-      // the next tile's state rows toward L2 (its prologue loads then hit L2)
-      if (gt + gridDim.x < total) {
-        const TileRef rn = resolve(gt + gridDim.x);
-        const Geometry& gn = rn.prm->p.g;
-        const int64_t on = rn.tile / gn.tiles_per_outer;
-        const float2* pn = reinterpret_cast<const float2*>(rn.prm->p.psi) + on * gn.n * gn.inner +
-                           (rn.tile - on * gn.tiles_per_outer) * S.bn;
-        for (int jj = tid; jj < n; jj += kWorkThreads)
-          prefetch_lines_l2(pn + (int64_t)jj * gn.inner, (uint32_t)(S.bn * sizeof(float2)));
-      }
       work_sync();  // tabs complete; the previous tile's staging has been stored
       if (tid == 0) trace_mark(tp, tile, TR_TABS);
 
@@ -841,6 +831,17 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         mbar_arrive(bready);
       }
       if (tid == 0) trace_mark(tp, tile, TR_PROLOGUE);
+      // the next tile's state rows toward L2 (its prologue loads then hit L2); issued behind
+      // this tile's prologue, since finding the next tile's pass reads its descriptor
+      if (gt + gridDim.x < total) {
+        const TileRef rn = resolve(gt + gridDim.x);
+        const Geometry& gn = rn.prm->p.g;
+        const int64_t on = rn.tile / gn.tiles_per_outer;
+        const float2* pn = reinterpret_cast<const float2*>(rn.prm->p.psi) + on * gn.n * gn.inner +
+                           (rn.tile - on * gn.tiles_per_outer) * S.bn;
+        for (int jj = tid; jj < n; jj += kWorkThreads)
+          prefetch_lines_l2(pn + (int64_t)jj * gn.inner, (uint32_t)(S.bn * sizeof(float2)));
+      }
       // (the first drain's barrier orders these writes before the epilogue reads them)
       if (late_tabs) build_tile_tabs(p, tabs, o, i0, S.bn);
       // lane-axis weights of this thread's epilogue rows for the norms after the first
