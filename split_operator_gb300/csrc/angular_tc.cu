@@ -954,6 +954,19 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       }
       work_sync();  // staging complete
 
+      // norm partials of this tile (float-float, fixed order) and the pass ticket first, so
+      // the fence waits for no state store and the ticket's round trip overlaps the store
+      for (int k = 0; k < p.nred; ++k) {
+        const FF t = block_sum(acc[k], scratch);
+        if (tid == 0) blk_red[k] = (double)t.hi + (double)t.lo;
+      }
+      unsigned int ticket = 0u;
+      if (tid == 0) {
+        for (int k = 0; k < p.nred; ++k) p.partials[(int64_t)k * g.tiles + tile] = blk_red[k];
+        __threadfence();
+        ticket = atomicAdd(p.counter, 1u);
+      }
+
       // coalesced store of the staged tile: thread = complex column
       {
         const int c = tid % S.bn, h = tid / S.bn, G = S.groups;
@@ -965,19 +978,11 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
           }
         }
       }
-      if (tid == 0) trace_mark(tp, tile, TR_STORE);
-
-      // norm partials of this tile (float-float, fixed order) and the last tile's FP64 fold
-      for (int k = 0; k < p.nred; ++k) {
-        const FF t = block_sum(acc[k], scratch);
-        if (tid == 0) blk_red[k] = (double)t.hi + (double)t.lo;
-      }
       if (tid == 0) {
-        for (int k = 0; k < p.nred; ++k) p.partials[(int64_t)k * g.tiles + tile] = blk_red[k];
-        __threadfence();
-        const unsigned int ticket = atomicAdd(p.counter, 1u);
+        trace_mark(tp, tile, TR_STORE);
         s_last = ticket == (unsigned int)(g.tiles - 1);
       }
+      // the last tile's FP64 fold of all of the pass's partials
       work_sync();
       if (s_last) {
         __threadfence();
