@@ -173,20 +173,30 @@ __device__ __forceinline__ bool work_all(bool v) {
 }
 
 // fixed-order sum of one float per work thread, in float-float; valid in thread 0
-__device__ FF block_sum(float v, FF* scratch) {
-  FF a{v, 0.0f};
+// The tile's nred float-float block sums together (fixed order): each warp reduces every
+// value by the same shuffle tree, lane 0 stores them, one barrier; thread k adds reduction
+// k's warp partials 0 .. 7 in order and stores its FP64 value in out[k]; a second barrier
+// publishes them.  scratch: kMaxRed x (kWorkThreads / 32) entries.
+__device__ __forceinline__ void block_sums(const float (&acc)[kMaxRed], int nred, FF* scratch, double* out) {
+  constexpr int kW = kWorkThreads / 32;
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const FF b{__shfl_down_sync(0xffffffffu, a.hi, off), __shfl_down_sync(0xffffffffu, a.lo, off)};
-    a = ff_add(a, b);
+  for (int k = 0; k < kMaxRed; ++k) {
+    if (k >= nred) break;
+    FF a{acc[k], 0.0f};
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const FF b{__shfl_down_sync(0xffffffffu, a.hi, off), __shfl_down_sync(0xffffffffu, a.lo, off)};
+      a = ff_add(a, b);
+    }
+    if ((threadIdx.x & 31) == 0) scratch[k * kW + (threadIdx.x >> 5)] = a;
   }
-  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = a;
   work_sync();
-  FF r{0.0f, 0.0f};
-  if (threadIdx.x == 0)
-    for (int w = 0; w < kWorkThreads / 32; ++w) r = ff_add(r, scratch[w]);
+  if ((int)threadIdx.x < nred) {
+    FF r{0.0f, 0.0f};
+    for (int w = 0; w < kW; ++w) r = ff_add(r, scratch[threadIdx.x * kW + w]);
+    out[threadIdx.x] = (double)r.hi + (double)r.lo;
+  }
   work_sync();
-  return r;
 }
 
 // logical coordinate of axis `a` for element (outer o, inner i) (a != sweep axis)
@@ -712,7 +722,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   __shared__ __align__(16) TcParams tp;  // the pass of the work warps' current tile
   __shared__ TileTabs tabs;
   __shared__ uint32_t tmem_base_s;
-  __shared__ FF scratch[kWorkThreads / 32];
+  __shared__ FF scratch[kMaxRed * (kWorkThreads / 32)];
   __shared__ double blk_red[kMaxRed];
   __shared__ double totals[kMaxRed];
   __shared__ int s_last;
@@ -956,10 +966,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
 
       // norm partials of this tile (float-float, fixed order) and the pass ticket first, so
       // the fence waits for no state store and the ticket's round trip overlaps the store
-      for (int k = 0; k < p.nred; ++k) {
-        const FF t = block_sum(acc[k], scratch);
-        if (tid == 0) blk_red[k] = (double)t.hi + (double)t.lo;
-      }
+      block_sums(acc, p.nred, scratch, blk_red);
       unsigned int ticket = 0u;
       if (tid == 0) {
         for (int k = 0; k < p.nred; ++k) p.partials[(int64_t)k * g.tiles + tile] = blk_red[k];
