@@ -11,13 +11,13 @@
 // radial points).  A tile is BN complex columns of the inner axis for all n rows.
 // Treating (re, im) as two real columns, a lane-matrix product is the real GEMM
 // D[M x 2BN] = A[M x n] . B[n x 2BN], A the (zero-padded) matrix, B the tile:
-//   n <= 128: M = 128, BN = 64 (N = 128), A chunks of K = 16
-//   n = 256 : M = 256 as two 128-row halves, BN = 32 (N = 64), A chunks of K = 8
-// (wide N: every tcgen05.mma instruction has a fixed issue cost, so few wide ones)
+//   n <= 128: M = 128, BN = 32 (N = 64), A chunks of K = 16
+//   n = 256 : M = 256 as two 128-row halves, BN = 16 (N = 32), A chunks of K = 8; a
+//             parity-structured Legendre pair as two K = 128 GEMMs (see tc_shape)
 // 3xTF32: A = A_hi + A_lo (split once from the FP64 matrix on the host), B = B_hi +
 // B_lo (split on the fly), both parts tf32-exact, D = A_hi B_hi + A_hi B_lo + A_lo B_hi.
 //
-// Persistent CTAs, one per SM, each walking its share of the tiles of the launch:
+// Persistent CTAs, two per SM, each walking its share of the tiles of the launch:
 //   warps 0-7  load the tile, run the point-wise ops, split it into the B operand,
 //              drain the accumulators, run the ops between / after the matrices,
 //              store, and fold the norms (named barrier 1 among themselves)
@@ -25,7 +25,7 @@
 //              shared-memory stages by bulk TMA (it runs ahead across tiles)
 //   warp 9     issues tcgen05.mma (one lane) as chunks land and the B operand is ready
 // The tensor core truncates its FP32 accumulation, so the A_hi B_hi products go to
-// three 128-column TMEM regions a couple of K steps each and the work warps drain the
+// three TMEM regions a couple of K steps each and the work warps drain the
 // regions into registers (round-to-nearest adds) every kFillSteps K steps; the
 // corrections, 2^-11 smaller, share a fourth region.  FP32 norm partials are folded per tile in
 // float-float and across tiles in FP64 by the last tile of the pass, in a fixed order.
