@@ -1092,7 +1092,7 @@ static bool configure_once(const void* kern, bool& flag) {
   return true;
 }
 
-// persistent grid: one CTA per SM (fewer when there are fewer tiles)
+// persistent grid: kCtasPerSm CTAs per SM (fewer when there are fewer tiles)
 static unsigned persistent_grid(int64_t tiles) {
   static int sms = 0;
   if (sms == 0) {

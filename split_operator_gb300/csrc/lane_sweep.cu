@@ -12,10 +12,13 @@
 // FFT: Stockham autosort between two shared-memory buffers (radix 8 stages for FP64,
 // radix 16 for FP32, one smaller closing stage), register butterflies, twiddles from
 // an FP64-built table, the 1/sqrt(N) of the reference folded into the last stage.
-// Lanes shorter than 16 or of non power-of-two length use a direct DFT with the same
+// Lanes shorter than 16 or of non power-of-two length use a direct DFT with the natural
 // table.  The lane matrix product also writes into the second buffer.
-// Norms: FP64 per-thread sums, fixed-order warp/block trees, per-CTA partials folded
-// by the last CTA in a fixed order, so results do not depend on scheduling.
+// Norms: per-thread sums (FP32 in FP32 passes, FP64 in FP64 ones), fixed-order warp/block
+// trees, per-CTA partials folded by the last CTA in a fixed order, so results do not
+// depend on scheduling.
+// The radial pass of the 2-D step ([FFT] [point-wise] [FFT] [point-wise] on contiguous
+// power-of-two FP32 lanes) runs the separate register-resident FFT-pair kernel below.
 #include <cstdio>
 
 #include "common.cuh"
