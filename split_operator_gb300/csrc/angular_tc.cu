@@ -769,8 +769,8 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
     const int i = 32 * lg + lane;                    // TMEM lane within a 128-row half
     const int j = (S.mh == 2 ? 128 * up : 0) + i;    // lane-axis row of a plain drain
     const bool row_ok = j < n;
-    // 64 FP32 columns per thread.  Plain: n <= 128 the upper warps take the second half
-    // of N = 128, n = 256 the second 128-row half (its N = 64 columns).  Parity split,
+    // kVals FP32 columns per thread.  Plain: n <= 128 the upper warps take the second half
+    // of N = 64, n = 256 the second 128-row half (its N = 32 columns).  Parity split,
     // sum / difference matrix: as plain, the row of half h lane i being 2 i + h.  Even /
     // odd matrix: columns 16 up .. 16 up + 15 of both halves (E, O), rows i and n-1-i.
     const int c0 = S.mh == 2 ? 0 : (kVals / 2) * up;  // complex column of v[0..1] (plain)
