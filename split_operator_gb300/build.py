@@ -15,7 +15,10 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libsplit_operator_gb300.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"] + ARCH
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+         # host-side warnings (misleading indentation, dangling else, unused values) are errors
+         "-Xcompiler", "-Wall", "-Xcompiler", "-Werror=misleading-indentation",
+         "-Xcompiler", "-Werror=dangling-else"] + ARCH
 
 
 def sources():
