@@ -275,6 +275,7 @@ int so_propagation_describe(so_propagation p, char* buf, size_t cap);
  * and clears the record. */
 int so_propagation_set_timing(so_propagation p, int enabled);
 int so_propagation_kernel_times(so_propagation p, char* buf, size_t cap);
+void so_propagation_free(so_propagation p);
 
 /* ---- Batched propagation (no counterpart in the reference, which runs one
  * Propagation at a time) ----
@@ -344,7 +345,6 @@ void so_mlp_free(so_mlp m);
  * that overlap on the GPU (other streams, other threads) race. */
 int so_fft_norm_noalloc(double* psi, size_t lanes, size_t n, int direction, const double* lane_weights,
                         const double* weights, double* norm_out, void* stream);
-void so_propagation_free(so_propagation p);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop
