@@ -284,7 +284,8 @@ void so_propagation_free(so_propagation p);
  * the repeated part is replayed from a captured CUDA graph.  The propagations keep
  * their own state (so_propagation_get_array, losses, norms stay valid) and must share
  * the step's pass structure (same operator stack kinds); savers are not allowed.
- * Work is issued on the first propagation's stream. */
+ * Work is issued on the first propagation's stream.  The batch shares its members: a
+ * propagation freed by the caller first stays alive until so_batch_free. */
 typedef struct so_batch_t* so_batch;
 int so_batch_new(const so_propagation* props, size_t count, so_batch* out);
 /* `steps` steps of every propagation (Propagation::step, propagation.rs:134-182) */

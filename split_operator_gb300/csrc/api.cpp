@@ -22,9 +22,11 @@ struct so_operation_stack_t {
   std::shared_ptr<so::OperationStack> st;
 };
 struct so_propagation_t {
-  std::unique_ptr<so::Propagation> p;
+  std::shared_ptr<so::Propagation> p;
 };
+// the batch shares its members (declared first, so they outlive the executor)
 struct so_batch_t {
+  std::vector<std::shared_ptr<so::Propagation>> members;
   std::unique_ptr<so::Batch> b;
 };
 
@@ -938,11 +940,14 @@ int so_batch_new(const so_propagation* props, size_t count, so_batch* out) {
   return guard([&] {
     need(props && out && count > 0, "null argument");
     std::vector<so::Propagation*> ps;
+    std::vector<std::shared_ptr<so::Propagation>> members;
     for (size_t i = 0; i < count; ++i) {
       need(props[i] != nullptr, "null propagation");
       ps.push_back(props[i]->p.get());
+      members.push_back(props[i]->p);
     }
-    *out = new so_batch_t{std::make_unique<so::Batch>(ps)};
+    auto exec = std::make_unique<so::Batch>(ps);
+    *out = new so_batch_t{std::move(members), std::move(exec)};
   });
 }
 int so_batch_steps(so_batch b, uint64_t steps) {
