@@ -127,3 +127,22 @@ def test_legendre_operator_matrices_are_built(so):
     t = so.legendre_diagonalization_operator(p)
     assert t.grid_transformation.name == "angular_momentum"
     np.testing.assert_array_equal(t.grid_transformation.weights, np.ones(6))
+
+
+def test_without_a_gpu_the_device_path_fails_loudly(so):
+    """Wave functions live in GPU memory: with no device the call returns SO_ERR_CUDA with a
+    message (no host fallback).  Batch entry points reject null handles before any device work."""
+    import ctypes
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from split_operator_gb300 import _lib
+    g = so.Grid.new_linear_continuos("x", -4.0, 4.0, 64, 0)
+    with pytest.raises(so.SplitOperatorError) as e:
+        so.WaveFunction(so.gaussian_distribution(g.nodes, 0.0, 0.5, 0.0), [g])
+    assert e.value.status == 3 and "CUDA" in str(e.value)
+    h = _lib.lib()
+    out = ctypes.c_void_p()
+    assert h.so_batch_new(None, 0, ctypes.byref(out)) == 1 and h.so_last_error() == b"null argument"
+    assert h.so_batch_steps(None, 1) == 1
+    assert h.so_batch_steps_host(None, None, None, 0, 1) == 1
