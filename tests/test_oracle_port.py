@@ -35,3 +35,17 @@ def test_port_harmonic_1d_matches_oracle():
     port.run(200)
     oprop.propagate(200)
     assert rel_l2(port.psi, oprop.wave_function.array) < 1e-12
+
+
+def test_port_matches_oracle_on_batch_instance_parameters():
+    """The reference arm times the port on instances of the batched workload (seeded Morse
+    D, a, re and P2 strength beta per instance): the port follows the oracle there too."""
+    from split_operator_gb300 import workloads as W
+    for prm in W.batched_instance_params(3):
+        kw = dict(seed=prm["seed"], d=prm["d"], a=prm["a"], re=prm["re"], beta=prm["beta"])
+        port = P.RadialAngular(256, 32, **kw)
+        oprop, damp = S.radial_angular_2d(nr=256, nth=32, step_no=10, **kw)
+        port.run(10, threads=2)
+        oprop.propagate(10)
+        assert rel_l2(port.psi, oprop.wave_function.array) < 1e-12
+        assert abs(port.loss[0] - damp.loss().loss()) < 1e-14
