@@ -275,6 +275,20 @@ int so_propagation_describe(so_propagation p, char* buf, size_t cap);
  * and clears the record. */
 int so_propagation_set_timing(so_propagation p, int enabled);
 int so_propagation_kernel_times(so_propagation p, char* buf, size_t cap);
+/* Checkpoint / resume (no counterpart in the reference, whose savers keep frames only).
+ * A checkpoint holds everything the next steps read: the state (exactly, in the
+ * propagation's storage precision), the norm cache, every loss checker's loss and last
+ * norm, the leak-control norm, the savers' frames and the step count; the fields the
+ * reference steps are loss_checker.rs:49-68, leak_control.rs:31-45 and the savers of
+ * wave_function_saver.rs:42-64.  so_propagation_checkpoint with buf == NULL only reports
+ * the size; a cap below the size is SO_ERR_INVALID.  so_propagation_restore accepts a
+ * checkpoint of a propagation with the same shape, precision and operator stack (any
+ * propagation built the same way, in this process or another) and continues exactly as
+ * the propagation that took it would have: bit for bit. */
+int so_propagation_checkpoint(so_propagation p, void* buf, size_t cap, size_t* size);
+int so_propagation_restore(so_propagation p, const void* buf, size_t size);
+/* steps of Propagation::step taken since creation (restore sets the checkpoint's count) */
+int so_propagation_steps_done(so_propagation p, uint64_t* out);
 void so_propagation_free(so_propagation p);
 
 /* ---- Batched propagation (no counterpart in the reference, which runs one
@@ -332,18 +346,20 @@ void so_mlp_free(so_mlp m);
  * they run: code inside a strict device memory pool, or a host framework that hands
  * over only pre-sized buffers.  Every pointer is the caller's device memory.
  * In place on psi (complex128, `lanes` contiguous lanes of `n` points, row-major):
- * the unitary DFT of every lane (direction -1 = FFTTransformation::transform, +1 =
- * inverse_transform, fft_transformation.rs:53-88), then, when `weights` is given,
- * *norm_out = sum |psi|^2 lane_weights[l] weights[x] (WaveFunction::norm with the
- * grids' weights, wave_function.rs:68-85); `lane_weights`, `weights`, `norm_out` are
- * all given or all NULL.  Issued on `stream` (cudaStream_t; NULL = legacy stream).
+ * every lane becomes its unitary discrete Fourier transform,
+ *   psi'[l][k] = n^(-1/2) sum_x psi[l][x] exp(direction * 2 pi i x k / n)
+ * (direction -1 forward, +1 inverse); then, when `weights` is given,
+ *   *norm_out = sum_{l,x} |psi'[l][x]|^2 lane_weights[l] weights[x].
+ * `lane_weights`, `weights` and `norm_out` are all given or all NULL.  Issued on
+ * `stream` (cudaStream_t; NULL = legacy stream).
  * Limits: n <= 4096 and at most 65536 CTAs of lanes (SO_ERR_UNSUPPORTED beyond).
  * The kernel's scratch (norm partials, a ticket counter) and the twiddle table are
  * fixed file-scope device arrays (about 0.6 MiB, held by every GPU that loads the
  * library until exit); no cudaMalloc / cudaFree is called.  The first call on a
  * device looks up those arrays' device addresses: make it before any stream
- * capture.  All calls share the arrays, which keep the last call's contents: calls
- * that overlap on the GPU (other streams, other threads) race. */
+ * capture.  All calls share the arrays, which keep the last call's contents (every
+ * call rebuilds the twiddle table and clears the counter itself): calls that overlap
+ * on the GPU (other streams, other threads) race. */
 int so_fft_norm_noalloc(double* psi, size_t lanes, size_t n, int direction, const double* lane_weights,
                         const double* weights, double* norm_out, void* stream);
 

@@ -130,6 +130,9 @@ SIGNATURES = {
     "so_propagation_describe": [_P, C.c_char_p, _S],
     "so_propagation_set_timing": [_P, _I],
     "so_propagation_kernel_times": [_P, C.c_char_p, _S],
+    "so_propagation_checkpoint": [_P, _P, _S, _SP],
+    "so_propagation_restore": [_P, _P, _S],
+    "so_propagation_steps_done": [_P, C.POINTER(C.c_uint64)],
     "so_fft_norm_noalloc": [_P, _S, _S, _I, _P, _P, _P, _P],
     "so_batch_new": [_PP, _S, _PP],
     "so_batch_steps": [_P, C.c_uint64],

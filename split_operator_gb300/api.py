@@ -644,6 +644,31 @@ class Propagation(_Handle):
     def set_timing(self, enabled: bool):
         call("so_propagation_set_timing", self._h, 1 if enabled else 0)
 
+    def steps_done(self) -> int:
+        v = C.c_uint64()
+        call("so_propagation_steps_done", self._h, C.byref(v))
+        return v.value
+
+    def checkpoint(self) -> bytes:
+        """Everything the next steps read (state, norm cache, losses, leak norm, savers,
+        step count) as one byte string; restore() on a propagation built the same way
+        continues bit for bit."""
+        n = C.c_size_t()
+        call("so_propagation_checkpoint", self._h, None, 0, C.byref(n))
+        buf = C.create_string_buffer(n.value)
+        call("so_propagation_checkpoint", self._h, buf, n.value, C.byref(n))
+        return buf.raw[: n.value]
+
+    def restore(self, blob: bytes):
+        call("so_propagation_restore", self._h, C.c_char_p(blob), len(blob))
+
+    def save_checkpoint(self, path: str):
+        """The checkpoint as a one-dimensional uint8 .npy file."""
+        np.save(path, np.frombuffer(self.checkpoint(), dtype=np.uint8))
+
+    def load_checkpoint(self, path: str):
+        self.restore(np.load(path).tobytes())
+
     def kernel_times(self):
         """[(pass name, launches, total_ms, algorithmic bytes)] since the last call."""
         buf = C.create_string_buffer(1 << 16)

@@ -934,6 +934,29 @@ int so_propagation_kernel_times(so_propagation p, char* buf, size_t cap) {
     std::snprintf(buf, cap, "%s", p->p->kernel_times().c_str());
   });
 }
+int so_propagation_checkpoint(so_propagation p, void* buf, size_t cap, size_t* size) {
+  return guard([&] {
+    need(p && size, "null argument");
+    const std::vector<unsigned char> b = p->p->checkpoint();
+    *size = b.size();
+    if (buf) {
+      need(cap >= b.size(), "checkpoint buffer is smaller than the checkpoint");
+      std::memcpy(buf, b.data(), b.size());
+    }
+  });
+}
+int so_propagation_restore(so_propagation p, const void* buf, size_t size) {
+  return guard([&] {
+    need(p && buf, "null argument");
+    p->p->restore(static_cast<const unsigned char*>(buf), size);
+  });
+}
+int so_propagation_steps_done(so_propagation p, uint64_t* out) {
+  return guard([&] {
+    need(p && out, "null argument");
+    *out = p->p->steps_done();
+  });
+}
 void so_propagation_free(so_propagation p) { delete p; }
 
 int so_batch_new(const so_propagation* props, size_t count, so_batch* out) {

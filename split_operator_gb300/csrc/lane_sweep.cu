@@ -713,8 +713,8 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
 // both FFTs' outer stages and of the point-wise ops, and the second tile buffer.
 constexpr int kPairV = 16;
 
-template <int RS>
-__device__ __forceinline__ void pair_load_smem(float2 (&v)[kPairV], const float2* buf, int t, int T, int lgnb,
+template <int RS, typename C>
+__device__ __forceinline__ void pair_load_smem(C (&v)[kPairV], const C* buf, int t, int T, int lgnb,
                                                int ls) {
   const int nb = 1 << lgnb;
 #pragma unroll
@@ -725,8 +725,8 @@ __device__ __forceinline__ void pair_load_smem(float2 (&v)[kPairV], const float2
   }
 }
 
-template <int RS>
-__device__ __forceinline__ void pair_store_smem(const float2 (&v)[kPairV], float2* buf, int t, int T, int lgnb,
+template <int RS, typename C>
+__device__ __forceinline__ void pair_store_smem(const C (&v)[kPairV], C* buf, int t, int T, int lgnb,
                                                 int p, int ls) {
   const int nb = 1 << lgnb;
 #pragma unroll
@@ -740,22 +740,22 @@ __device__ __forceinline__ void pair_store_smem(const float2 (&v)[kPairV], float
 
 // first stage (p = 1) inputs straight from the lanes in global memory (invalid lanes: 0)
 // (psi: the tile's first lane; nl: its valid lanes; offsets within a tile fit 32 bits)
-template <int RS>
-__device__ __forceinline__ void pair_load_global(float2 (&v)[kPairV], const float2* __restrict__ psi, int t, int T,
-                                                 int lgnb, int nl, int n) {
+template <int RS, typename C>
+__device__ __forceinline__ void pair_load_global(C (&v)[kPairV], const C* __restrict__ psi, int t, int T, int lgnb,
+                                                 int nl, int n) {
   const int nb = 1 << lgnb;
 #pragma unroll
   for (int j = 0; j < kPairV / RS; ++j) {
     const int b = t + j * T, l = b >> lgnb, i = b & (nb - 1);
     const int o = l * n + i;
 #pragma unroll
-    for (int r = 0; r < RS; ++r) v[j * RS + r] = l < nl ? psi[o + r * nb] : float2{0.f, 0.f};
+    for (int r = 0; r < RS; ++r) v[j * RS + r] = l < nl ? psi[o + r * nb] : C{0, 0};
   }
 }
 
-template <int RS>
-__device__ __forceinline__ void pair_butterflies(float2 (&v)[kPairV], int t, int T, int lgnb, int p, int dir,
-                                                 const float2* __restrict__ tw) {
+template <int RS, typename C>
+__device__ __forceinline__ void pair_butterflies(C (&v)[kPairV], int t, int T, int lgnb, int p, int dir,
+                                                 const C* __restrict__ tw) {
   const int nb = 1 << lgnb;
 #pragma unroll
   for (int j = 0; j < kPairV / RS; ++j) {
@@ -763,7 +763,7 @@ __device__ __forceinline__ void pair_butterflies(float2 (&v)[kPairV], int t, int
     if (k > 0) {
 #pragma unroll
       for (int r = 1; r < RS; ++r) {
-        float2 w = __ldg(tw + (r - 1) * p + k);
+        C w = __ldg(tw + (r - 1) * p + k);
         if (dir > 0) w.y = -w.y;
         v[j * RS + r] = cmul(v[j * RS + r], w);
       }
@@ -774,17 +774,17 @@ __device__ __forceinline__ void pair_butterflies(float2 (&v)[kPairV], int t, int
 
 // point-wise ops [ob, oe) on the outputs of a last stage: value j RS + q sits at lane
 // b >> lgnb, point x = k + q p with k = b & (p - 1), p = 2^lgnb
-template <int RS>
-__device__ __forceinline__ void pair_pointwise(float2 (&v)[kPairV], const PassParams& pp, int ob, int oe, int t,
-                                               int T, int lgnb, int64_t lane0, int nl, float sc) {
+template <int RS, typename C, typename R>
+__device__ __forceinline__ void pair_pointwise(C (&v)[kPairV], const PassParams& pp, int ob, int oe, int t, int T,
+                                               int lgnb, int64_t lane0, int nl, R sc) {
   const int p = 1 << lgnb, n = (int)pp.g.n;
 #pragma unroll
-  for (int e = 0; e < kPairV; ++e) v[e] = float2{v[e].x * sc, v[e].y * sc};
+  for (int e = 0; e < kPairV; ++e) v[e] = C{v[e].x * sc, v[e].y * sc};
   for (int oi = ob; oi < oe; ++oi) {
     const DevOp& op = pp.ops[oi];
     const bool nd = op.kind == OP_DIAGND;
     // DIAGND: the tile's rows of the full table; DIAG1D along the lane: the lane table
-    const float2* tab = reinterpret_cast<const float2*>(op.ptr) + (nd ? lane0 * n : 0);
+    const C* tab = reinterpret_cast<const C*>(op.ptr) + (nd ? lane0 * n : 0);
 #pragma unroll
     for (int j = 0; j < kPairV / RS; ++j) {
       const int b = t + j * T, l = b >> lgnb, k = b & (p - 1);
@@ -797,9 +797,9 @@ __device__ __forceinline__ void pair_pointwise(float2 (&v)[kPairV], const PassPa
   }
 }
 
-template <int RS>
-__device__ __forceinline__ void pair_store_global(const float2 (&v)[kPairV], float2* __restrict__ psi, int t, int T,
-                                                  int lgnb, int nl, int n) {
+template <int RS, typename C>
+__device__ __forceinline__ void pair_store_global(const C (&v)[kPairV], C* __restrict__ psi, int t, int T, int lgnb,
+                                                  int nl, int n) {
   const int p = 1 << lgnb;
 #pragma unroll
   for (int j = 0; j < kPairV / RS; ++j) {
@@ -816,83 +816,99 @@ __device__ __forceinline__ void pair_store_global(const float2 (&v)[kPairV], flo
 enum PairIn { PIN_GLOBAL, PIN_SMEM, PIN_REGS };
 enum PairOut { POUT_SMEM, POUT_REGS, POUT_GLOBAL };
 
-template <int RS>
-__device__ __forceinline__ void pair_stage_rs(float2 (&v)[kPairV], float2* buf, const PassParams& pp, int in,
-                                              int out, int p, int dir, const float2* tw, int ob, int oe,
-                                              int64_t lane0, float sc) {
+template <int RS, typename C, typename R>
+__device__ __forceinline__ void pair_stage_rs(C (&v)[kPairV], C* buf, const PassParams& pp, int in, int out, int p,
+                                              int dir, const C* tw, int ob, int oe, int64_t lane0, R sc) {
   const Geometry& g = pp.g;
   const int t = threadIdx.x, T = blockDim.x, n = (int)g.n, ls = g.lane_stride;
   const int lgnb = __ffs(n / RS) - 1;
   const int64_t rem = g.outer - lane0;
   const int nl = rem < g.lanes_per_tile ? (int)rem : g.lanes_per_tile;  // valid lanes of the tile
-  float2* tile_psi = reinterpret_cast<float2*>(pp.psi) + lane0 * n;
+  C* tile_psi = reinterpret_cast<C*>(pp.psi) + lane0 * n;
   if (in == PIN_GLOBAL) {
-    pair_load_global<RS>(v, tile_psi, t, T, lgnb, nl, n);
+    pair_load_global<RS, C>(v, tile_psi, t, T, lgnb, nl, n);
   } else if (in == PIN_SMEM) {
-    pair_load_smem<RS>(v, buf, t, T, lgnb, ls);
+    pair_load_smem<RS, C>(v, buf, t, T, lgnb, ls);
     __syncthreads();  // every read of the stage before any write (in place)
   }
-  pair_butterflies<RS>(v, t, T, lgnb, p, dir, tw);
+  pair_butterflies<RS, C>(v, t, T, lgnb, p, dir, tw);
   if (out == POUT_SMEM) {
-    pair_store_smem<RS>(v, buf, t, T, lgnb, p, ls);
+    pair_store_smem<RS, C>(v, buf, t, T, lgnb, p, ls);
     __syncthreads();
   } else {
     // a last stage: p = n / RS = nb, outputs at k + q p
-    pair_pointwise<RS>(v, pp, ob, oe, t, T, lgnb, lane0, nl, sc);
-    if (out == POUT_GLOBAL) pair_store_global<RS>(v, tile_psi, t, T, lgnb, nl, n);
+    pair_pointwise<RS, C, R>(v, pp, ob, oe, t, T, lgnb, lane0, nl, sc);
+    if (out == POUT_GLOBAL) pair_store_global<RS, C>(v, tile_psi, t, T, lgnb, nl, n);
   }
 }
 
-__device__ __forceinline__ void pair_stage(int rs, float2 (&v)[kPairV], float2* buf, const PassParams& pp, int in,
-                                           int out, int p, int dir, const float2* tw, int ob, int oe, int64_t lane0,
-                                           float sc) {
+template <int RMAX, typename C, typename R>
+__device__ __forceinline__ void pair_stage(int rs, C (&v)[kPairV], C* buf, const PassParams& pp, int in, int out,
+                                           int p, int dir, const C* tw, int ob, int oe, int64_t lane0, R sc) {
+  if constexpr (RMAX == 16) {
+    if (rs == 16) {
+      pair_stage_rs<16, C, R>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc);
+      return;
+    }
+  }
   switch (rs) {
-    case 16: pair_stage_rs<16>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
-    case 8: pair_stage_rs<8>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
-    case 4: pair_stage_rs<4>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
-    default: pair_stage_rs<2>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
+    case 8: pair_stage_rs<8, C, R>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
+    case 4: pair_stage_rs<4, C, R>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
+    default: pair_stage_rs<2, C, R>(v, buf, pp, in, out, p, dir, tw, ob, oe, lane0, sc); break;
   }
 }
 
+// RMAX: the radix of the stages (16 for FP32, 8 for FP64: the radix of the stage-major
+// twiddle table each precision builds), S - 1 stages of RMAX and one closing radix rl
+template <typename R, int RMAX>
 __device__ __forceinline__ void fft_pair_tile(const PassParams& pp, int64_t tile) {
+  using C = typename Cx<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* buf = reinterpret_cast<float2*>(smem_raw);
+  C* buf = reinterpret_cast<C*>(smem_raw);
   const Geometry& g = pp.g;
   const int n = (int)g.n;
   const int64_t lane0 = tile * g.lanes_per_tile;
-  const float2* tw = reinterpret_cast<const float2*>(pp.twiddle);
-  const float sc = inv_sqrt_pow2<float>(__ffs(n) - 1);
+  const C* tw = reinterpret_cast<const C*>(pp.twiddle);
+  const R sc = inv_sqrt_pow2<R>(__ffs(n) - 1);
   int f1 = 1;
   while (f1 < pp.nops && pp.ops[f1].kind != OP_FFT) ++f1;
-  // the radices of fft_radices(n, 16, ...): S - 1 stages of 16 and the closing radix rl
+  // the radices of fft_radices(n, RMAX, ...): S - 1 stages of RMAX and the closing radix rl
   // (the forward order ends with it, the reversed order starts with it)
-  const int lg = __ffs(n) - 1, S = (lg + 3) / 4, rl = 1 << (lg - 4 * (S - 1));
-  float2 v[kPairV];
+  constexpr int kLgR = RMAX == 16 ? 4 : 3;
+  const int lg = __ffs(n) - 1, S = (lg + kLgR - 1) / kLgR, rl = 1 << (lg - kLgR * (S - 1));
+  C v[kPairV];
   int p = 1, off = 0;
   for (int s = 0; s < S; ++s) {
-    const int rs = s + 1 < S ? 16 : rl;
+    const int rs = s + 1 < S ? RMAX : rl;
     const int in = s == 0 ? PIN_GLOBAL : PIN_SMEM, out = s + 1 < S ? POUT_SMEM : POUT_REGS;
-    pair_stage(rs, v, buf, pp, in, out, p, pp.ops[0].dir, tw + off, 1, f1, lane0, sc);
+    pair_stage<RMAX, C, R>(rs, v, buf, pp, in, out, p, pp.ops[0].dir, tw + off, 1, f1, lane0, sc);
     if (p > 1) off += (rs - 1) * p;
     p *= rs;
   }
   p = 1;
   off = 0;
   for (int s = 0; s < S; ++s) {
-    const int rs = s == 0 ? rl : 16;
+    const int rs = s == 0 ? rl : RMAX;
     const int in = s == 0 ? PIN_REGS : PIN_SMEM, out = s + 1 < S ? POUT_SMEM : POUT_GLOBAL;
-    pair_stage(rs, v, buf, pp, in, out, p, pp.ops[f1].dir, tw + n + off, f1 + 1, pp.nops, lane0, sc);
+    pair_stage<RMAX, C, R>(rs, v, buf, pp, in, out, p, pp.ops[f1].dir, tw + n + off, f1 + 1, pp.nops, lane0, sc);
     if (p > 1) off += (rs - 1) * p;
     p *= rs;
   }
 }
 
 __global__ void __launch_bounds__(512, 2) fft_pair_kernel(const __grid_constant__ PassParams p) {
-  fft_pair_tile(p, blockIdx.x);
+  fft_pair_tile<float, 16>(p, blockIdx.x);
 }
 
-__global__ void __launch_bounds__(512, 2) fft_pair_kernel_batched(const PassParams* __restrict__ params,
-                                                                  const int64_t* __restrict__ offsets, int count) {
+// FP64 lanes of 8192 points (one lane of 16 values per thread for 512 threads: one CTA per
+// SM, whose 139 KB lane buffer leaves no room for a second)
+__global__ void __launch_bounds__(512, 1) fft_pair_kernel_f64(const __grid_constant__ PassParams p) {
+  fft_pair_tile<double, 8>(p, blockIdx.x);
+}
+
+template <typename R, int RMAX>
+__device__ __forceinline__ void fft_pair_batched_tile(const PassParams* __restrict__ params,
+                                                      const int64_t* __restrict__ offsets, int count) {
   const int64_t b = blockIdx.x;
   int lo = 0, hi = count - 1;
   while (lo < hi) {
@@ -906,14 +922,27 @@ __global__ void __launch_bounds__(512, 2) fft_pair_kernel_batched(const PassPara
   for (int k = threadIdx.x; k < (int)(sizeof(PassParams) / 4); k += blockDim.x)
     reinterpret_cast<uint32_t*>(&sp)[k] = reinterpret_cast<const uint32_t*>(params + lo)[k];
   __syncthreads();
-  fft_pair_tile(sp, b - offsets[lo]);
+  fft_pair_tile<R, RMAX>(sp, b - offsets[lo]);
+}
+
+__global__ void __launch_bounds__(512, 2) fft_pair_kernel_batched(const PassParams* __restrict__ params,
+                                                                  const int64_t* __restrict__ offsets, int count) {
+  fft_pair_batched_tile<float, 16>(params, offsets, count);
+}
+
+__global__ void __launch_bounds__(512, 1) fft_pair_kernel_batched_f64(const PassParams* __restrict__ params,
+                                                                      const int64_t* __restrict__ offsets, int count) {
+  fft_pair_batched_tile<double, 8>(params, offsets, count);
 }
 
 int fft_pair_threads(const Geometry& g) { return g.n >= 8192 ? 512 : 256; }
 
 bool fft_pair_plan(PassParams& p, bool fp64, bool resident) {
   Geometry& g = p.g;
-  if (fp64 || resident || g.inner != 1 || !stage_twiddles(g.n) || g.n > 8192 || p.twiddle == nullptr) return false;
+  if (resident || g.inner != 1 || !stage_twiddles(g.n) || g.n > 8192 || p.twiddle == nullptr) return false;
+  // FP64: only the lanes longer than the general pass's FP64 tile (4096 points) take the pair
+  // kernel; shorter FP64 lanes keep the general pass
+  if (fp64 && g.n <= 4096) return false;
   if (p.nops < 2 || p.ops[0].kind != OP_FFT) return false;
   int ffts = 0;
   for (int i = 0; i < p.nops; ++i) {
@@ -936,8 +965,8 @@ bool fft_pair_plan(PassParams& p, bool fp64, bool resident) {
   return true;
 }
 
-static size_t fft_pair_smem(const Geometry& g) {
-  return ((size_t)g.lanes_per_tile * g.lane_stride * sizeof(float2) + 15) & ~(size_t)15;
+static size_t fft_pair_smem(const Geometry& g, bool fp64) {
+  return ((size_t)g.lanes_per_tile * g.lane_stride * (fp64 ? sizeof(double2) : sizeof(float2)) + 15) & ~(size_t)15;
 }
 
 template <typename R, int RMAX, bool SWEEP>
@@ -988,15 +1017,18 @@ cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassPar
                                 const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
                                 cudaStream_t s) {
   if (fused) {
-    if (fp64 || smem > 220 * 1024 || threads > 512) return cudaErrorInvalidValue;
-    static bool configured = false;
-    if (!configured) {
-      cudaError_t e = cudaFuncSetAttribute(fft_pair_kernel_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           220 * 1024);
+    if (smem > 220 * 1024 || threads > 512) return cudaErrorInvalidValue;
+    static bool configured[2] = {false, false};
+    const void* kern = fp64 ? (const void*)fft_pair_kernel_batched_f64 : (const void*)fft_pair_kernel_batched;
+    if (!configured[fp64 ? 1 : 0]) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       if (e != cudaSuccess) return e;
-      configured = true;
+      configured[fp64 ? 1 : 0] = true;
     }
-    fft_pair_kernel_batched<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
+    if (fp64)
+      fft_pair_kernel_batched_f64<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
+    else
+      fft_pair_kernel_batched<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
     count_launch();
     return cudaGetLastError();
   }
@@ -1009,7 +1041,7 @@ cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassPar
 
 size_t pass_smem_bytes(const PassParams& p, bool fp64) {
   const Geometry& g = p.g;
-  if (p.fused) return fft_pair_smem(g);
+  if (p.fused) return fft_pair_smem(g, fp64);
   const bool fft = p.twiddle != nullptr;
   const size_t cs = fp64 ? 16 : 8;
   size_t b = (p.one_buffer ? 1 : 2) * (((size_t)g.lanes_per_tile * g.lane_stride * cs + 15) & ~(size_t)15);
@@ -1059,6 +1091,20 @@ static cudaError_t launch_impl(const PassParams& p, cudaStream_t s) {
 }
 
 cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s) {
+  if (p.fused) {
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e =
+          cudaFuncSetAttribute(fft_pair_kernel_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    const size_t smem = fft_pair_smem(p.g, true);
+    if (smem > 220 * 1024) return cudaErrorInvalidValue;
+    fft_pair_kernel_f64<<<(unsigned)p.g.tiles, fft_pair_threads(p.g), smem, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+  }
   return p.sweep ? launch_impl<double, 8, true>(p, s) : launch_impl<double, 8, false>(p, s);
 }
 cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s) {
@@ -1070,7 +1116,7 @@ cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s) {
       if (e != cudaSuccess) return e;
       configured = true;
     }
-    const size_t smem = fft_pair_smem(p.g);
+    const size_t smem = fft_pair_smem(p.g, false);
     if (smem > 220 * 1024) return cudaErrorInvalidValue;
     fft_pair_kernel<<<(unsigned)p.g.tiles, fft_pair_threads(p.g), smem, s>>>(p);
     count_launch();

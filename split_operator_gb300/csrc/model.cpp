@@ -152,11 +152,13 @@ Geometry Engine::geometry(int sweep_axis, bool resident) const {
   for (int q = g.spos + 1; q < nd; ++q) g.inner *= g.sshape[q];
   g.outer = 1;
   for (int q = 0; q < g.spos; ++q) g.outer *= g.sshape[q];
-  // two tile buffers of at most ~139 KB together
+  // two tile buffers of at most ~139 KB together; FP64 lanes of 4097..8192 points only in
+  // FFT-pair passes (one in-place lane buffer), which Engine::launch checks
   const int64_t tile_max = fp64 ? 4096 : 8192;
+  const int64_t lane_max = resident ? tile_max : 8192;
   g.vals = 8;
-  if (g.n > tile_max)
-    throw Error(SO_ERR_UNSUPPORTED, "lanes longer than " + std::to_string(tile_max) + " points are not supported");
+  if (g.n > lane_max)
+    throw Error(SO_ERR_UNSUPPORTED, "lanes longer than " + std::to_string(lane_max) + " points are not supported");
   int64_t L;
   if (resident) {
     if (g.inner == 1)
@@ -169,14 +171,14 @@ Geometry Engine::geometry(int sweep_axis, bool resident) const {
     g.tiles_per_outer = 1;
     g.tiles = 1;
   } else if (g.inner == 1) {
-    const int64_t lmax = std::max<int64_t>(1, pow2_floor(tile_max / g.n));
+    const int64_t lmax = std::max<int64_t>(1, pow2_floor(std::max<int64_t>(1, tile_max / g.n)));
     int64_t want = pow2_floor(std::max<int64_t>(1, g.outer / 304));
     want = std::max<int64_t>(want, pow2_floor(std::max<int64_t>(1, 1024 / g.n)));
     L = std::min(want, lmax);
     g.tiles_per_outer = 1;
     g.tiles = (g.outer + L - 1) / L;
   } else {
-    const int64_t lmax = std::max<int64_t>(1, pow2_floor(tile_max / g.n));
+    const int64_t lmax = std::max<int64_t>(1, pow2_floor(std::max<int64_t>(1, tile_max / g.n)));
     L = std::min<int64_t>({lmax, fp64 ? 16 : 32, pow2_floor(g.inner)});
     while (L > 4 && g.outer * ((g.inner + L - 1) / L) < 304) L /= 2;
     g.tiles_per_outer = (int32_t)((g.inner + L - 1) / L);
@@ -521,7 +523,10 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   if (fft) p.twiddle = twiddle((size_t)p.g.n);
   pass_choose_buffers(p, fp64);
   if (!fp64 && (tc_tf32 || tc_bf16) && !resident && try_launch_tc(ops, axis, p)) return;
-  if (fft_pair && fft_pair_plan(p, fp64, resident)) name_tag = " fftpair";
+  if ((fft_pair || (fp64 && p.g.n > 4096)) && fft_pair_plan(p, fp64, resident)) name_tag = " fftpair";
+  if (fp64 && p.g.n > 4096 && !p.fused)
+    throw Error(SO_ERR_UNSUPPORTED, "FP64 lanes longer than 4096 points are not supported outside FFT-pair passes "
+                                    "([FFT] [point-wise] [FFT] [point-wise] on contiguous power-of-two lanes)");
   if (!resident && (size_t)p.g.tiles > partials_cap_) {
     partials_cap_ = (size_t)p.g.tiles;
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
@@ -566,12 +571,18 @@ void Engine::timed_begin(const std::string& name) {
 void Engine::timed_end() { cuda_check(cudaEventRecord(timed_.back().b, stream), "event record"); }
 
 double Engine::pass_bytes(const std::vector<DevOp>& ops, const Geometry& g) const {
-  // algorithmic bytes: read + write of the state, plus every full-size table streamed
+  // algorithmic bytes: read + write of the state, plus each distinct full-size table the
+  // pass streams, once (a table applied twice in one pass -- the V/2 phase at the end of
+  // one step and the start of the next -- is read once)
   double pts = 1.0;
   for (int q = 0; q < g.ndim; ++q) pts *= (double)g.sshape[q];
   double b = 2.0 * pts * (double)elem_bytes();
+  std::vector<const void*> seen;
   for (const DevOp& o : ops)
-    if (o.kind == OP_DIAGND || o.kind == OP_DOT) b += pts * (double)elem_bytes();
+    if ((o.kind == OP_DIAGND || o.kind == OP_DOT) && std::find(seen.begin(), seen.end(), o.ptr) == seen.end()) {
+      seen.push_back(o.ptr);
+      b += pts * (double)elem_bytes();
+    }
   return b;
 }
 
@@ -1201,6 +1212,7 @@ static bool same_program(const std::vector<Action>& a, const std::vector<Action>
 
 void Propagation::steps(uint64_t n) {
   Engine& e = *wf_->eng;
+  steps_done_ += n;
   if (!e.resident_capable()) {
     Emitter em{&e};
     for (uint64_t i = 0; i < n; ++i) step(em);
@@ -1309,6 +1321,178 @@ std::unique_ptr<WaveFunction> Propagation::snapshot() {
   w->eng->import_host(host.data());
   w->eng->sync();
   return w;
+}
+
+// ------------------------------------------------------------ checkpoint / resume
+// Byte layout (native endianness; a checkpoint is read back on the same kind of host):
+//   "SOCKPT01", precision i32, ndim u64, shape u64 x ndim, steps_done u64,
+//   possible_norm_change u8, norm cache f64, per axis: current grid name, last seen name;
+//   operator count u64, per operator: type name, scalar count u64, scalars f64 x count,
+//   saver flag u8 [current_frame u64, times, data]; then the state as complex128 in the
+//   logical row-major order (exact for both state precisions: FP32 values are FP64 values).
+namespace {
+struct BlobWriter {
+  std::vector<unsigned char> b;
+  void bytes(const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    b.insert(b.end(), c, c + n);
+  }
+  template <class T>
+  void put(const T& v) {
+    bytes(&v, sizeof(T));
+  }
+  void str(const std::string& s) {
+    put<uint64_t>(s.size());
+    bytes(s.data(), s.size());
+  }
+  void vec(const std::vector<double>& v) {
+    put<uint64_t>(v.size());
+    bytes(v.data(), v.size() * sizeof(double));
+  }
+};
+struct BlobReader {
+  const unsigned char* p;
+  size_t n, off = 0;
+  void bytes(void* dst, size_t k) {
+    if (off + k > n) throw Error(SO_ERR_INVALID, "checkpoint is truncated");
+    std::memcpy(dst, p + off, k);
+    off += k;
+  }
+  template <class T>
+  T get() {
+    T v;
+    bytes(&v, sizeof(T));
+    return v;
+  }
+  std::string str() {
+    const uint64_t k = get<uint64_t>();
+    if (k > n - off) throw Error(SO_ERR_INVALID, "checkpoint is truncated");
+    std::string s(reinterpret_cast<const char*>(p + off), (size_t)k);
+    off += (size_t)k;
+    return s;
+  }
+  std::vector<double> vec() {
+    const uint64_t k = get<uint64_t>();
+    if (k > (n - off) / sizeof(double)) throw Error(SO_ERR_INVALID, "checkpoint is truncated");
+    std::vector<double> v((size_t)k);
+    bytes(v.data(), v.size() * sizeof(double));
+    return v;
+  }
+};
+constexpr char kCkptMagic[8] = {'S', 'O', 'C', 'K', 'P', 'T', '0', '1'};
+}  // namespace
+
+std::vector<unsigned char> Propagation::checkpoint() {
+  Engine& e = *wf_->eng;
+  e.flush();
+  BlobWriter w;
+  w.bytes(kCkptMagic, sizeof(kCkptMagic));
+  w.put<int32_t>(precision);
+  w.put<uint64_t>(wf_->shape.size());
+  for (size_t s : wf_->shape) w.put<uint64_t>(s);
+  w.put<uint64_t>(steps_done_);
+  w.put<uint8_t>(wf_->possible_norm_change ? 1 : 0);
+  w.put<double>(e.read_slot(wf_->cache_slot));
+  for (size_t a = 0; a < wf_->shape.size(); ++a) {
+    w.str(wf_->grids[a].name);
+    w.str(wf_->last_grid_names[a]);
+  }
+  w.put<uint64_t>(stack_->stack.size());
+  for (auto& ent : stack_->stack) {
+    Operator& op = *ent.op;
+    w.str(op.type);
+    const std::vector<ScalarState*> sc = op.scalar_states();
+    std::vector<double> vals;
+    for (ScalarState* st : sc)
+      for (size_t i = 0; i < st->host.size(); ++i) vals.push_back(st->get(i));
+    w.vec(vals);
+    auto* sv = dynamic_cast<StateSaver*>(&op);
+    w.put<uint8_t>(sv ? 1 : 0);
+    if (sv) {
+      w.put<uint64_t>(sv->current_frame);
+      w.vec(sv->times);
+      w.vec(sv->data);
+    }
+  }
+  std::vector<double> host(wf_->points() * 2);
+  e.export_host(host.data());
+  w.vec(host);
+  e.check_nonfinite();
+  return std::move(w.b);
+}
+
+void Propagation::restore(const unsigned char* data, size_t size) {
+  if (!data) throw Error(SO_ERR_INVALID, "null checkpoint");
+  BlobReader r{data, size};
+  char magic[sizeof(kCkptMagic)];
+  r.bytes(magic, sizeof(magic));
+  if (std::memcmp(magic, kCkptMagic, sizeof(magic)) != 0) throw Error(SO_ERR_INVALID, "not a checkpoint");
+  // read and check everything before changing anything
+  const int32_t prec = r.get<int32_t>();
+  if (prec != precision) throw Error(SO_ERR_STATE, "checkpoint was taken at another precision");
+  const uint64_t nd = r.get<uint64_t>();
+  if (nd != wf_->shape.size()) throw Error(SO_ERR_SHAPE, "checkpoint has another number of axes");
+  for (size_t a = 0; a < nd; ++a)
+    if (r.get<uint64_t>() != wf_->shape[a]) throw Error(SO_ERR_SHAPE, "checkpoint has another shape");
+  const uint64_t done = r.get<uint64_t>();
+  const bool pnc = r.get<uint8_t>() != 0;
+  const double cached_norm = r.get<double>();
+  std::vector<std::string> last(nd);
+  for (size_t a = 0; a < nd; ++a) {
+    if (r.str() != wf_->grids[a].name)
+      throw Error(SO_ERR_STATE, "checkpoint was taken in another representation of axis " + std::to_string(a));
+    last[a] = r.str();
+  }
+  if (r.get<uint64_t>() != stack_->stack.size()) throw Error(SO_ERR_STATE, "checkpoint has another operator stack");
+  struct OpState {
+    std::vector<double> vals;
+    bool saver = false;
+    uint64_t frame = 0;
+    std::vector<double> times, data;
+  };
+  std::vector<OpState> ops(stack_->stack.size());
+  for (size_t i = 0; i < ops.size(); ++i) {
+    Operator& op = *stack_->stack[i].op;
+    if (r.str() != op.type) throw Error(SO_ERR_STATE, "checkpoint operator " + std::to_string(i) + " differs");
+    ops[i].vals = r.vec();
+    size_t want = 0;
+    for (ScalarState* st : op.scalar_states()) want += st->host.size();
+    if (ops[i].vals.size() != want) throw Error(SO_ERR_STATE, "checkpoint operator " + std::to_string(i) + " differs");
+    ops[i].saver = r.get<uint8_t>() != 0;
+    auto* sv = dynamic_cast<StateSaver*>(&op);
+    if (ops[i].saver != (sv != nullptr)) throw Error(SO_ERR_STATE, "checkpoint saver layout differs");
+    if (sv) {
+      ops[i].frame = r.get<uint64_t>();
+      ops[i].times = r.vec();
+      ops[i].data = r.vec();
+      if (ops[i].data.size() != sv->data.size()) throw Error(SO_ERR_STATE, "checkpoint saver size differs");
+    }
+  }
+  const std::vector<double> host = r.vec();
+  if (host.size() != wf_->points() * 2) throw Error(SO_ERR_SHAPE, "checkpoint state has another size");
+  if (r.off != size) throw Error(SO_ERR_INVALID, "checkpoint has trailing bytes");
+  // apply
+  Engine& e = *wf_->eng;
+  e.import_host(host.data());
+  e.write_slot(wf_->cache_slot, cached_norm);
+  wf_->possible_norm_change = pnc;
+  wf_->last_grid_names = last;
+  for (size_t i = 0; i < ops.size(); ++i) {
+    Operator& op = *stack_->stack[i].op;
+    size_t k = 0;
+    for (ScalarState* st : op.scalar_states()) {
+      // bind to this engine so the values land where the next step reads them
+      st->bind(&e);
+      for (size_t j = 0; j < st->host.size(); ++j) st->set(j, ops[i].vals[k++]);
+    }
+    if (auto* sv = dynamic_cast<StateSaver*>(&op)) {
+      sv->current_frame = (size_t)ops[i].frame;
+      sv->times = ops[i].times;
+      sv->data = ops[i].data;
+    }
+  }
+  steps_done_ = done;
+  e.sync();
 }
 
 void Propagation::reset_savers() {
@@ -1607,6 +1791,7 @@ void Batch::steps(uint64_t n, bool wait, bool sync_members) {
   // tail: the last step's closing passes (merged form only)
   if (merged)
     for (size_t i = m + 1; i < np; ++i) run_groups(pos[i]);
+  for (Propagation* p : props_) p->count_steps(n);
   if (trace)
     std::fprintf(stderr, "batch steps(%llu) of %zu: sync %.3f record %.3f groups%s %.3f launched %.3f ms\n",
                  (unsigned long long)n, props_.size(), t_sync, t_rec, reuse ? " (reused)" : "", t_groups, ms());

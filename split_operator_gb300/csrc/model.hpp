@@ -279,6 +279,12 @@ struct Operator {
   // Saver
   virtual void monitor(WaveFunction&, Emitter&) { throw Error(SO_ERR_INVALID, "not a saver"); }
   virtual void reset() {}
+  // Device-or-host scalars the operator carries between steps (checkpoints)
+  virtual std::vector<ScalarState*> scalar_states() {
+    std::vector<ScalarState*> v;
+    if (LossChecker* lc = loss_checker()) v.push_back(&lc->st);
+    return v;
+  }
 };
 
 struct OneDimPropagator : Operator {
@@ -348,6 +354,11 @@ struct LeakControl : Operator {  // leak_control.rs
   void first_half(WaveFunction& wf, Emitter& em) override;
   void second_half(WaveFunction& wf, Emitter& em) override;
   LossChecker* loss_checker() override { return lc.get(); }
+  std::vector<ScalarState*> scalar_states() override {
+    std::vector<ScalarState*> v{&st};
+    if (lc) v.push_back(&lc->st);
+    return v;
+  }
 };
 
 struct BorderDumping : Operator {  // border_dumping.rs:36-93
@@ -412,10 +423,20 @@ class Propagation {
   // Run the host logic of `n` steps, capturing the passes instead of launching them.
   std::vector<RecordedPass> record_steps(uint64_t n);
   bool has_savers() const;
+  // Steps taken since creation (or since the restored checkpoint was taken).
+  uint64_t steps_done() const { return steps_done_; }
+  void count_steps(uint64_t n) { steps_done_ += n; }  // steps run by a batch on this propagation
+  // Everything a later run needs to continue exactly where this one stands: the state in
+  // its storage precision, the norm cache, every loss checker, leak-control norm and saver,
+  // and the step count.  restore() checks that the blob fits this propagation's shape,
+  // precision and operator stack, then replaces the lot.
+  std::vector<unsigned char> checkpoint();
+  void restore(const unsigned char* data, size_t size);
 
   int precision;
 
  private:
+  uint64_t steps_done_ = 0;
   void step(Emitter& em);
   std::unique_ptr<WaveFunction> wf_;
   so_time_grid time_;

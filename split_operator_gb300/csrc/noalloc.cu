@@ -33,7 +33,6 @@ struct DeviceScratch {
   double* partials = nullptr;
   unsigned int* counter = nullptr;
   double2* twiddle = nullptr;
-  int64_t twiddle_n = 0;  // lane length the table currently holds
 };
 DeviceScratch g_dev[kMaxDevices];
 
@@ -114,11 +113,12 @@ extern "C" int so_fft_norm_noalloc(double* psi, size_t lanes, size_t n, int dire
   // the ticket counter must start at zero (the kernel's last CTA resets it too)
   if (cudaMemsetAsync(d.counter, 0, sizeof(unsigned int), stream) != cudaSuccess)
     return fail(SO_ERR_CUDA, "so_fft_norm_noalloc: counter reset failed");
-  if (d.twiddle_n != (int64_t)n) {
-    twiddle_kernel<<<(unsigned)std::min<int64_t>(64, (g.n + 255) / 256), 256, 0, stream>>>(d.twiddle, g.n);
-    if (cudaGetLastError() != cudaSuccess) return fail(SO_ERR_CUDA, "so_fft_norm_noalloc: twiddle kernel failed");
-    d.twiddle_n = (int64_t)n;
-  }
+  // the twiddle table is rebuilt on every call (n <= 4096 entries, one small kernel): a
+  // table kept from an earlier call could belong to another lane length by the time this
+  // call's pass runs, whatever order the caller's work reaches the GPU in
+  twiddle_kernel<<<(unsigned)std::min<int64_t>(64, (g.n + 255) / 256), 256, 0, stream>>>(d.twiddle, g.n);
+  if (cudaGetLastError() != cudaSuccess) return fail(SO_ERR_CUDA, "so_fft_norm_noalloc: twiddle kernel failed");
+  count_launch();
 
   PassParams p{};
   p.g = g;

@@ -2,8 +2,9 @@
 dt = 0.5, border damping with a loss checker), 10^4 real-time steps.
 
 * FP64 GPU path against the C++ FP64 restatement of the reference passes
-  (propagation.rs:134-182 step order): relative L2 <= 1e-9 after 10^4 steps, norm and
-  accumulated loss to the same order.
+  (propagation.rs:134-182 step order): relative L2 <= 1e-9 after 10^4 steps, norm,
+  accumulated loss and the real-time mean energy (propagation.rs:283-290) to the same
+  order.
 * Each FP32 mode against the FP64 GPU path: one step from the same state within
   relative L2 1e-6 (FP32 SIMT and 3xTF32) or 2e-5 (split-BF16x3: a bf16 pair keeps
   16 significand bits, so each operand carries a relative error up to 2^-17 ~ 7.6e-6);
@@ -77,6 +78,15 @@ def test_long_run_fp64_vs_cpu_restatement_and_fp32_modes(tmp_path):
                       "loss_diff": p.all_losses()[0] - row["fp64_loss"]}
         rows.append(row)
     report["rows"] = rows
+    # real-time energy (propagation.rs:283-290): -arg<psi(t+dt)|psi(t)> / dt over one more step
+    before = port.psi.copy()
+    port.run(1)
+    ov = np.sum(port.psi * np.conj(before) * port.wr[:, None] * port.wth[None, :])
+    e_cpu = float(-np.angle(ov) / 0.5)
+    energy = {"cpu": e_cpu, "fp64": p64.mean_energy()}
+    for m, p in p32.items():
+        energy[m] = p.mean_energy()
+    report["energy_after_10^4_steps"] = energy
     report["cpu_seconds"] = t_port
     out = os.environ.get("SO_REPORT_DIR") or str(tmp_path)
     with open(os.path.join(out, "precision_report.json"), "w") as f:
@@ -90,5 +100,6 @@ def test_long_run_fp64_vs_cpu_restatement_and_fp32_modes(tmp_path):
     assert last["fp64_vs_cpu_rel_l2"] <= 1e-9
     assert abs(last["fp64_norm"] - last["cpu_norm"]) <= 1e-9
     assert abs(last["fp64_loss"] - last["cpu_loss"]) <= 1e-9
+    assert abs(energy["fp64"] - energy["cpu"]) <= 1e-9 * abs(energy["cpu"])
     for m in FP32_MODES:
         assert np.isfinite(last[m]["rel_l2_vs_fp64"])

@@ -296,10 +296,10 @@ def test_three_dim_two_fft_axes_matches_oracle(so, precision, tol):
     assert abs(prop.norm() - oprop.wave_function.norm()) < 10 * tol * abs(oprop.wave_function.norm())
 
 
-@pytest.mark.parametrize("precision,n", [("fp32_simt", 16384), ("fp64", 8192)])
+@pytest.mark.parametrize("precision,n", [("fp32_simt", 16384), ("fp64", 16384)])
 def test_lanes_beyond_the_tile_limit_are_rejected(so, precision, n):
-    """A lane longer than a CTA tile holds (8192 FP32 / 4096 FP64 points) is refused with a
-    status before any kernel runs; the context stays usable."""
+    """A lane longer than a CTA tile holds (8192 points) is refused with a status before any
+    kernel runs; the context stays usable."""
     from split_operator_gb300 import workloads as W
     with pytest.raises(so.SplitOperatorError) as e:
         p = W.radial_angular_2d(nr=n, nth=8, step_no=2, precision=precision)[0]
@@ -308,6 +308,33 @@ def test_lanes_beyond_the_tile_limit_are_rejected(so, precision, n):
     q = W.radial_angular_2d(nr=256, nth=8, step_no=2, precision=precision)[0]
     q.steps(1)
     assert np.isfinite(q.norm())
+
+
+def test_fp64_lanes_beyond_4096_need_the_fft_pair_form(so):
+    """FP64 lanes of 4097..8192 points run only in FFT-pair passes (one in-place lane buffer);
+    a 1-D propagation whose FFT pass also folds norms is refused with a status."""
+    from split_operator_gb300 import workloads as W
+    with pytest.raises(so.SplitOperatorError) as e:
+        W.harmonic_1d(n=8192, step_no=2)[0].steps(1)
+    assert "not supported" in str(e.value)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_tf32x3", 1e-6)])
+def test_radial_angular_8192_lanes_match_oracle(so, precision, tol):
+    """Nr = 8192 (the longest radial lanes of the batched workload): the FP64 FFT-pair kernel
+    (radix-8 stages, 16 values per thread) and the FP32 tensor-core + FFT-pair step against the
+    FP64 oracle, step by step."""
+    from split_operator_gb300 import workloads as W
+    nr, nth, steps = 8192, 32, 3
+    prop, _ = W.radial_angular_2d(nr=nr, nth=nth, step_no=steps, seed=41, precision=precision)
+    oprop, _ = S.radial_angular_2d(nr=nr, nth=nth, step_no=steps, seed=41)
+    prop.set_timing(True)
+    for k in range(steps):
+        prop.steps(1)
+        oprop.step()
+        assert rel_l2(prop.get_array(), oprop.wave_function.array) < tol * (k + 1), k
+    assert abs(prop.all_losses()[0] - oprop.all_losses()[0]) < tol
+    assert any("fftpair" in t[0] for t in prop.kernel_times())
 
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 3e-6)])
