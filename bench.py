@@ -39,7 +39,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch", choices=["batch", "single"])
     ap.add_argument("--instances", type=int, default=512)
-    ap.add_argument("--precision", default="fp32_tf32x3", choices=["fp64", "fp32_tf32x3", "fp32_bf16x3", "fp32_simt"])
+    ap.add_argument("--precision", default="fp32_tf32x3",
+                    choices=["fp64", "fp32_tf32x3", "fp32_bf16x3", "fp32_bf16x6", "fp32_simt"])
     ap.add_argument("--nr", type=int, default=4096)
     ap.add_argument("--nth", type=int, default=128)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -133,7 +134,7 @@ def ncu_traffic():
 
 def kernel_of(group_name):
     """The CUDA kernel a batched group runs: its name carries the pass family."""
-    if "tc3xtf32" in group_name or "tcbf16x3" in group_name:
+    if "tc3xtf32" in group_name or "tcbf16x3" in group_name or "tcbf16x6" in group_name:
         return "angular_tc_kernel_batched"
     if "fftpair" in group_name:
         return "fft_pair_kernel_batched"

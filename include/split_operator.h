@@ -62,7 +62,9 @@ enum {
   SO_PRECISION_FP64 = 0,        /* FP64 state, tables and transforms */
   SO_PRECISION_FP32_TF32X3 = 1, /* FP32 state; real lane matrices as 3xTF32 tensor-core GEMM */
   SO_PRECISION_FP32_BF16X3 = 2, /* FP32 state; real lane matrices as split-BF16x3 tensor-core GEMM */
-  SO_PRECISION_FP32_SIMT = 3    /* FP32 state; lane matrices on FP32 CUDA cores */
+  SO_PRECISION_FP32_SIMT = 3,   /* FP32 state; lane matrices on FP32 CUDA cores */
+  SO_PRECISION_FP32_BF16X6 = 4  /* FP32 state; real lane matrices as split-BF16x6 tensor-core GEMM:
+                                   three fixed-point bf16 slices per operand, exact FP32 sums */
 };
 
 /* ---- library ------------------------------------------------------------ */

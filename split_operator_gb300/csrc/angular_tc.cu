@@ -57,6 +57,8 @@ constexpr int kColtSlots = 4;        // DIAG1D ops on a non-lane axis per pass
 
 struct TcShape {
   bool par;      // parity-split lane matrices (two K = n/2 GEMMs, one per M half)
+  bool oz;       // split-BF16x6: three fixed-point bf16 slices per operand, exact FP32 sums
+  int slices;    // operand slices: 2 (hi, lo) or 3 (split-BF16x6)
   int kc;        // K values per 16-byte core-matrix row (4 tf32, 8 bf16)
   int km;        // K per MMA instruction (8 tf32, 16 bf16)
   int kdim;      // K of each GEMM: n, or n / 2 with par
@@ -87,8 +89,13 @@ struct TcShape {
 // bf: split-BF16x3 operands (2-byte elements, 8 K values per 16-byte core-matrix row,
 // K = 16 per instruction) instead of 3xTF32 (4-byte, 4 per row, K = 8); in bytes the
 // chunk, core-matrix and descriptor steps are the same.
-__host__ __device__ inline TcShape tc_shape(int n, bool par = false, bool bf = false) {
+// oz: split-BF16x6 (bf16 operands in three fixed-point slices, six products, one exact
+// accumulation per GEMM: see the comment above oz_quanta); implies bf.
+__host__ __device__ inline TcShape tc_shape(int n, bool par = false, bool bf = false, bool oz = false) {
   TcShape s{};
+  bf = bf || oz;
+  s.oz = oz;
+  s.slices = oz ? 3 : 2;
   s.par = par && n == 256;
   s.kc = bf ? 8 : 4;
   s.km = bf ? 16 : 8;
@@ -100,8 +107,8 @@ __host__ __device__ inline TcShape tc_shape(int n, bool par = false, bool bf = f
   s.nk = s.kdim / s.chunk_k;
   s.ksteps = s.kdim / s.km;
   s.reg_cols = s.nc * s.mh;
-  s.nmain = kRegions - 1;
-  s.fills = (s.ksteps + kFillSteps - 1) / kFillSteps;
+  s.nmain = oz ? 3 : kRegions - 1;  // oz: the three product orders R0, R1, R2
+  s.fills = oz ? 1 : (s.ksteps + kFillSteps - 1) / kFillSteps;
   s.sbo_a = (s.chunk_k / s.kc) * 128;
   s.a_half16 = (16 * s.sbo_a) >> 4;
   s.stage_row = s.nc + 4;
@@ -110,22 +117,24 @@ __host__ __device__ inline TcShape tc_shape(int n, bool par = false, bool bf = f
 }
 
 struct TcSmemLayout {
-  uint32_t stage0, bhi, blo, bars, sbo_b, bhalf, bbytes, total;
+  uint32_t stage0, stage_bytes, bhi, bmid, blo, bars, sbo_b, bhalf, bbytes, total;
 };
 
-// [kStages x 16 KB A stages][B_hi][B_lo][mbarriers: full[kStages], empty[kStages], dbar,
-// freebar, bready, quiet].  With par each of B_hi / B_lo holds two K = n/2 operands,
-// bhalf bytes apart (the even / odd or sum / difference halves).
-__host__ __device__ inline TcSmemLayout tc_layout(int n, bool par = false, bool bf = false) {
-  const TcShape s = tc_shape(n, par, bf);
+// [kStages x A stages (slices x 8 KB each)][B_hi][B_mid (oz)][B_lo][mbarriers: full[kStages],
+// empty[kStages], dbar, freebar, bready, quiet].  With par each B slice holds two K = n/2
+// operands, bhalf bytes apart (the even / odd or sum / difference halves).
+__host__ __device__ inline TcSmemLayout tc_layout(int n, bool par = false, bool bf = false, bool oz = false) {
+  const TcShape s = tc_shape(n, par, bf, oz);
   TcSmemLayout L{};
   L.sbo_b = (uint32_t)(s.kdim / s.kc) * kLboB + 16;
   L.bhalf = (uint32_t)(s.nc / 8) * L.sbo_b;
   L.bbytes = (s.par ? 2u : 1u) * L.bhalf;
   L.bbytes = (L.bbytes + 127u) & ~127u;
   L.stage0 = 0;
-  L.bhi = kStages * 2u * kChunkBytes;
-  L.blo = L.bhi + L.bbytes;
+  L.stage_bytes = (uint32_t)s.slices * kChunkBytes;
+  L.bhi = kStages * L.stage_bytes;
+  L.bmid = L.bhi + L.bbytes;  // (oz only)
+  L.blo = (s.oz ? L.bmid : L.bhi) + L.bbytes;
   L.bars = L.blo + L.bbytes;
   L.total = L.bars + (2 * kStages + 4) * 8;
   return L;
@@ -394,6 +403,77 @@ __device__ __forceinline__ void store4(unsigned char* bh, unsigned char* bl, uin
   }
 }
 
+// ---- split-BF16x6: exact tensor-core sums (the Ozaki scheme with bf16 slices)
+// The tensor core truncates when it adds products whose bits spread over more than an FP32
+// significand; a sum whose terms are all multiples of one quantum q and stay below 2^24 q in
+// magnitude has no such bits, so the core adds it exactly.  Each B column (and, on the host,
+// each A row) is cut at the power of two just above its largest magnitude into three
+// fixed-point slices of 8 significant bits -- x = s0 + s1 + s2 + O(2^-24 max), s_i a
+// multiple of q_i = 2^(e-8-8i) with |s_i / q_i| <= 256 -- which bf16 holds exactly.  A
+// product of two slices is then an integer below 2^16 times q_A q_B, and a GEMM of K <= 256
+// such products stays below 2^24 of its quantum: the three product orders accumulate
+// exactly over all of K in three TMEM regions, R0 = A0 B0, R1 = A0 B1 + A1 B0,
+// R2 = A0 B2 + A1 B1 + A2 B0 (the dropped orders are 2^-24 of the leading one), and the
+// only rounding is the round-to-nearest R2 + R1 + R0 of the drain -- no truncation bias.
+// Reference: K. Ozaki, T. Ogita, S. Oishi, S. M. Rump, "Error-free transformations of
+// matrix multiplication by using fast routines of matrix multiplication and its
+// applications", Numer. Algorithms 59 (2012).
+struct OzQ {
+  float q0, q1, q2, i0, i1, i2;  // slice quanta and their reciprocals (powers of two)
+};
+
+// quanta of a column whose largest magnitude has the FP32 bits `maxbits`: q0 = 2^(E+1-8)
+// for max in [2^E, 2^(E+1)); columns below 2^-103 (and empty ones) share the smallest
+// quanta whose third slice is still a normal number
+__device__ __forceinline__ OzQ oz_quanta(uint32_t maxbits) {
+  uint32_t e = maxbits >> 23;  // biased exponent of the (non-negative) maximum
+  e = e < 24u ? 24u : (e > 254u ? 254u : e);
+  const uint32_t e0 = e - 7u;  // biased exponent of q0
+  return {__uint_as_float(e0 << 23), __uint_as_float((e0 - 8u) << 23), __uint_as_float((e0 - 16u) << 23),
+          __uint_as_float((254u - e0) << 23), __uint_as_float((262u - e0) << 23),
+          __uint_as_float((270u - e0) << 23)};
+}
+
+// x -> three bf16 slices (each exact: a bf16 value's FP32 bits end in 16 zero bits)
+__device__ __forceinline__ void oz_split(float x, const OzQ& q, uint32_t& h0, uint32_t& h1, uint32_t& h2) {
+  const float s0 = rintf(x * q.i0) * q.q0;
+  float r = x - s0;
+  const float s1 = rintf(r * q.i1) * q.q1;
+  r -= s1;
+  const float s2 = rintf(r * q.i2) * q.q2;
+  h0 = __float_as_uint(s0) >> 16;
+  h1 = __float_as_uint(s1) >> 16;
+  h2 = __float_as_uint(s2) >> 16;
+}
+
+// four consecutive K values of one B column (one quantum) at byte offset `off` of the three
+// slice images: one 8-byte store per slice
+__device__ __forceinline__ void store4_oz(unsigned char* b0, unsigned char* b1, unsigned char* b2, uint32_t off,
+                                          float a, float b, float c, float d, const OzQ& q) {
+  uint32_t x0[4], x1[4], x2[4];
+  oz_split(a, q, x0[0], x1[0], x2[0]);
+  oz_split(b, q, x0[1], x1[1], x2[1]);
+  oz_split(c, q, x0[2], x1[2], x2[2]);
+  oz_split(d, q, x0[3], x1[3], x2[3]);
+  *reinterpret_cast<uint2*>(b0 + off) = make_uint2(x0[0] | x0[1] << 16, x0[2] | x0[3] << 16);
+  *reinterpret_cast<uint2*>(b1 + off) = make_uint2(x1[0] | x1[1] << 16, x1[2] | x1[3] << 16);
+  *reinterpret_cast<uint2*>(b2 + off) = make_uint2(x2[0] | x2[1] << 16, x2[2] | x2[3] << 16);
+}
+
+__device__ __forceinline__ void store1_oz(unsigned char* b0, unsigned char* b1, unsigned char* b2, uint32_t off,
+                                          float x, const OzQ& q) {
+  uint32_t h0, h1, h2;
+  oz_split(x, q, h0, h1, h2);
+  *reinterpret_cast<uint16_t*>(b0 + off) = (uint16_t)h0;
+  *reinterpret_cast<uint16_t*>(b1 + off) = (uint16_t)h1;
+  *reinterpret_cast<uint16_t*>(b2 + off) = (uint16_t)h2;
+}
+
+// per-column maxima in shared memory (FP32 bits of |x|, which order like the values)
+__device__ __forceinline__ void colmax_add(uint32_t* cm, int col, float m) {
+  atomicMax(cm + col, __float_as_uint(m));
+}
+
 // one operand element: hi / lo parts at byte offset `off`
 template <bool BF>
 __device__ __forceinline__ void store1(unsigned char* bh, unsigned char* bl, uint32_t off, float x) {
@@ -417,11 +497,13 @@ __device__ __forceinline__ void store1(unsigned char* bh, unsigned char* bl, uin
 //   mode 0: row j -> K row j (RB = 4)
 //   mode 2: even / odd halves, row j -> half j & 1, K row j >> 1 (RB = 8)
 //   mode 1: sum / difference pairs, rows j < n/2 and n-1-j -> K row j of both halves (RB = 4)
-template <int NK, int RB, int MODE, bool BF>
+// OZ (split-BF16x6): the operand goes to three slice images (bh, bm, bl) with the quanta of
+// each column's largest value, gathered in cm (per-column maxima, zero on entry) first.
+template <int NK, int RB, int MODE, bool BF, bool OZ>
 __device__ __forceinline__ void prologue_vec(const PassParams& p, const TileTabs& T, int oe, const float2* psi,
                                              int64_t base, int c, int a, int G, int n, unsigned char* bh,
-                                             unsigned char* bl, uint32_t bhalf, uint32_t sbo_b, float* acc,
-                                             unsigned long long* loaded_mark) {
+                                             unsigned char* bm, unsigned char* bl, uint32_t bhalf, uint32_t sbo_b,
+                                             float* acc, unsigned long long* loaded_mark, uint32_t* cm) {
   const int64_t inner = p.g.inner;
   const int64_t bstride = (int64_t)RB * G;  // rows between a thread's row blocks
   float2 v[RB][NK];
@@ -450,6 +532,56 @@ __device__ __forceinline__ void prologue_vec(const PassParams& p, const TileTabs
     if constexpr (MODE == 1)
       apply_col<NK>(p, T, 0, oe, w[r], n - 1 - j0, -(int)bstride, c, base + (int64_t)(n - 1 - j0) * inner + c,
                     -bstride * inner, acc);
+  }
+  if constexpr (OZ) {
+    // the column's largest stored magnitude (re and im are separate B columns); for the sum /
+    // difference pairs |v| + |w| bounds both |v + w| and |v - w|
+    float mr = 0.0f, mi = 0.0f;
+#pragma unroll
+    for (int r = 0; r < RB; ++r)
+#pragma unroll
+      for (int k = 0; k < NK; ++k) {
+        if constexpr (MODE == 1) {
+          mr = fmaxf(mr, fabsf(v[r][k].x) + fabsf(w[r][k].x));
+          mi = fmaxf(mi, fabsf(v[r][k].y) + fabsf(w[r][k].y));
+        } else {
+          mr = fmaxf(mr, fabsf(v[r][k].x));
+          mi = fmaxf(mi, fabsf(v[r][k].y));
+        }
+      }
+    colmax_add(cm, 2 * c, mr);
+    colmax_add(cm, 2 * c + 1, mi);
+    work_sync();
+    const OzQ qr = oz_quanta(cm[2 * c]), qi = oz_quanta(cm[2 * c + 1]);
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const int j0 = RB * a + (int)bstride * k;
+      if constexpr (MODE == 0) {
+        const uint32_t orr = boff<true>(2 * c, j0, sbo_b), oim = boff<true>(2 * c + 1, j0, sbo_b);
+        store4_oz(bh, bm, bl, orr, v[0][k].x, v[1][k].x, v[2][k].x, v[3][k].x, qr);
+        store4_oz(bh, bm, bl, oim, v[0][k].y, v[1][k].y, v[2][k].y, v[3][k].y, qi);
+      } else if constexpr (MODE == 2) {
+#pragma unroll
+        for (int hf = 0; hf < 2; ++hf) {
+          const uint32_t o = hf * bhalf;
+          const uint32_t orr = o + boff<true>(2 * c, j0 >> 1, sbo_b), oim = o + boff<true>(2 * c + 1, j0 >> 1, sbo_b);
+          store4_oz(bh, bm, bl, orr, v[hf][k].x, v[2 + hf][k].x, v[4 + hf][k].x, v[6 + hf][k].x, qr);
+          store4_oz(bh, bm, bl, oim, v[hf][k].y, v[2 + hf][k].y, v[4 + hf][k].y, v[6 + hf][k].y, qi);
+        }
+      } else {
+        const uint32_t orr = boff<true>(2 * c, j0, sbo_b), oim = boff<true>(2 * c + 1, j0, sbo_b);
+#pragma unroll
+        for (int hf = 0; hf < 2; ++hf) {
+          const float sg = hf ? -1.0f : 1.0f;
+          const uint32_t o = hf * bhalf;
+          store4_oz(bh, bm, bl, o + orr, v[0][k].x + sg * w[0][k].x, v[1][k].x + sg * w[1][k].x,
+                    v[2][k].x + sg * w[2][k].x, v[3][k].x + sg * w[3][k].x, qr);
+          store4_oz(bh, bm, bl, o + oim, v[0][k].y + sg * w[0][k].y, v[1][k].y + sg * w[1][k].y,
+                    v[2][k].y + sg * w[2][k].y, v[3][k].y + sg * w[3][k].y, qi);
+        }
+      }
+    }
+    return;
   }
 #pragma unroll
   for (int k = 0; k < NK; ++k) {
@@ -493,6 +625,36 @@ __device__ __forceinline__ void write_b_row(const float2 (&x)[NV], int c0, int k
     const uint32_t o = o0 + (uint32_t)(u >> 2) * sbo_b + (uint32_t)(u & 3) * 32u;
     store1<BF>(bh, bl, o, x[u].x);
     store1<BF>(bh, bl, o + 16, x[u].y);
+  }
+}
+
+// The same row into the three slice images of split-BF16x6, with the quanta of its columns
+// (cm: per-column maxima of the whole operand, complete when this runs)
+template <int NV>
+__device__ __forceinline__ void write_b_row_oz(const float2 (&x)[NV], int c0, int k, unsigned char* b0,
+                                               unsigned char* b1, unsigned char* b2, uint32_t sbo_b,
+                                               const uint32_t* cm) {
+  const uint32_t o0 = boff<true>(2 * c0, k, sbo_b);
+#pragma unroll
+  for (int u = 0; u < NV; ++u) {
+    const uint32_t o = o0 + (uint32_t)(u >> 2) * sbo_b + (uint32_t)(u & 3) * 32u;
+    store1_oz(b0, b1, b2, o, x[u].x, oz_quanta(cm[2 * (c0 + u)]));
+    store1_oz(b0, b1, b2, o + 16, x[u].y, oz_quanta(cm[2 * (c0 + u) + 1]));
+  }
+}
+
+// Column maxima of a B operand written row by row: every lane of the warp holds one row of
+// the same NV complex columns c0 .. (rows that are not written pass zeros); the warp reduces
+// each column and one lane per column adds it to cm.  Called by all 32 lanes.
+template <int NV>
+__device__ __forceinline__ void colmax_rows(const float2 (&x)[NV], int c0, uint32_t* cm) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int u = 0; u < NV; ++u) {
+    const uint32_t mr = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(x[u].x)));
+    const uint32_t mi = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(x[u].y)));
+    if (lane == (2 * u) % 32) atomicMax(cm + 2 * (c0 + u), mr);
+    if (lane == (2 * u + 1) % 32) atomicMax(cm + 2 * (c0 + u) + 1, mi);
   }
 }
 
@@ -576,7 +738,7 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
   using namespace tc;
   uint64_t* full = reinterpret_cast<uint64_t*>(sm_ptr(sm0 + L.bars));
   uint64_t* empty = full + kStages;
-  const uint32_t stage_bytes = 2u * kChunkBytes;
+  const uint32_t stage_bytes = L.stage_bytes;
   int64_t cc = 0;  // chunks issued
   bool ok = true;
   for (int64_t gt = blockIdx.x; gt < total && ok && !*fail; gt += gridDim.x) {
@@ -594,8 +756,8 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
         const int ct = m * S.nk + q;  // chunk within the tile
         if (r.prm->trace && ct < 8) r.prm->trace[r.tile * kTraceSlots + TR_TMA + ct] = globaltimer_ns();
         mbar_expect_tx(&full[s], stage_bytes);
-        bulk_g2s(sm_ptr(sm0 + L.stage0 + (uint32_t)s * stage_bytes), img + (size_t)q * 2 * (kChunkBytes / 4),
-                 stage_bytes, &full[s]);
+        bulk_g2s(sm_ptr(sm0 + L.stage0 + (uint32_t)s * stage_bytes),
+                 img + (size_t)q * S.slices * (kChunkBytes / 4), stage_bytes, &full[s]);
         ++cc;
       }
     }
@@ -613,7 +775,10 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
 // (t - t0) nused / span and both corrections into the correction region -- then a
 // commit of the fill to dbar.  Each chunk's MMAs are committed to its stage's empty
 // barrier, which the TMA warp waits on before refilling the stage.
-template <bool BF, typename Resolve>
+// OZ (split-BF16x6): one fill over all K steps; step t issues the six slice products into
+// the regions R0 (A0 B0), R1 (A0 B1, A1 B0) and R2 (A0 B2, A1 B1, A2 B0), which accumulate
+// exactly, so the work warps drain them once per matrix.
+template <bool BF, bool OZ, typename Resolve>
 __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const TcShape S, uint32_t sm0,
                                         const TcSmemLayout L, uint32_t tmem, volatile int* fail) {
   using namespace tc;
@@ -623,7 +788,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
   uint64_t* freebar = dbar + 1;
   uint64_t* bready = dbar + 2;
   uint64_t* quiet = dbar + 3;
-  const uint32_t stage_bytes = 2u * kChunkBytes;
+  const uint32_t stage_bytes = L.stage_bytes;
   const uint32_t idesc = BF ? idesc_bf16(128, (uint32_t)S.nc) : idesc_tf32(128, (uint32_t)S.nc);
   const uint64_t bbits = smem_desc_bits(kLboB, L.sbo_b), abits = smem_desc_bits(128, (uint32_t)S.sbo_a);
   const int kpc = S.chunk_k / S.km;  // K steps per chunk
@@ -655,6 +820,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
         // B by 2 K core matrices (2 x kLboB bytes) per K step, A by 256 bytes per K step
         // within a chunk; the main region index moves when (t - t0) nused crosses span
         uint64_t bh = smem_desc_at(bbits, sm0 + L.bhi + (uint32_t)(fs.t0 * 2 * kLboB));
+        uint64_t bm = smem_desc_at(bbits, sm0 + L.bmid + (uint32_t)(fs.t0 * 2 * kLboB));
         uint64_t bl = smem_desc_at(bbits, sm0 + L.blo + (uint32_t)(fs.t0 * 2 * kLboB));
         int rm = 0, racc = 0;
         bool newreg = true;  // this step starts region rm
@@ -672,6 +838,21 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
           }
           const uint32_t first_main = newreg ? 0u : 1u;  // 0: the step starts the region
           const uint32_t first_corr = t == 0 ? 0u : 1u;
+          if constexpr (OZ) {
+            constexpr uint64_t kSlice = (uint64_t)(kChunkBytes >> 4);  // descriptor step between A slices
+            for (int hh = 0; hh < S.mh; ++hh) {
+              const uint64_t a0 = ahi + (uint64_t)(hh * S.a_half16), a1 = a0 + kSlice, a2 = a0 + 2 * kSlice;
+              const uint64_t bo = (uint64_t)hh * bstep_half;
+              const uint32_t r0 = tmem + (uint32_t)(hh * S.nc), r1 = r0 + (uint32_t)S.reg_cols,
+                             r2 = r0 + 2u * (uint32_t)S.reg_cols;
+              mma_bf16(r0, a0, bh + bo, idesc, first_corr);
+              mma_bf16(r1, a0, bm + bo, idesc, first_corr);
+              mma_bf16(r1, a1, bh + bo, idesc, 1u);
+              mma_bf16(r2, a0, bl + bo, idesc, first_corr);
+              mma_bf16(r2, a1, bm + bo, idesc, 1u);
+              mma_bf16(r2, a2, bh + bo, idesc, 1u);
+            }
+          } else {
           for (int hh = 0; hh < S.mh; ++hh) {
             const uint64_t ah = ahi + (uint64_t)(hh * S.a_half16);
             const uint64_t bo = (uint64_t)hh * bstep_half;  // parity split: each half its own B
@@ -685,7 +866,9 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
               mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(kChunkBytes >> 4), bh + bo, idesc, 1u);
             }
           }
+          }
           bh += (uint64_t)(2 * kLboB >> 4);
+          bm += (uint64_t)(2 * kLboB >> 4);
           bl += (uint64_t)(2 * kLboB >> 4);
           ahi += (uint64_t)(256 >> 4);
           racc += fs.nused;
@@ -715,7 +898,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
 
 // The tiles blockIdx.x, blockIdx.x + gridDim.x, ... of a launch (every tile of a launch
 // has the same lane extent n).
-template <bool BF, typename Resolve>
+template <bool BF, bool OZ, typename Resolve>
 __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t total) {
   using namespace tc;
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -727,20 +910,22 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   __shared__ double totals[kMaxRed];
   __shared__ int s_last;
   __shared__ volatile int s_fail;
+  __shared__ uint32_t s_colmax[2][64];  // split-BF16x6: column maxima of the two B operands of a tile
   static_assert(sizeof(TcParams) % 4 == 0, "TcParams is copied as 32-bit words");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (blockIdx.x >= total) return;
   const TcParams* first = resolve(blockIdx.x).prm;  // every tile of a launch shares n and parity mode
   const int n = (int)first->p.g.n;
   const bool par = first->parity[0] != 0;
-  const TcShape S = tc_shape(n, par, BF);
-  const TcSmemLayout L = tc_layout(n, par, BF);
+  const TcShape S = tc_shape(n, par, BF, OZ);
+  const TcSmemLayout L = tc_layout(n, par, BF, OZ);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars);
   uint64_t* dbar = bars + 2 * kStages;  // MMAs of a fill completed (the work warps drain)
   uint64_t* freebar = dbar + 1;         // the work warps drained a fill (regions free again)
   uint64_t* bready = dbar + 2;          // the B operand of the next matrix is written
   float* bhi = reinterpret_cast<float*>(sm + L.bhi);  // also the FP32 output staging
-  unsigned char* bhb = sm + L.bhi;                    // B operand images (hi, lo)
+  unsigned char* bhb = sm + L.bhi;                    // B operand images (hi, lo; mid for OZ)
+  unsigned char* bmb = sm + L.bmid;
   unsigned char* blb = sm + L.blo;
 
   if (tid == 0) {
@@ -762,7 +947,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   if (warp == kWorkThreads / 32) {
     if (lane == 0) tma_producer(resolve, total, S, sm0, L, &s_fail);
   } else if (warp == kWorkThreads / 32 + 1) {
-    if (lane == 0) mma_issuer<BF>(resolve, total, S, sm0, L, tmem, &s_fail);
+    if (lane == 0) mma_issuer<BF, OZ>(resolve, total, S, sm0, L, tmem, &s_fail);
   } else {
     // ================= work warps
     const int lg = warp & 3, up = warp >> 2;
@@ -812,6 +997,8 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
           for (int jj = tid; jj < n; jj += kWorkThreads)
             prefetch_lines_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * sizeof(float2)));
       }
+      if constexpr (OZ)
+        for (int k = tid; k < 128; k += kWorkThreads) s_colmax[k >> 6][k & 63] = 0u;
       work_sync();  // tabs complete; the previous tile's staging has been stored
       if (tid == 0) trace_mark(tp, tile, TR_TABS);
 
@@ -826,16 +1013,17 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         const int k0 = tp.parity[0];
         const int mo = tp.mat_op[0];
         unsigned long long* lm = (tid == 0 && tp.trace) ? tp.trace + tile * kTraceSlots + TR_LOADED : nullptr;
+        uint32_t* cm0 = s_colmax[0];
         if (k0 == 1)
-          prologue_vec<2, 4, 1, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, bhb2, L.sbo_b, acc, lm);
+          prologue_vec<2, 4, 1, BF, OZ>(p, tabs, mo, psi, base, c, h, G, n, bhb, bmb, blb, bhb2, L.sbo_b, acc, lm, cm0);
         else if (k0 == 2)
-          prologue_vec<2, 8, 2, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, bhb2, L.sbo_b, acc, lm);
+          prologue_vec<2, 8, 2, BF, OZ>(p, tabs, mo, psi, base, c, h, G, n, bhb, bmb, blb, bhb2, L.sbo_b, acc, lm, cm0);
         else if (n / G == 16)
-          prologue_vec<4, 4, 0, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, 0, L.sbo_b, acc, lm);
+          prologue_vec<4, 4, 0, BF, OZ>(p, tabs, mo, psi, base, c, h, G, n, bhb, bmb, blb, 0, L.sbo_b, acc, lm, cm0);
         else if (n / G == 8)
-          prologue_vec<2, 4, 0, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, 0, L.sbo_b, acc, lm);
+          prologue_vec<2, 4, 0, BF, OZ>(p, tabs, mo, psi, base, c, h, G, n, bhb, bmb, blb, 0, L.sbo_b, acc, lm, cm0);
         else
-          prologue_vec<1, 4, 0, BF>(p, tabs, mo, psi, base, c, h, G, n, bhb, blb, 0, L.sbo_b, acc, lm);
+          prologue_vec<1, 4, 0, BF, OZ>(p, tabs, mo, psi, base, c, h, G, n, bhb, bmb, blb, 0, L.sbo_b, acc, lm, cm0);
         if (tid == 0) trace_mark(tp, tile, TR_STORED);
         fence_proxy_async();
         mbar_arrive(bready);
@@ -875,6 +1063,24 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         float v[kVals];
 #pragma unroll
         for (int e = 0; e < kVals; ++e) v[e] = 0.0f;
+        if constexpr (OZ) {
+          // one drain per matrix: R2 + R1 + R0, the small orders first (round to nearest)
+          ok = work_all(mbar_wait(dbar, drains & 1u, kWaitLimit));
+          if (ok) {
+            ++drains;
+            tc_fence_after();
+#pragma unroll
+            for (int hv = 0; hv < kVals / 16; ++hv) {
+              const uint32_t col = kind == 2 ? (uint32_t)((hv / kLd) * S.nc + (kVals / 2) * up + 16 * (hv % kLd))
+                                             : (uint32_t)(kVals * up + 16 * hv);
+              float w0[16], w1[16], w2[16];
+              tmem_ld16x3(lane_base + col, (uint32_t)S.reg_cols, w0, w1, w2);
+#pragma unroll
+              for (int e = 0; e < 16; ++e) v[16 * hv + e] = (w2[e] + w1[e]) + w0[e];
+            }
+            tc_fence_before();
+          }
+        } else
         for (int f = 0; f < S.fills; ++f) {
           ok = work_all(mbar_wait(dbar, drains & 1u, kWaitLimit));
           if (!ok) break;
@@ -908,7 +1114,28 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         const int sb = tp.mat_op[m] + 1, se = last ? p.nops : tp.mat_op[m + 1];
         if (kind != 2) {
           const int jr = kind == 1 ? 2 * i + up : j;
-          if (jr < n) {
+          if constexpr (OZ) {
+            // every work thread takes part in the column maxima of the next operand (rows past
+            // the lane extent pass zeros)
+            const bool valid = jr < n;
+            float2 x[kVals / 2];
+#pragma unroll
+            for (int u = 0; u < kVals / 2; ++u) x[u] = valid ? float2{v[2 * u], v[2 * u + 1]} : float2{0.0f, 0.0f};
+            if (valid)
+              apply_row<kVals / 2>(p, tabs, sb, se, x, jr, c0, base + (int64_t)jr * g.inner + c0, acc, rw_ptr,
+                                   kind == 1 ? rw_sum : rw_plain);
+            if (last) {
+              if (valid) stage_row<kVals / 2>(x, c0, jr, stg, S.stage_row);
+            } else {
+              colmax_rows<kVals / 2>(x, c0, s_colmax[1]);
+              work_sync();
+              if (valid) {
+                const uint32_t ho = next == 2 ? (uint32_t)(jr & 1) * bhb2 : 0u;
+                write_b_row_oz<kVals / 2>(x, c0, next == 2 ? jr >> 1 : jr, bhb + ho, bmb + ho, blb + ho, L.sbo_b,
+                                          s_colmax[1]);
+              }
+            }
+          } else if (jr < n) {
             // op-major over the thread's 32 complex values: the table loads of an op are all
             // in flight together
             float2 x[kVals / 2];
@@ -938,6 +1165,25 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
           if (last) {
             stage_row<kVals / 4>(xa, cc0, ja, stg, S.stage_row);
             stage_row<kVals / 4>(xb, cc0, jb, stg, S.stage_row);
+          } else if (OZ && next == 1) {
+            float2 sp[kVals / 4], sm2[kVals / 4];
+#pragma unroll
+            for (int u = 0; u < kVals / 4; ++u) {
+              sp[u] = {xa[u].x + xb[u].x, xa[u].y + xb[u].y};
+              sm2[u] = {xa[u].x - xb[u].x, xa[u].y - xb[u].y};
+            }
+            colmax_rows<kVals / 4>(sp, cc0, s_colmax[1]);
+            colmax_rows<kVals / 4>(sm2, cc0, s_colmax[1]);
+            work_sync();
+            write_b_row_oz<kVals / 4>(sp, cc0, i, bhb, bmb, blb, L.sbo_b, s_colmax[1]);
+            write_b_row_oz<kVals / 4>(sm2, cc0, i, bhb + bhb2, bmb + bhb2, blb + bhb2, L.sbo_b, s_colmax[1]);
+          } else if (OZ) {
+            colmax_rows<kVals / 4>(xa, cc0, s_colmax[1]);
+            colmax_rows<kVals / 4>(xb, cc0, s_colmax[1]);
+            work_sync();
+            const uint32_t hoa = (uint32_t)(ja & 1) * bhb2, hob = (uint32_t)(jb & 1) * bhb2;
+            write_b_row_oz<kVals / 4>(xa, cc0, ja >> 1, bhb + hoa, bmb + hoa, blb + hoa, L.sbo_b, s_colmax[1]);
+            write_b_row_oz<kVals / 4>(xb, cc0, jb >> 1, bhb + hob, bmb + hob, blb + hob, L.sbo_b, s_colmax[1]);
           } else if (next == 1) {
             // sum / difference operand of the next matrix, K row i
             float2 sd[kVals / 4];
@@ -1022,16 +1268,17 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
-template <bool BF>
+// OPM: operand mode, 0 = 3xTF32, 1 = split-BF16x3, 2 = split-BF16x6 (exact sums)
+template <int OPM>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel(const __grid_constant__ TcParams tp) {
   const TcParams* prm = &tp;
-  tc_persistent<BF>([prm](int64_t t) { return TileRef{prm, t}; }, tp.p.g.tiles);
+  tc_persistent<OPM != 0, OPM == 2>([prm](int64_t t) { return TileRef{prm, t}; }, tp.p.g.tiles);
 }
 
 // Many propagations' lane-matrix passes in one launch (all with the same lane extent):
 // global tile b is tile (b - offsets[i]) of params[i], offsets[i] <= b < offsets[i + 1];
 // offsets[count] is the total.
-template <bool BF>
+template <int OPM>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel_batched(const TcParams* __restrict__ params,
                                                                         const uint2* __restrict__ owners,
                                                                         int64_t total) {
@@ -1042,11 +1289,11 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel_batche
     const uint2 o = __ldg(owners + b);
     return TileRef{params + o.x, (int64_t)o.y};
   };
-  tc_persistent<BF>(resolve, total);
+  tc_persistent<OPM != 0, OPM == 2>(resolve, total);
 }
 
 // ------------------------------------------------------------------ host side
-size_t angular_tc_smem_bytes(int n, bool par, bool bf) { return tc_layout(n, par, bf).total; }
+size_t angular_tc_smem_bytes(int n, bool par, int mode) { return tc_layout(n, par, mode != 0, mode == 2).total; }
 
 int angular_tc_columns(int n) { return tc_shape(n).bn; }
 
@@ -1075,7 +1322,10 @@ static size_t tc_max_dynamic_smem() {
   size_t m = 0;
   for (int n = 32; n <= 256; n *= 2)
     for (int par = 0; par < 2; ++par)
-      for (int bf = 0; bf < 2; ++bf) m = tc_layout(n, par, bf).total > m ? tc_layout(n, par, bf).total : m;
+      for (int mode = 0; mode < 3; ++mode) {
+        const size_t t = tc_layout(n, par, mode != 0, mode == 2).total;
+        m = t > m ? t : m;
+      }
   return m;
 }
 
@@ -1106,17 +1356,21 @@ static unsigned persistent_grid(int64_t tiles) {
 }
 
 cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners_dev, int64_t blocks, size_t smem,
-                                      bool bf, cudaStream_t s) {
-  static bool configured[2] = {false, false};
-  const void* kern = bf ? (const void*)angular_tc_kernel_batched<true> : (const void*)angular_tc_kernel_batched<false>;
-  if (!configure_once(kern, configured[bf ? 1 : 0])) return cudaGetLastError();
+                                      int mode, cudaStream_t s) {
+  static bool configured[3] = {false, false, false};
+  if (mode < 0 || mode > 2) return cudaErrorInvalidValue;
+  const void* kerns[3] = {(const void*)angular_tc_kernel_batched<0>, (const void*)angular_tc_kernel_batched<1>,
+                          (const void*)angular_tc_kernel_batched<2>};
+  if (!configure_once(kerns[mode], configured[mode])) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
   const TcParams* prm = reinterpret_cast<const TcParams*>(params_dev);
   const uint2* own = reinterpret_cast<const uint2*>(owners_dev);
-  if (bf)
-    angular_tc_kernel_batched<true><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
+  if (mode == 2)
+    angular_tc_kernel_batched<2><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
+  else if (mode == 1)
+    angular_tc_kernel_batched<1><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
   else
-    angular_tc_kernel_batched<false><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
+    angular_tc_kernel_batched<0><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
   count_launch();
   return cudaGetLastError();
 }
@@ -1184,10 +1438,56 @@ static void tc_images(const TcShape& S, bool bf, F a, std::vector<float>& out) {
   }
 }
 
+// Split-BF16x6 chunk images: per K chunk three 8 KB slice images s0, s1, s2 (bf16, the same
+// core-matrix order), each row cut at the power of two above its largest magnitude over all
+// of K: a = s0 + s1 + s2 + O(2^-24 max), s_i a multiple of 2^(e-8-8i) with |s_i| <= 2^(e-8i)
+// (see oz_quanta for the B side and why the sums are then exact).
+template <typename F>
+static void tc_images_oz(const TcShape& S, F a, std::vector<float>& out) {
+  const int rows = 128 * S.mh;
+  out.assign((size_t)S.nk * 3 * (kChunkBytes / 4), 0.0f);
+  std::vector<double> q0(rows, 0.0);
+  for (int r = 0; r < rows; ++r) {
+    double amax = 0.0;
+    for (int k = 0; k < S.kdim; ++k) amax = std::max(amax, std::fabs(a(r, k)));
+    int e = 0;
+    if (amax > 0.0) std::frexp(amax, &e);  // amax < 2^e
+    q0[r] = amax > 0.0 ? std::ldexp(1.0, e - 8) : 0.0;
+  }
+  auto bf16_bits = [](double s) {  // s is exactly a bf16 value
+    const float f = (float)s;
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    return (uint16_t)(b >> 16);
+  };
+  for (int q = 0; q < S.nk; ++q) {
+    unsigned char* base = reinterpret_cast<unsigned char*>(out.data() + (size_t)q * 3 * (kChunkBytes / 4));
+    for (int r = 0; r < rows; ++r) {
+      if (q0[r] == 0.0) continue;
+      const double qs[3] = {q0[r], std::ldexp(q0[r], -8), std::ldexp(q0[r], -16)};
+      for (int kk = 0; kk < S.chunk_k; ++kk) {
+        double rem = a(r, q * S.chunk_k + kk);
+        const size_t off = (size_t)(r >> 3) * S.sbo_a + (size_t)(kk / S.kc) * 128 + (size_t)(r & 7) * 16 +
+                           (size_t)(kk % S.kc) * 2;
+        for (int sl = 0; sl < 3; ++sl) {
+          const double sv = std::nearbyint(rem / qs[sl]) * qs[sl];
+          rem -= sv;
+          const uint16_t h = bf16_bits(sv);
+          std::memcpy(base + (size_t)sl * kChunkBytes + off, &h, 2);
+        }
+      }
+    }
+  }
+}
+
 // One real n x n matrix (row-major FP64: out[r] = sum_k m[r][k] in[k]), zero-padded to M.
-void angular_tc_images(const double* m, int n, bool bf, std::vector<float>& out) {
-  tc_images(tc_shape(n, false, bf), bf, [&](int r, int k) { return (r < n && k < n) ? m[(size_t)r * n + k] : 0.0; },
-            out);
+// mode: 0 3xTF32, 1 split-BF16x3, 2 split-BF16x6
+void angular_tc_images(const double* m, int n, int mode, std::vector<float>& out) {
+  auto a = [&](int r, int k) { return (r < n && k < n) ? m[(size_t)r * n + k] : 0.0; };
+  if (mode == 2)
+    tc_images_oz(tc_shape(n, false, true, true), a, out);
+  else
+    tc_images(tc_shape(n, false, mode == 1), mode == 1, a, out);
 }
 
 // Parity structure of a lane matrix for the split form (n = 256 only):
@@ -1213,13 +1513,22 @@ int angular_tc_parity(const double* m, int n) {
 
 // A images of the split form: rows 0..127 the first half (even l, or E), rows 128..255
 // the second (odd l, or O), K = n / 2.
-void angular_tc_parity_images(const double* m, int n, int kind, bool bf, std::vector<float>& out) {
+void angular_tc_parity_images(const double* m, int n, int kind, int mode, std::vector<float>& out) {
   const int hn = n / 2;
-  const TcShape S = tc_shape(n, true, bf);
-  if (kind == 1)
-    tc_images(S, bf, [&](int r, int k) { return m[(size_t)(2 * (r % hn) + r / hn) * n + k]; }, out);
-  else
-    tc_images(S, bf, [&](int r, int k) { return m[(size_t)(r % hn) * n + 2 * k + r / hn]; }, out);
+  const bool bf = mode != 0;
+  const TcShape S = tc_shape(n, true, bf, mode == 2);
+  auto a1 = [&](int r, int k) { return m[(size_t)(2 * (r % hn) + r / hn) * n + k]; };
+  auto a2 = [&](int r, int k) { return m[(size_t)(r % hn) * n + 2 * k + r / hn]; };
+  if (mode == 2) {
+    if (kind == 1)
+      tc_images_oz(S, a1, out);
+    else
+      tc_images_oz(S, a2, out);
+  } else if (kind == 1) {
+    tc_images(S, bf, a1, out);
+  } else {
+    tc_images(S, bf, a2, out);
+  }
 }
 
 int angular_tc_trace_slots() { return kTraceSlots; }
@@ -1261,7 +1570,7 @@ cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_ou
 }
 
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
-                              int error_slot, const int* parity, bool bf, cudaStream_t s,
+                              int error_slot, const int* parity, int mode, cudaStream_t s,
                               unsigned long long* trace) {
   TcParams tp{};
   tp.trace = trace;
@@ -1273,15 +1582,19 @@ cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, 
     tp.parity[i] = parity ? parity[i] : 0;
   }
   tp.error_slot = error_slot;
-  const size_t smem = angular_tc_smem_bytes((int)p.g.n, tp.parity[0] != 0, bf);
-  static bool configured[2] = {false, false};
-  const void* kern = bf ? (const void*)angular_tc_kernel<true> : (const void*)angular_tc_kernel<false>;
-  if (!configure_once(kern, configured[bf ? 1 : 0])) return cudaGetLastError();
+  if (mode < 0 || mode > 2) return cudaErrorInvalidValue;
+  const size_t smem = angular_tc_smem_bytes((int)p.g.n, tp.parity[0] != 0, mode);
+  static bool configured[3] = {false, false, false};
+  const void* kerns[3] = {(const void*)angular_tc_kernel<0>, (const void*)angular_tc_kernel<1>,
+                          (const void*)angular_tc_kernel<2>};
+  if (!configure_once(kerns[mode], configured[mode])) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
-  if (bf)
-    angular_tc_kernel<true><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
+  if (mode == 2)
+    angular_tc_kernel<2><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
+  else if (mode == 1)
+    angular_tc_kernel<1><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
   else
-    angular_tc_kernel<false><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
+    angular_tc_kernel<0><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
   count_launch();
   return cudaGetLastError();
 }

@@ -160,16 +160,17 @@ int angular_tc_columns(int n);  // complex columns of the inner axis per CTA til
 bool angular_tc_eligible(const Geometry& g);
 // the pass's point-wise ops fit the per-tile tables of the tensor-core kernel
 bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis);
-size_t angular_tc_smem_bytes(int n, bool par = false, bool bf = false);
-// A-operand chunk images (bf: split-BF16x3 bf16 parts; else 3xTF32 tf32 parts), raw bytes in a float vector
-void angular_tc_images(const double* m, int n, bool bf, std::vector<float>& out);
+// operand modes of the tensor-core pass: 0 3xTF32, 1 split-BF16x3, 2 split-BF16x6 (exact sums)
+size_t angular_tc_smem_bytes(int n, bool par = false, int mode = 0);
+// A-operand chunk images of an operand mode, raw bytes in a float vector
+void angular_tc_images(const double* m, int n, int mode, std::vector<float>& out);
 // parity structure of a real n x n lane matrix (0 none, 1 row signs, 2 column signs; n = 256 only)
 int angular_tc_parity(const double* m, int n);
-void angular_tc_parity_images(const double* m, int n, int kind, bool bf, std::vector<float>& out);
+void angular_tc_parity_images(const double* m, int n, int kind, int mode, std::vector<float>& out);
 // parity: per matrix 0 / 1 / 2 (all 0, or all non-zero with the split images); trace: optional
 // per-tile phase timestamps (angular_tc_trace_slots() per tile), nullptr: off
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
-                              int error_slot, const int* parity, bool bf, cudaStream_t s,
+                              int error_slot, const int* parity, int mode, cudaStream_t s,
                               unsigned long long* trace = nullptr);
 int angular_tc_trace_slots();
 // one CTA waits (limit_ns, both wait forms) on an mbarrier nothing completes; out[3]:
@@ -186,7 +187,7 @@ void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const floa
                     const int* parity, void* out);
 // owners_dev: blocks pairs (pass index, tile within the pass), uint32 each, in global tile order
 cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners_dev, int64_t blocks, size_t smem,
-                                      bool bf, cudaStream_t s);
+                                      int mode, cudaStream_t s);
 
 // Auxiliary kernels (aux_kernels.cu)
 cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);

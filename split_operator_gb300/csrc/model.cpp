@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 
 #include "model.hpp"
@@ -311,24 +312,63 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
   }
   c.version = version;
   c.real = real;
-  if (!fp64 && (tc_tf32 || tc_bf16) && real && count == 1 && (n == 32 || n == 64 || n == 128 || n == 256)) {
+  if (!fp64 && tc_mode() >= 0 && real && count == 1 && (n == 32 || n == 64 || n == 128 || n == 256)) {
     std::vector<double> md(n * n);
     for (size_t i = 0; i < n * n; ++i) md[i] = m[i].real();
-    std::vector<float> img;
-    angular_tc_images(md.data(), (int)n, tc_bf16, img);
-    upload(c.tc_images, img, stream);
-    tc_images_by_matrix_[c.buf.ptr] = c.tc_images.as<float>();
+    int kind = 0;
+    shared_tc_images(md, (int)n, tc_mode(), stream, c.tc_images, c.tc_par_images, kind);
+    tc_images_by_matrix_[c.buf.ptr] = c.tc_images->as<float>();
     // the parity-split form as well, when the matrix has the structure (Legendre pairs)
-    const int kind = angular_tc_parity(md.data(), (int)n);
-    if (kind) {
-      angular_tc_parity_images(md.data(), (int)n, kind, tc_bf16, img);
-      upload(c.tc_par_images, img, stream);
-      tc_parity_by_matrix_[c.buf.ptr] = {kind, c.tc_par_images.as<float>()};
-    } else {
+    if (kind)
+      tc_parity_by_matrix_[c.buf.ptr] = {kind, c.tc_par_images->as<float>()};
+    else
       tc_parity_by_matrix_.erase(c.buf.ptr);
-    }
   }
   return c.buf.ptr;
+}
+
+// Process-wide cache of tensor-core A images by matrix value: every propagation on the same
+// polar grid has the same Legendre pair, so a batch of hundreds of propagations streams a
+// few images (which stay in L2) instead of one copy per propagation.  Entries are held
+// weakly: an image lives as long as an engine uses it.
+namespace {
+struct ImageEntry {
+  int device, n, mode, kind;
+  std::vector<double> m;
+  std::weak_ptr<DeviceBuffer> img, par;
+};
+std::mutex g_images_mu;
+std::vector<ImageEntry> g_images;
+}  // namespace
+
+void Engine::shared_tc_images(const std::vector<double>& md, int n, int mode, cudaStream_t s,
+                              std::shared_ptr<DeviceBuffer>& img, std::shared_ptr<DeviceBuffer>& par, int& kind) {
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lock(g_images_mu);
+  g_images.erase(std::remove_if(g_images.begin(), g_images.end(), [](const ImageEntry& e) { return e.img.expired(); }),
+                 g_images.end());
+  for (const ImageEntry& e : g_images)
+    if (e.device == dev && e.n == n && e.mode == mode && e.m == md) {
+      img = e.img.lock();
+      par = e.par.lock();
+      if (img && (e.kind == 0 || par)) {
+        kind = e.kind;
+        return;
+      }
+    }
+  std::vector<float> h;
+  angular_tc_images(md.data(), n, mode, h);
+  img = std::make_shared<DeviceBuffer>();
+  upload(*img, h, s);
+  kind = angular_tc_parity(md.data(), n);
+  par.reset();
+  if (kind) {
+    angular_tc_parity_images(md.data(), n, kind, mode, h);
+    par = std::make_shared<DeviceBuffer>();
+    upload(*par, h, s);
+  }
+  g_images.push_back(ImageEntry{dev, n, mode, kind, md, img, par});
 }
 
 bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& p) {
@@ -377,14 +417,15 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
     p.partials = partials_.as<double>();
   }
-  std::string name = std::string(tc_bf16 ? "f32 tcbf16x3" : "f32 tc3xtf32") + (par ? " parity axis" : " axis") +
+  static const char* const kTcNames[3] = {"f32 tc3xtf32", "f32 tcbf16x3", "f32 tcbf16x6"};
+  std::string name = std::string(kTcNames[tc_mode()]) + (par ? " parity axis" : " axis") +
                      std::to_string(axis) + ":";
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
     // threads: the lane extent, the parity mode and the operand format (one batched launch
     // serves one of each; the kernel's thread count is fixed)
     RecordedPass r{RecordedPass::TensorCore, false, p, std::vector<unsigned char>(tc_params_bytes()),
-                   (int)g.n | (par ? 1 << 16 : 0) | (tc_bf16 ? 1 << 17 : 0), angular_tc_smem_bytes((int)g.n, par, tc_bf16),
+                   (int)g.n | (par ? 1 << 16 : 0) | (tc_mode() << 17), angular_tc_smem_bytes((int)g.n, par, tc_mode()),
                    name, pass_bytes(ops, g)};
     make_tc_params(p, mats, nmat, images, timeout_slot, parity, r.tcp.data());
     recording->push_back(std::move(r));
@@ -401,7 +442,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     trace = DeviceBuffer((size_t)g.tiles * angular_tc_trace_slots() * sizeof(unsigned long long));
     cuda_check(cudaMemsetAsync(trace.ptr, 0, trace.bytes, stream), "trace clear");
   }
-  cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, parity, tc_bf16, stream,
+  cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, parity, tc_mode(), stream,
                                trace_path ? trace.as<unsigned long long>() : nullptr),
              "tensor-core pass launch");
   if (trace_path) {
@@ -478,7 +519,7 @@ void Engine::submit(const Action& a) {
   }
   const int need = k == OP_NORM ? 1 : (k == OP_DOT ? 2 : 0);
   if ((int)cur_.size() >= kMaxOps || cur_red_ + need > kMaxRed) flush();
-  if (k == OP_MAT && (tc_tf32 || tc_bf16)) {
+  if (k == OP_MAT && tc_mode() >= 0) {
     // the tensor-core pass holds at most two lane-matrix products
     int mats = 0;
     for (const DevOp& o : cur_) mats += o.kind == OP_MAT;
@@ -522,7 +563,7 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   p.nred = nred;
   if (fft) p.twiddle = twiddle((size_t)p.g.n);
   pass_choose_buffers(p, fp64);
-  if (!fp64 && (tc_tf32 || tc_bf16) && !resident && try_launch_tc(ops, axis, p)) return;
+  if (!fp64 && tc_mode() >= 0 && !resident && try_launch_tc(ops, axis, p)) return;
   if ((fft_pair || (fp64 && p.g.n > 4096)) && fft_pair_plan(p, fp64, resident)) name_tag = " fftpair";
   if (fp64 && p.g.n > 4096 && !p.fused)
     throw Error(SO_ERR_UNSUPPORTED, "FP64 lanes longer than 4096 points are not supported outside FFT-pair passes "
@@ -1129,11 +1170,12 @@ static std::vector<int> choose_perm(size_t ndim, const OperationStack& st) {
 
 Propagation::Propagation(WaveFunction& src, so_time_grid time, std::shared_ptr<OperationStack> stack, int prec)
     : precision(prec), time_(time), stack_(std::move(stack)) {
-  if (prec < SO_PRECISION_FP64 || prec > SO_PRECISION_FP32_SIMT) throw Error(SO_ERR_INVALID, "unknown precision");
+  if (prec < SO_PRECISION_FP64 || prec > SO_PRECISION_FP32_BF16X6) throw Error(SO_ERR_INVALID, "unknown precision");
   const bool fp64 = prec == SO_PRECISION_FP64;
   wf_ = std::make_unique<WaveFunction>(src.shape, src.grids, choose_perm(src.shape.size(), *stack_), fp64);
   wf_->eng->tc_tf32 = prec == SO_PRECISION_FP32_TF32X3;
   wf_->eng->tc_bf16 = prec == SO_PRECISION_FP32_BF16X3;
+  wf_->eng->tc_bf16x6 = prec == SO_PRECISION_FP32_BF16X6;
   {
     const char* fp = std::getenv("SO_FFT_PAIR");  // "0": FFT pairs run the general pass kernel
     wf_->eng->fft_pair = !(fp && fp[0] == '0');
@@ -1686,7 +1728,7 @@ void Batch::run_groups(std::vector<Group>& gs) {
     }
     if (g.kind == RecordedPass::TensorCore)
       cuda_check(launch_angular_tc_batched(g.params.ptr, g.owners.ptr, g.blocks, g.smem,
-                                           (g.threads >> 17) & 1, stream_),
+                                           (g.threads >> 17) & 3, stream_),
                  "batched tensor-core pass");
     else
       cuda_check(launch_pass_batched(g.fp64, g.sweep, (g.threads >> 16) & 1, g.params.as<PassParams>(),

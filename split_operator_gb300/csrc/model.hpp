@@ -124,9 +124,14 @@ class Engine {
   cudaStream_t stream = nullptr;
   int nonfinite_slot = 0;
   int timeout_slot = 0;
-  bool tc_tf32 = false;  // real lane matrices on the tensor cores (3xTF32); FP32 state only
+  // real lane matrices on the tensor cores (FP32 state only): 3xTF32, split-BF16x3 or
+  // split-BF16x6 (exact tensor-core sums)
+  bool tc_tf32 = false;
   bool tc_bf16 = false;
-  bool fft_pair = true;  // FP32 FFT-pair passes run the fused register kernel (SO_FFT_PAIR=0: the general pass)  // the same as split-BF16x3
+  bool tc_bf16x6 = false;
+  // operand mode of the tensor-core pass (0 3xTF32, 1 split-BF16x3, 2 split-BF16x6), -1: none
+  int tc_mode() const { return tc_tf32 ? 0 : (tc_bf16 ? 1 : (tc_bf16x6 ? 2 : -1)); }
+  bool fft_pair = true;  // FP32 FFT-pair passes run the fused register kernel (SO_FFT_PAIR=0: the general pass)
 
   size_t points() const;
   size_t elem_bytes() const { return fp64 ? 16 : 8; }
@@ -195,13 +200,17 @@ class Engine {
     uint64_t version;
     DeviceBuffer buf;
     bool real;
-    DeviceBuffer tc_images;      // 3xTF32 A-operand chunk images (tensor-core passes)
-    DeviceBuffer tc_par_images;  // the same for the parity-split form (when the matrix has it)
+    // A-operand chunk images of the tensor-core passes, and the same for the parity-split
+    // form (when the matrix has it): shared by every engine of the process whose matrix has
+    // the same values (all propagations on one polar grid), so one copy stays hot in L2
+    std::shared_ptr<DeviceBuffer> tc_images, tc_par_images;
   };
   std::map<std::pair<const void*, int>, Cached> tables_;
   std::map<const void*, const float*> tc_images_by_matrix_;
   std::map<const void*, std::pair<int, const float*>> tc_parity_by_matrix_;  // parity kind, split images
   bool try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& p);
+  static void shared_tc_images(const std::vector<double>& md, int n, int mode, cudaStream_t s,
+                               std::shared_ptr<DeviceBuffer>& img, std::shared_ptr<DeviceBuffer>& par, int& kind);
   std::map<uint64_t, DeviceBuffer> weights_;
   std::map<size_t, DeviceBuffer> twiddles_;
   // open pass

@@ -193,6 +193,30 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// three 32 x 16 loads at column offsets 0, step, 2 step from taddr (the regions R0, R1, R2 of
+// one accumulator layout), one wait for all of them
+__device__ __forceinline__ void tmem_ld16x3(uint32_t taddr, uint32_t step, float* v0, float* v1, float* v2) {
+  uint32_t r[48];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[16 * k + 0]), "=r"(r[16 * k + 1]), "=r"(r[16 * k + 2]), "=r"(r[16 * k + 3]), "=r"(r[16 * k + 4]),
+          "=r"(r[16 * k + 5]), "=r"(r[16 * k + 6]), "=r"(r[16 * k + 7]), "=r"(r[16 * k + 8]), "=r"(r[16 * k + 9]),
+          "=r"(r[16 * k + 10]), "=r"(r[16 * k + 11]), "=r"(r[16 * k + 12]), "=r"(r[16 * k + 13]),
+          "=r"(r[16 * k + 14]), "=r"(r[16 * k + 15])
+        : "r"(taddr + (uint32_t)k * step)
+        : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    v0[i] = __uint_as_float(r[i]);
+    v1[i] = __uint_as_float(r[16 + i]);
+    v2[i] = __uint_as_float(r[32 + i]);
+  }
+}
+
 __device__ __forceinline__ float round_tf32(float x) {
   return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }

@@ -24,8 +24,8 @@ pytestmark = pytest.mark.gpu
 
 NR, NTH = 4096, 128
 CHECKPOINTS = (100, 1000, 10000)
-FP32_MODES = ("fp32_simt", "fp32_tf32x3", "fp32_bf16x3")
-ONE_STEP_TOL = {"fp32_simt": 1e-6, "fp32_tf32x3": 1e-6, "fp32_bf16x3": 2e-5}
+FP32_MODES = ("fp32_simt", "fp32_tf32x3", "fp32_bf16x3", "fp32_bf16x6")
+ONE_STEP_TOL = {"fp32_simt": 1e-6, "fp32_tf32x3": 1e-6, "fp32_bf16x3": 2e-5, "fp32_bf16x6": 1e-6}
 
 
 def _norm(psi, wr, wth):

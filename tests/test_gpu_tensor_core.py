@@ -1,4 +1,5 @@
-"""Tensor-core (tcgen05, 3xTF32) lane-matrix pass against FP64 references."""
+"""Tensor-core (tcgen05) lane-matrix pass against FP64 references: 3xTF32, split-BF16x3 and
+split-BF16x6 (three fixed-point bf16 slices per operand, exact FP32 sums)."""
 import numpy as np
 import pytest
 
@@ -38,7 +39,7 @@ def test_real_lane_matrix_3xtf32_matches_fp64(so, n, nr):
     assert err2 < 4e-6, err2
 
 
-@pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_simt"])
+@pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_simt", "fp32_bf16x6"])
 @pytest.mark.parametrize("n", [128, 64, 256])
 def test_two_lane_matrices_in_one_pass(so, precision, n):
     """Stack [T-transformation, diagonal D]: a step is T, D, T2 (the inverse slot holds T2),
@@ -73,10 +74,12 @@ def test_two_lane_matrices_in_one_pass(so, precision, n):
     assert err < 1e-5, err
 
 
-@pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_simt"])
+@pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_simt", "fp32_bf16x6"])
 def test_orthogonal_lane_matrix_keeps_the_norm(so, precision):
     """200 applications of an orthogonal matrix: the norm may random-walk at the FP32
-    level but must not drift systematically (a biased split would shrink it)."""
+    level but must not drift systematically (a biased split would shrink it).  The
+    split-BF16x6 sums are exact on the tensor core, so it keeps the norm like the FP32
+    CUDA-core product does."""
     n, nr = 128, 512
     rng = np.random.default_rng(7)
     q, _ = np.linalg.qr(rng.standard_normal((n, n)))
@@ -96,6 +99,12 @@ def test_orthogonal_lane_matrix_keeps_the_norm(so, precision):
     # measured on GB300: SIMT ~1e-7, 3xTF32 ~2.4e-5 (tensor-core accumulation truncates;
     # the pass spreads the products over several accumulators, one accumulator gave 3.3e-4)
     assert drift < (4e-5 if precision == "fp32_tf32x3" else 2e-6), drift
+    if precision == "fp32_bf16x6":
+        # and the matrix products themselves: 200 applications of q against FP64
+        ref = psi.copy()
+        for _ in range(200):
+            ref = ref @ q.T
+        assert rel_l2(a, ref) < 2e-5
 
 
 def test_tensor_core_pass_is_used(so):
@@ -107,11 +116,12 @@ def test_tensor_core_pass_is_used(so):
     assert any("tc3xtf32" in k for k in names), names
 
 
+@pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_bf16x6"])
 @pytest.mark.parametrize("nr,nth", [(256, 32), (512, 64), (1024, 128), (512, 256)])
-def test_radial_angular_tf32x3_close_to_oracle(so, nr, nth):
+def test_radial_angular_tf32x3_close_to_oracle(so, nr, nth, precision):
     from split_operator_gb300 import workloads as W
     steps = 20
-    prop, h = W.radial_angular_2d(nr=nr, nth=nth, step_no=steps, r0=25.0, precision="fp32_tf32x3")
+    prop, h = W.radial_angular_2d(nr=nr, nth=nth, step_no=steps, r0=25.0, precision=precision)
     oprop, odamp = S.radial_angular_2d(nr=nr, nth=nth, step_no=steps, r0=25.0)
     prop.steps(1)
     oprop.step()
@@ -126,14 +136,15 @@ def test_radial_angular_tf32x3_close_to_oracle(so, nr, nth):
     assert abs(prop.norm() - oprop.wave_function.norm()) < (6e-5 if nth == 256 else 2.5e-5)
 
 
-def test_parity_split_legendre_pair_matches_plain_form(so, monkeypatch):
+@pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_bf16x6"])
+def test_parity_split_legendre_pair_matches_plain_form(so, monkeypatch, precision):
     """n = 256 Legendre pair: the parity-split GEMMs (two K = 128 halves) give the same
     propagation as the plain 256 x 256 form, both within FP32 accuracy of FP64."""
     from split_operator_gb300 import workloads as W
     out = {}
     for flag in ("1", "0"):
         monkeypatch.setenv("SO_TC_PARITY", flag)
-        prop, _ = W.radial_angular_2d(nr=512, nth=256, step_no=10 ** 6, precision="fp32_tf32x3")
+        prop, _ = W.radial_angular_2d(nr=512, nth=256, step_no=10 ** 6, precision=precision)
         prop.set_timing(True)
         prop.steps(6)
         names = [t[0] for t in prop.kernel_times()]
@@ -168,3 +179,33 @@ def test_real_lane_matrix_split_bf16x3(so, n, nr):
     assert any("tcbf16x3" in k[0] for k in prop.kernel_times())
     err = rel_l2(prop.get_array(), psi @ t.T)
     assert err < 3e-5, err
+
+
+@pytest.mark.parametrize("n,nr", [(128, 256), (64, 128), (32, 64), (128, 4096), (256, 256), (256, 1024)])
+def test_real_lane_matrix_split_bf16x6(so, n, nr):
+    """Split-BF16x6: each operand as three fixed-point bf16 slices (8 significant bits each,
+    one quantum per matrix row and per state column), six slice products accumulated exactly
+    by the tensor core.  What remains is the FP32 state in and out, the 2^-24 slicing
+    remainder and the final round-to-nearest: about 1e-7, several times below 3xTF32."""
+    rng = np.random.default_rng(11 * n + nr)
+    psi = rng.standard_normal((nr, n)) + 1j * rng.standard_normal((nr, n))
+    # rows and columns of very different magnitudes: every row and column gets its own quantum
+    psi *= np.exp(rng.uniform(-8, 8, nr))[:, None]
+    t = rng.standard_normal((n, n)) / np.sqrt(n) * np.exp(rng.uniform(-4, 4, n))[:, None]
+    g0 = so.Grid.new_linear_continuos("r", 0.0, 1.0, nr, 0)
+    g1 = so.Grid.new_linear_countable("th", 0.0, 1.0, n, 1)
+    wf = so.WaveFunction(psi, [g0, g1])
+    mt = so.MatrixTransformation(g1, so.Grid.new_linear_countable("l", 0.0, 1.0, n, 1))
+    mt.set_diagonalization_matrix(t.astype(np.complex128), np.eye(n, dtype=np.complex128))
+    st = so.OperationStack()
+    st.add_transformation(mt, so.NORMAL)
+    prop = so.Propagation(wf, so.TimeGrid(1.0, 3), st, "fp32_bf16x6")
+    prop.set_timing(True)
+    prop.steps(1)
+    assert any("tcbf16x6" in k[0] for k in prop.kernel_times())
+    ref = psi @ t.T
+    got = prop.get_array()
+    # per output element: within a few FP32 rounding units of its row of |T| |psi|
+    bound = (np.abs(psi) @ np.abs(t).T)
+    assert np.max(np.abs(got - ref) / bound) < 6e-7, np.max(np.abs(got - ref) / bound)
+    assert rel_l2(got, ref) < 5e-7
