@@ -47,6 +47,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
                     help="timed region only (no e2e, accuracy or CPU legs): the case profiled under ncu")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="built-in launch schedules (the autotuner is skipped)")
+    ap.add_argument("--tune-cache", default=None,
+                    help="autotuner schedule cache: loaded instead of tuning when it exists, else written")
     return ap.parse_args()
 
 
@@ -310,6 +314,23 @@ def run_ours(a):
         batch.set_timing(False)
         return e0.elapsed_time(e1), kt
 
+    # launch schedules: the built-in ones are timed first (for the record), then the autotuner
+    # picks per lane extent on this workload (states restored) unless a cache file is given
+    tune = None
+    if not single and not a.no_tune:
+        import tempfile
+        so.reset_schedules()
+        run_steps(a.warmup, False)
+        ms_default, _ = run_steps(a.steps, False)
+        cache = a.tune_cache or os.path.join(tempfile.gettempdir(), f"split_operator_gb300_schedules_{os.getpid()}.json")
+        if a.tune_cache and os.path.exists(a.tune_cache):
+            so.load_schedules(a.tune_cache)
+            rep = {"loaded_from": a.tune_cache}
+        else:
+            t0 = time.perf_counter()
+            rep = batch.tune(cache, trial_steps=3)
+            rep["tune_wall_s"] = time.perf_counter() - t0
+        tune = {"default_schedule_ms_per_step": ms_default / a.steps, "report": rep}
     run_steps(a.warmup, False)
     clocks = Clocks(local)
     clocks.start()
@@ -329,11 +350,15 @@ def run_ours(a):
         # per-launch breakdown of the same K steps with CUDA events on every batched launch
         ms_t, kt = run_steps(a.steps, True)
     roof = roofline_from(kt, ms if single else ms_t)
+    if tune is not None:
+        tune["tuned_ms_per_step"] = ms_max / a.steps
+        tune["gain"] = tune["default_schedule_ms_per_step"] / tune["tuned_ms_per_step"]
 
     if a.quick:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms_max / a.steps,
-                              "quick": True, "passes": [list(t) for t in kt], "roofline": roof}), flush=True)
+                              "quick": True, "passes": [list(t) for t in kt], "roofline": roof, "autotune": tune}),
+                  flush=True)
         return
 
     # end to end through the C ABI: pinned FP64 host state in, one step, state out
@@ -486,7 +511,7 @@ def run_ours(a):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "global_batch": len(props) * world, "wall_s_timed_region": wall},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clocks.summary(), "accuracy_vs_fp64": acc, "passes": [list(t) for t in kt]}
+            "clocks": clocks.summary(), "accuracy_vs_fp64": acc, "autotune": tune, "passes": [list(t) for t in kt]}
     print(json.dumps(line), flush=True)
 
 

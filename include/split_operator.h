@@ -322,7 +322,22 @@ int so_batch_get_arrays(so_batch b, double* const* out, size_t count);
  * copied in (copy engines), stepped and copied out, so the host link's two directions
  * and the chunks' steps overlap.  `in` and `out` may be the same arrays. */
 int so_batch_steps_host(so_batch b, const double* const* in, double* const* out, size_t count, uint64_t steps);
+/* Autotuner (no counterpart in the reference, whose lane loops over rayon --
+ * fft_transformation.rs:59-68, matrix_transformation.rs:64-65 -- have no launch shape to pick).
+ * For every lane extent of the batch's passes it times candidate launch schedules on the live
+ * workload with CUDA events, `trial_steps` steps each: FFT-pair pass threads per CTA (lanes per
+ * tile) and Stockham radix; tensor-core pass CTAs per SM and tile order.  The fastest per extent
+ * goes into the process-wide schedule table that every later pass launch reads; the table is
+ * written to `cache_path` as JSON (NULL: no file).  Every member's state, losses and step count
+ * are restored afterwards.  `report` (may be NULL) receives a JSON report of the trials. */
+int so_batch_tune(so_batch b, const char* cache_path, int trial_steps, char* report, size_t cap);
 void so_batch_free(so_batch b);
+
+/* The process-wide launch schedule table (read by every pass launch): load a cache file the
+ * tuner wrote, save the current table, or return to the built-in defaults. */
+int so_schedules_load(const char* path);
+int so_schedules_save(const char* path);
+int so_schedules_reset(void);
 
 /* ---- Learned starting states (no counterpart in the reference) ----
  * A multilayer perceptron (tanh hidden layers, linear output) trained with hand-written

@@ -130,6 +130,10 @@ SIGNATURES = {
     "so_propagation_describe": [_P, C.c_char_p, _S],
     "so_propagation_set_timing": [_P, _I],
     "so_propagation_kernel_times": [_P, C.c_char_p, _S],
+    "so_batch_tune": [_P, _STR, _I, C.c_char_p, _S],
+    "so_schedules_load": [_STR],
+    "so_schedules_save": [_STR],
+    "so_schedules_reset": [],
     "so_propagation_checkpoint": [_P, _P, _S, _SP],
     "so_propagation_restore": [_P, _P, _S],
     "so_propagation_steps_done": [_P, C.POINTER(C.c_uint64)],

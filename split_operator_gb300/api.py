@@ -722,6 +722,14 @@ class Batch(_Handle):
         arr = (C.c_void_p * len(host_ptrs))(*host_ptrs)
         call("so_batch_get_arrays", self._h, C.cast(arr, C.POINTER(C.c_void_p)), len(host_ptrs))
 
+    def tune(self, cache_path: Optional[str] = None, trial_steps: int = 4) -> dict:
+        """Autotune the launch schedules of the batch's FFT-pair and tensor-core passes on the
+        live workload (states restored afterwards); returns the trial report."""
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        call("so_batch_tune", self._h, cache_path.encode() if cache_path else None, trial_steps, buf, 1 << 16)
+        return json.loads(buf.value.decode())
+
     def steps_host_ptr(self, in_ptrs: Sequence[int], out_ptrs: Sequence[int], n: int):
         """States in from host addresses, n steps, states out to host addresses: one
         pipelined call (chunks of members overlap their copies and steps)."""
@@ -805,3 +813,17 @@ def launch_count() -> int:
     v = C.c_uint64()
     call("so_launch_count", C.byref(v))
     return v.value
+
+
+def load_schedules(path: str):
+    """Launch schedules from a cache file the autotuner wrote (process-wide)."""
+    call("so_schedules_load", path.encode())
+
+
+def save_schedules(path: str):
+    call("so_schedules_save", path.encode())
+
+
+def reset_schedules():
+    """Back to the built-in launch schedules."""
+    call("so_schedules_reset")

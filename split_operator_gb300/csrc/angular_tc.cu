@@ -707,7 +707,10 @@ enum TraceSlot {
   TR_TABS = 32,   // per-tile tables built (work warps)
   TR_LOADED = 33, // prologue values in registers (work thread 0)
   TR_STORED = 34, // prologue operand stores issued (work thread 0)
-  kTraceSlots = 35
+  TR_DRAIN0 = 35, // first matrix: accumulators drained (work thread 0)
+  TR_APPLY0 = 36, // first matrix: point-wise ops after it applied (work thread 0)
+  TR_SYNC0 = 37,  // first matrix: the next operand's column maxima complete (split-BF16x6)
+  kTraceSlots = 38
 };
 __device__ __forceinline__ void trace_mark(const TcParams& tp, int64_t tile, int slot) {
   if (tp.trace) tp.trace[tile * kTraceSlots + slot] = tc::globaltimer_ns();
@@ -1060,6 +1063,10 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       bool ok = true;
       for (int m = 0; m < tp.nmat && ok; ++m) {
         const int kind = tp.parity[m];
+        const bool last = m + 1 == tp.nmat;
+        const int next = last ? -1 : tp.parity[m + 1];
+        // ops between this matrix and the next one (or the end of the program)
+        const int sb = tp.mat_op[m] + 1, se = last ? p.nops : tp.mat_op[m + 1];
         float v[kVals];
 #pragma unroll
         for (int e = 0; e < kVals; ++e) v[e] = 0.0f;
@@ -1070,13 +1077,15 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             ++drains;
             tc_fence_after();
 #pragma unroll
-            for (int hv = 0; hv < kVals / 16; ++hv) {
-              const uint32_t col = kind == 2 ? (uint32_t)((hv / kLd) * S.nc + (kVals / 2) * up + 16 * (hv % kLd))
-                                             : (uint32_t)(kVals * up + 16 * hv);
-              float w0[16], w1[16], w2[16];
-              tmem_ld16x3(lane_base + col, (uint32_t)S.reg_cols, w0, w1, w2);
+            for (int hv = 0; hv < kVals / 8; ++hv) {
+              // 8 columns of each region at a time (registers: the preloaded table row is live)
+              const int h16 = hv >> 1;
+              const uint32_t col = (kind == 2 ? (uint32_t)((h16 / kLd) * S.nc + (kVals / 2) * up + 16 * (h16 % kLd))
+                                              : (uint32_t)(kVals * up + 16 * h16)) + 8u * (uint32_t)(hv & 1);
+              float w0[8], w1[8], w2[8];
+              tmem_ld8x3(lane_base + col, (uint32_t)S.reg_cols, w0, w1, w2);
 #pragma unroll
-              for (int e = 0; e < 16; ++e) v[16 * hv + e] = (w2[e] + w1[e]) + w0[e];
+              for (int e = 0; e < 8; ++e) v[8 * hv + e] = (w2[e] + w1[e]) + w0[e];
             }
             tc_fence_before();
           }
@@ -1108,10 +1117,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         }
         if (!ok) break;
         if (tid == 0 && m < 2) trace_mark(tp, tile, TR_MAT0 + 2 * m);
-        const bool last = m + 1 == tp.nmat;
-        const int next = last ? -1 : tp.parity[m + 1];
-        // ops between this matrix and the next one (or the end of the program)
-        const int sb = tp.mat_op[m] + 1, se = last ? p.nops : tp.mat_op[m + 1];
+        if (tid == 0 && m == 0) trace_mark(tp, tile, TR_DRAIN0);
         if (kind != 2) {
           const int jr = kind == 1 ? 2 * i + up : j;
           if constexpr (OZ) {
@@ -1124,11 +1130,14 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             if (valid)
               apply_row<kVals / 2>(p, tabs, sb, se, x, jr, c0, base + (int64_t)jr * g.inner + c0, acc, rw_ptr,
                                    kind == 1 ? rw_sum : rw_plain);
+            if (tid == 0 && m == 0) trace_mark(tp, tile, TR_APPLY0);
             if (last) {
               if (valid) stage_row<kVals / 2>(x, c0, jr, stg, S.stage_row);
             } else {
-              colmax_rows<kVals / 2>(x, c0, s_colmax[1]);
+              // a warp whose rows all lie past the lane extent (n < 128) adds nothing
+              if (S.mh == 2 || 32 * lg < n) colmax_rows<kVals / 2>(x, c0, s_colmax[1]);
               work_sync();
+              if (tid == 0 && m == 0) trace_mark(tp, tile, TR_SYNC0);
               if (valid) {
                 const uint32_t ho = next == 2 ? (uint32_t)(jr & 1) * bhb2 : 0u;
                 write_b_row_oz<kVals / 2>(x, c0, next == 2 ? jr >> 1 : jr, bhb + ho, bmb + ho, blb + ho, L.sbo_b,
@@ -1162,6 +1171,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
           }
           apply_row<kVals / 4>(p, tabs, sb, se, xa, ja, cc0, base + (int64_t)ja * g.inner + cc0, acc, rw_ptr, rw_a);
           apply_row<kVals / 4>(p, tabs, sb, se, xb, jb, cc0, base + (int64_t)jb * g.inner + cc0, acc, rw_ptr, rw_b);
+          if (tid == 0 && m == 0) trace_mark(tp, tile, TR_APPLY0);
           if (last) {
             stage_row<kVals / 4>(xa, cc0, ja, stg, S.stage_row);
             stage_row<kVals / 4>(xb, cc0, jb, stg, S.stage_row);
@@ -1175,12 +1185,14 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             colmax_rows<kVals / 4>(sp, cc0, s_colmax[1]);
             colmax_rows<kVals / 4>(sm2, cc0, s_colmax[1]);
             work_sync();
+            if (tid == 0 && m == 0) trace_mark(tp, tile, TR_SYNC0);
             write_b_row_oz<kVals / 4>(sp, cc0, i, bhb, bmb, blb, L.sbo_b, s_colmax[1]);
             write_b_row_oz<kVals / 4>(sm2, cc0, i, bhb + bhb2, bmb + bhb2, blb + bhb2, L.sbo_b, s_colmax[1]);
           } else if (OZ) {
             colmax_rows<kVals / 4>(xa, cc0, s_colmax[1]);
             colmax_rows<kVals / 4>(xb, cc0, s_colmax[1]);
             work_sync();
+            if (tid == 0 && m == 0) trace_mark(tp, tile, TR_SYNC0);
             const uint32_t hoa = (uint32_t)(ja & 1) * bhb2, hob = (uint32_t)(jb & 1) * bhb2;
             write_b_row_oz<kVals / 4>(xa, cc0, ja >> 1, bhb + hoa, bmb + hoa, blb + hoa, L.sbo_b, s_colmax[1]);
             write_b_row_oz<kVals / 4>(xb, cc0, jb >> 1, bhb + hob, bmb + hob, blb + hob, L.sbo_b, s_colmax[1]);
@@ -1342,8 +1354,9 @@ static bool configure_once(const void* kern, bool& flag) {
   return true;
 }
 
-// persistent grid: kCtasPerSm CTAs per SM (fewer when there are fewer tiles)
-static unsigned persistent_grid(int64_t tiles) {
+// persistent grid: ctas_per_sm (1 or 2; 0 = kCtasPerSm) CTAs per SM, fewer when there are
+// fewer tiles
+static unsigned persistent_grid(int64_t tiles, int ctas_per_sm = 0) {
   static int sms = 0;
   if (sms == 0) {
     int dev = 0;
@@ -1351,12 +1364,15 @@ static unsigned persistent_grid(int64_t tiles) {
                                                   cudaSuccess)
       sms = 1;
   }
-  const int64_t slots = (int64_t)sms * kCtasPerSm;
+  const int per = (ctas_per_sm == 1 || ctas_per_sm == 2) ? ctas_per_sm : kCtasPerSm;
+  const int64_t slots = (int64_t)sms * per;
   return (unsigned)(tiles < slots ? tiles : slots);
 }
 
+int64_t angular_tc_grid(int64_t tiles, int ctas_per_sm) { return (int64_t)persistent_grid(tiles, ctas_per_sm); }
+
 cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners_dev, int64_t blocks, size_t smem,
-                                      int mode, cudaStream_t s) {
+                                      int mode, cudaStream_t s, int ctas_per_sm) {
   static bool configured[3] = {false, false, false};
   if (mode < 0 || mode > 2) return cudaErrorInvalidValue;
   const void* kerns[3] = {(const void*)angular_tc_kernel_batched<0>, (const void*)angular_tc_kernel_batched<1>,
@@ -1365,12 +1381,13 @@ cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
   const TcParams* prm = reinterpret_cast<const TcParams*>(params_dev);
   const uint2* own = reinterpret_cast<const uint2*>(owners_dev);
+  const unsigned grid = persistent_grid(blocks, ctas_per_sm);
   if (mode == 2)
-    angular_tc_kernel_batched<2><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
+    angular_tc_kernel_batched<2><<<grid, kThreads, smem, s>>>(prm, own, blocks);
   else if (mode == 1)
-    angular_tc_kernel_batched<1><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
+    angular_tc_kernel_batched<1><<<grid, kThreads, smem, s>>>(prm, own, blocks);
   else
-    angular_tc_kernel_batched<0><<<persistent_grid(blocks), kThreads, smem, s>>>(prm, own, blocks);
+    angular_tc_kernel_batched<0><<<grid, kThreads, smem, s>>>(prm, own, blocks);
   count_launch();
   return cudaGetLastError();
 }
@@ -1571,7 +1588,7 @@ cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_ou
 
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
                               int error_slot, const int* parity, int mode, cudaStream_t s,
-                              unsigned long long* trace) {
+                              unsigned long long* trace, int ctas_per_sm) {
   TcParams tp{};
   tp.trace = trace;
   tp.p = p;
@@ -1589,12 +1606,13 @@ cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, 
                           (const void*)angular_tc_kernel<2>};
   if (!configure_once(kerns[mode], configured[mode])) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
+  const unsigned grid = persistent_grid(p.g.tiles, ctas_per_sm);
   if (mode == 2)
-    angular_tc_kernel<2><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
+    angular_tc_kernel<2><<<grid, kThreads, smem, s>>>(tp);
   else if (mode == 1)
-    angular_tc_kernel<1><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
+    angular_tc_kernel<1><<<grid, kThreads, smem, s>>>(tp);
   else
-    angular_tc_kernel<0><<<persistent_grid(p.g.tiles), kThreads, smem, s>>>(tp);
+    angular_tc_kernel<0><<<grid, kThreads, smem, s>>>(tp);
   count_launch();
   return cudaGetLastError();
 }

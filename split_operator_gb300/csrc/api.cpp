@@ -1018,6 +1018,40 @@ int so_batch_steps_host(so_batch b, const double* const* in, double* const* out,
     b->b->steps_host(in, out, steps);
   });
 }
+int so_batch_tune(so_batch b, const char* cache_path, int trial_steps, char* report, size_t cap) {
+  return guard([&] {
+    need(b, "null argument");
+    const std::string r = b->b->tune(cache_path ? cache_path : "", trial_steps);
+    if (report && cap > 0) std::snprintf(report, cap, "%s", r.c_str());
+  });
+}
 void so_batch_free(so_batch b) { delete b; }
+
+int so_schedules_load(const char* path) {
+  return guard([&] {
+    need(path, "null argument");
+    FILE* f = std::fopen(path, "r");
+    need(f != nullptr, "cannot open the schedule cache", SO_ERR_IO);
+    std::string text;
+    char buf[4096];
+    size_t k;
+    while ((k = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, k);
+    std::fclose(f);
+    need(so::schedules_from_json(text), "the schedule cache is not in the tuner's format");
+  });
+}
+int so_schedules_save(const char* path) {
+  return guard([&] {
+    need(path, "null argument");
+    FILE* f = std::fopen(path, "w");
+    need(f != nullptr, "cannot write the schedule cache", SO_ERR_IO);
+    const std::string js = so::schedules_json();
+    const bool ok = std::fwrite(js.data(), 1, js.size(), f) == js.size();
+    need(std::fclose(f) == 0 && ok, "cannot write the schedule cache", SO_ERR_IO);
+  });
+}
+int so_schedules_reset(void) {
+  return guard([&] { so::reset_schedules(); });
+}
 
 }  // extern "C"

@@ -14,6 +14,7 @@
 #pragma once
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <vector>
 #include <cuda_runtime.h>
 
@@ -87,6 +88,7 @@ struct PassParams {
   int32_t one_buffer;           // 1: no op needs the second tile buffer (FFT stages run in place)
   int32_t sweep;                // 1: only point-wise ops, norms, scalars and power-of-two FFTs
   int32_t fused;                // 1: an FFT pair with point-wise ops, run by fft_pair_kernel
+  int32_t radix;                // fused: radix of the Stockham stages (16 or 8; the twiddle table's order)
   DevOp ops[kMaxOps];
 };
 
@@ -141,11 +143,31 @@ __host__ __device__ inline bool twiddles_in_smem(const Geometry& g) {
   return !(stage_twiddles(g.n) && g.lanes_per_tile < 4);
 }
 
+// Launch schedules (schedule.cpp), per lane extent n; 0 fields mean the built-in default.
+// FFT-pair pass: threads per CTA (128, 256 or 512; lanes per tile = 16 threads / n) and the
+// radix of its Stockham stages (16 or 8).  Tensor-core pass: persistent CTAs per SM (1 or 2)
+// and the batched tile order (0 strided, 1 one run of consecutive tiles per CTA).
+struct PairSchedule {
+  int threads, radix;
+};
+struct TcSchedule {
+  int ctas_per_sm, blocked;
+};
+PairSchedule pair_schedule(int64_t n, bool fp64);
+TcSchedule tc_schedule(int64_t n, int mode);
+void set_pair_schedule(int64_t n, bool fp64, PairSchedule s);
+void set_tc_schedule(int64_t n, int mode, TcSchedule s);
+void reset_schedules();
+uint64_t schedule_epoch();  // changes whenever a schedule does
+std::string schedules_json();
+bool schedules_from_json(const std::string& text);
+
 // FFT pair pass (lane_sweep.cu): [FFT] [DIAG1D along / DIAGND]* [FFT] [DIAG1D along / DIAGND]*
 // over contiguous power-of-two FP32 lanes, every thread holding 16 values in registers.
 // fft_pair_plan checks the pass and sets its tiling (lanes per tile, tiles) and p.fused.
 bool fft_pair_plan(PassParams& p, bool fp64, bool resident);
-int fft_pair_threads(const Geometry& g);
+int fft_pair_threads(const Geometry& g);  // the default threads per CTA
+int fft_pair_block(const Geometry& g);    // threads per CTA of a planned pass (lanes per tile x n / 16)
 
 // Host launchers (lane_sweep.cu)
 cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);
@@ -171,7 +193,7 @@ void angular_tc_parity_images(const double* m, int n, int kind, int mode, std::v
 // per-tile phase timestamps (angular_tc_trace_slots() per tile), nullptr: off
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
                               int error_slot, const int* parity, int mode, cudaStream_t s,
-                              unsigned long long* trace = nullptr);
+                              unsigned long long* trace = nullptr, int ctas_per_sm = 0);
 int angular_tc_trace_slots();
 // one CTA waits (limit_ns, both wait forms) on an mbarrier nothing completes; out[3]:
 // timed out (try_wait form), timed out (polling form), elapsed ns
@@ -180,14 +202,17 @@ cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_ou
 // Batched launches over many propagations' passes (block -> (instance, tile) by offsets)
 cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassParams* params_dev,
                                 const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
-                                cudaStream_t s);
+                                cudaStream_t s, int radix = 0);
 size_t tc_params_bytes();
 void tc_params_set_trace(void* params, unsigned long long* trace);  // the TcParams' trace field
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
                     const int* parity, void* out);
+// persistent CTAs a launch of `tiles` tensor-core tiles runs on (CTA k takes the tiles at
+// positions k, k + grid, k + 2 grid, ... of the owners table)
+int64_t angular_tc_grid(int64_t tiles, int ctas_per_sm = 0);
 // owners_dev: blocks pairs (pass index, tile within the pass), uint32 each, in global tile order
 cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners_dev, int64_t blocks, size_t smem,
-                                      int mode, cudaStream_t s);
+                                      int mode, cudaStream_t s, int ctas_per_sm = 0);
 
 // Auxiliary kernels (aux_kernels.cu)
 cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);

@@ -900,6 +900,11 @@ __global__ void __launch_bounds__(512, 2) fft_pair_kernel(const __grid_constant_
   fft_pair_tile<float, 16>(p, blockIdx.x);
 }
 
+// FP32 with radix-8 stages (one more stage than radix 16, fewer registers per butterfly)
+__global__ void __launch_bounds__(512, 2) fft_pair_kernel_r8(const __grid_constant__ PassParams p) {
+  fft_pair_tile<float, 8>(p, blockIdx.x);
+}
+
 // FP64 lanes of 8192 points (one lane of 16 values per thread for 512 threads: one CTA per
 // SM, whose 139 KB lane buffer leaves no room for a second)
 __global__ void __launch_bounds__(512, 1) fft_pair_kernel_f64(const __grid_constant__ PassParams p) {
@@ -935,7 +940,14 @@ __global__ void __launch_bounds__(512, 1) fft_pair_kernel_batched_f64(const Pass
   fft_pair_batched_tile<double, 8>(params, offsets, count);
 }
 
+__global__ void __launch_bounds__(512, 2) fft_pair_kernel_batched_r8(const PassParams* __restrict__ params,
+                                                                     const int64_t* __restrict__ offsets, int count) {
+  fft_pair_batched_tile<float, 8>(params, offsets, count);
+}
+
 int fft_pair_threads(const Geometry& g) { return g.n >= 8192 ? 512 : 256; }
+
+int fft_pair_block(const Geometry& g) { return (int)((int64_t)g.lanes_per_tile * g.n / kPairV); }
 
 bool fft_pair_plan(PassParams& p, bool fp64, bool resident) {
   Geometry& g = p.g;
@@ -956,12 +968,19 @@ bool fft_pair_plan(PassParams& p, bool fp64, bool resident) {
     }
   }
   if (ffts != 2) return false;
-  const int T = fft_pair_threads(g);
+  // the tuned schedule when it is valid for this lane: T threads hold kPairV values each, so
+  // a tile is L = kPairV T / n >= 1 whole lanes; FP64 stays at radix 8 (its table's order)
+  const PairSchedule sc = pair_schedule(g.n, fp64);
+  int T = fft_pair_threads(g);
+  if ((sc.threads == 128 || sc.threads == 256 || sc.threads == 512) && (int64_t)kPairV * sc.threads >= g.n &&
+      !(fp64 && sc.threads != 512))
+    T = sc.threads;
   const int64_t L = (int64_t)kPairV * T / g.n;
   g.lanes_per_tile = (int32_t)L;
   g.tiles_per_outer = 1;
   g.tiles = (g.outer + L - 1) / L;
   p.fused = 1;
+  p.radix = fp64 ? 8 : (sc.radix == 8 ? 8 : 16);
   return true;
 }
 
@@ -1015,18 +1034,22 @@ static cudaError_t launch_batched_impl(const PassParams* params_dev, const int64
 
 cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassParams* params_dev,
                                 const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
-                                cudaStream_t s) {
+                                cudaStream_t s, int radix) {
   if (fused) {
     if (smem > 220 * 1024 || threads > 512) return cudaErrorInvalidValue;
-    static bool configured[2] = {false, false};
-    const void* kern = fp64 ? (const void*)fft_pair_kernel_batched_f64 : (const void*)fft_pair_kernel_batched;
-    if (!configured[fp64 ? 1 : 0]) {
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    static bool configured[3] = {false, false, false};
+    const int which = fp64 ? 1 : (radix == 8 ? 2 : 0);
+    const void* kerns[3] = {(const void*)fft_pair_kernel_batched, (const void*)fft_pair_kernel_batched_f64,
+                            (const void*)fft_pair_kernel_batched_r8};
+    if (!configured[which]) {
+      cudaError_t e = cudaFuncSetAttribute(kerns[which], cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       if (e != cudaSuccess) return e;
-      configured[fp64 ? 1 : 0] = true;
+      configured[which] = true;
     }
-    if (fp64)
+    if (which == 1)
       fft_pair_kernel_batched_f64<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
+    else if (which == 2)
+      fft_pair_kernel_batched_r8<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
     else
       fft_pair_kernel_batched<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
     count_launch();
@@ -1101,7 +1124,7 @@ cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s) {
     }
     const size_t smem = fft_pair_smem(p.g, true);
     if (smem > 220 * 1024) return cudaErrorInvalidValue;
-    fft_pair_kernel_f64<<<(unsigned)p.g.tiles, fft_pair_threads(p.g), smem, s>>>(p);
+    fft_pair_kernel_f64<<<(unsigned)p.g.tiles, fft_pair_block(p.g), smem, s>>>(p);
     count_launch();
     return cudaGetLastError();
   }
@@ -1109,16 +1132,20 @@ cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s) {
 }
 cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s) {
   if (p.fused) {
-    static bool configured = false;
-    if (!configured) {
-      cudaError_t e =
-          cudaFuncSetAttribute(fft_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    static bool configured[2] = {false, false};
+    const bool r8 = p.radix == 8;
+    const void* kern = r8 ? (const void*)fft_pair_kernel_r8 : (const void*)fft_pair_kernel;
+    if (!configured[r8 ? 1 : 0]) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       if (e != cudaSuccess) return e;
-      configured = true;
+      configured[r8 ? 1 : 0] = true;
     }
     const size_t smem = fft_pair_smem(p.g, false);
     if (smem > 220 * 1024) return cudaErrorInvalidValue;
-    fft_pair_kernel<<<(unsigned)p.g.tiles, fft_pair_threads(p.g), smem, s>>>(p);
+    if (r8)
+      fft_pair_kernel_r8<<<(unsigned)p.g.tiles, fft_pair_block(p.g), smem, s>>>(p);
+    else
+      fft_pair_kernel<<<(unsigned)p.g.tiles, fft_pair_block(p.g), smem, s>>>(p);
     count_launch();
     return cudaGetLastError();
   }

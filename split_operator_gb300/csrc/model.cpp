@@ -10,6 +10,7 @@
 #include <cstring>
 #include <mutex>
 #include <numeric>
+#include <tuple>
 
 #include "model.hpp"
 
@@ -421,12 +422,14 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
   std::string name = std::string(kTcNames[tc_mode()]) + (par ? " parity axis" : " axis") +
                      std::to_string(axis) + ":";
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
+  const TcSchedule sched = tc_schedule(g.n, tc_mode());
   if (recording) {
-    // threads: the lane extent, the parity mode and the operand format (one batched launch
-    // serves one of each; the kernel's thread count is fixed)
+    // threads: the lane extent, the parity mode, the operand format and the schedule (CTAs per
+    // SM, tile order): one batched launch serves one of each; the kernel's thread count is fixed
     RecordedPass r{RecordedPass::TensorCore, false, p, std::vector<unsigned char>(tc_params_bytes()),
-                   (int)g.n | (par ? 1 << 16 : 0) | (tc_mode() << 17), angular_tc_smem_bytes((int)g.n, par, tc_mode()),
-                   name, pass_bytes(ops, g)};
+                   (int)g.n | (par ? 1 << 16 : 0) | (tc_mode() << 17) | ((sched.ctas_per_sm & 3) << 20) |
+                       (sched.blocked ? 1 << 22 : 0),
+                   angular_tc_smem_bytes((int)g.n, par, tc_mode()), name, pass_bytes(ops, g)};
     make_tc_params(p, mats, nmat, images, timeout_slot, parity, r.tcp.data());
     recording->push_back(std::move(r));
     return true;
@@ -443,7 +446,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     cuda_check(cudaMemsetAsync(trace.ptr, 0, trace.bytes, stream), "trace clear");
   }
   cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, parity, tc_mode(), stream,
-                               trace_path ? trace.as<unsigned long long>() : nullptr),
+                               trace_path ? trace.as<unsigned long long>() : nullptr, sched.ctas_per_sm),
              "tensor-core pass launch");
   if (trace_path) {
     std::vector<unsigned long long> h(trace.bytes / sizeof(unsigned long long));
@@ -485,8 +488,9 @@ void WaveFunction::set_weights(DevOp& op) {
   }
 }
 
-const void* Engine::twiddle(size_t n) {
-  auto it = twiddles_.find(n);
+const void* Engine::twiddle(size_t n, int radix) {
+  const int rmax = radix ? radix : (fp64 ? 8 : 16);
+  auto it = twiddles_.find({n, rmax});
   if (it != twiddles_.end()) return it->second.ptr;
   DeviceBuffer b;
   std::vector<cplx> tw = twiddles(n);
@@ -494,7 +498,6 @@ const void* Engine::twiddle(size_t n) {
     // the Stockham stages' order (same values, permuted): forward radix order in [0, n),
     // reversed radix order (the FFT pair pass's second transform) in [n, 2n)
     std::vector<cplx> st(2 * n, cplx(0.0, 0.0));
-    const int rmax = fp64 ? 8 : 16;
     for (size_t e = 0; e < n; ++e) {
       st[e] = tw[(size_t)stage_twiddle_exponent((int64_t)e, (int64_t)n, rmax, false)];
       st[n + e] = tw[(size_t)stage_twiddle_exponent((int64_t)e, (int64_t)n, rmax, true)];
@@ -503,7 +506,7 @@ const void* Engine::twiddle(size_t n) {
   }
   upload_complex(b, tw, fp64, stream);
   const void* p = b.ptr;
-  twiddles_.emplace(n, std::move(b));
+  twiddles_.emplace(std::make_pair(n, rmax), std::move(b));
   return p;
 }
 
@@ -564,7 +567,10 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   if (fft) p.twiddle = twiddle((size_t)p.g.n);
   pass_choose_buffers(p, fp64);
   if (!fp64 && tc_mode() >= 0 && !resident && try_launch_tc(ops, axis, p)) return;
-  if ((fft_pair || (fp64 && p.g.n > 4096)) && fft_pair_plan(p, fp64, resident)) name_tag = " fftpair";
+  if ((fft_pair || (fp64 && p.g.n > 4096)) && fft_pair_plan(p, fp64, resident)) {
+    name_tag = p.radix == 8 && !fp64 ? " fftpair r8" : " fftpair";
+    if (p.radix != (fp64 ? 8 : 16)) p.twiddle = twiddle((size_t)p.g.n, p.radix);  // the table in its stage order
+  }
   if (fp64 && p.g.n > 4096 && !p.fused)
     throw Error(SO_ERR_UNSUPPORTED, "FP64 lanes longer than 4096 points are not supported outside FFT-pair passes "
                                     "([FFT] [point-wise] [FFT] [point-wise] on contiguous power-of-two lanes)");
@@ -578,7 +584,9 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
     // fused FFT pairs: bit 16 of the thread count (their own launch group and kernel)
-    const int threads = p.fused ? (fft_pair_threads(p.g) | (1 << 16)) : pass_threads(p.g);
+    // radix-8 FP32 pairs: bit 19 (their own kernel)
+    const int threads =
+        p.fused ? (fft_pair_block(p.g) | (1 << 16) | (p.radix == 8 && !fp64 ? 1 << 19 : 0)) : pass_threads(p.g);
     RecordedPass r{resident ? RecordedPass::Resident : RecordedPass::Generic, fp64, p, {},
                    threads, pass_smem_bytes(p, fp64), name, pass_bytes(ops, p.g)};
     recording->push_back(std::move(r));
@@ -1665,6 +1673,7 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
     g.smem = v[0]->smem;
     g.count = (int)v.size();
     g.name = "batched " + std::to_string(v.size()) + "x " + v[0]->name;
+    g.n = v[0]->p.g.n;
     std::vector<int64_t> off(v.size() + 1, 0);
     const size_t pb = g.kind == RecordedPass::TensorCore ? tc_params_bytes() : sizeof(PassParams);
     std::vector<unsigned char> params(pb * v.size());
@@ -1681,7 +1690,7 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
         if (trace_path) {
           TraceBuf tb;
           tb.tiles = v[i]->p.g.tiles;
-          tb.name = v[i]->name + " member " + std::to_string(i);
+          tb.name = v[i]->name + " n=" + std::to_string(v[i]->p.g.n) + " member " + std::to_string(i);
           tb.buf = DeviceBuffer((size_t)tb.tiles * angular_tc_trace_slots() * sizeof(unsigned long long));
           cuda_check(cudaMemset(tb.buf.ptr, 0, tb.buf.bytes), "trace clear");
           tc_params_set_trace(params.data() + i * pb, tb.buf.as<unsigned long long>());
@@ -1707,6 +1716,20 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
           own[(size_t)t * 2] = (uint32_t)i;
           own[(size_t)t * 2 + 1] = (uint32_t)(t - off[i]);
         }
+      if ((g.threads >> 22) & 1) {
+        // blocked: CTA k (positions k, k + G, k + 2G, ...) takes one run of consecutive tiles,
+        // mostly of one member (one pass description, neighbouring columns)
+        const int64_t G = angular_tc_grid(g.blocks, (g.threads >> 20) & 3), base = g.blocks / G,
+                      rem = g.blocks % G;
+        std::vector<uint32_t> blk(own.size());
+        for (int64_t b = 0; b < g.blocks; ++b) {
+          const int64_t k = b % G, i = b / G;
+          const int64_t t = k * base + std::min(k, rem) + i;
+          blk[(size_t)b * 2] = own[(size_t)t * 2];
+          blk[(size_t)b * 2 + 1] = own[(size_t)t * 2 + 1];
+        }
+        own.swap(blk);
+      }
       g.owners = DeviceBuffer(own.size() * sizeof(uint32_t));
       cuda_check(cudaMemcpy(g.owners.ptr, own.data(), own.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
                  "batch tile owners");
@@ -1722,17 +1745,26 @@ void Batch::run_groups(std::vector<Group>& gs) {
     if (timing_) {
       t.name = g.name;
       t.bytes = g.bytes;
+      if (g.kind == RecordedPass::TensorCore) {
+        t.cls_kind = 1;
+        t.cls_mode = (g.threads >> 17) & 3;
+      } else if ((g.threads >> 16) & 1) {
+        t.cls_kind = 0;
+        t.cls_mode = g.fp64 ? 1 : 0;
+      }
+      t.cls_n = g.n;
       cuda_check(cudaEventCreate(&t.a), "event");
       cuda_check(cudaEventCreate(&t.b), "event");
       cuda_check(cudaEventRecord(t.a, stream_), "event record");
     }
     if (g.kind == RecordedPass::TensorCore)
-      cuda_check(launch_angular_tc_batched(g.params.ptr, g.owners.ptr, g.blocks, g.smem,
-                                           (g.threads >> 17) & 3, stream_),
+      cuda_check(launch_angular_tc_batched(g.params.ptr, g.owners.ptr, g.blocks, g.smem, (g.threads >> 17) & 3,
+                                           stream_, (g.threads >> 20) & 3),
                  "batched tensor-core pass");
     else
       cuda_check(launch_pass_batched(g.fp64, g.sweep, (g.threads >> 16) & 1, g.params.as<PassParams>(),
-                                     g.offsets.as<int64_t>(), g.count, g.blocks, g.threads & 0xffff, g.smem, stream_),
+                                     g.offsets.as<int64_t>(), g.count, g.blocks, g.threads & 0xffff, g.smem, stream_,
+                                     ((g.threads >> 19) & 1) ? 8 : 0),
                  "batched pass");
     if (timing_) {
       cuda_check(cudaEventRecord(t.b, stream_), "event record");
@@ -1793,7 +1825,7 @@ void Batch::steps(uint64_t n, bool wait, bool sync_members) {
       }
   // the launch groups (device parameter blocks) of the last call are reused when every
   // recorded pass has the same parameters: consecutive calls of a steady propagation
-  bool reuse = cached_rec_.size() == rec.size();
+  bool reuse = cached_rec_.size() == rec.size() && cached_epoch_ == schedule_epoch();
   for (size_t i = 0; reuse && i < rec.size(); ++i) {
     reuse = cached_rec_[i].size() == rec[i].size();
     for (size_t j = 0; reuse && j < rec[i].size(); ++j) reuse = same_params(rec[i][j], cached_rec_[i][j]);
@@ -1803,6 +1835,7 @@ void Batch::steps(uint64_t n, bool wait, bool sync_members) {
     cached_pos_.resize(np);
     for (size_t i = 0; i < np; ++i) cached_pos_[i] = build_groups(rec, i);
     cached_rec_ = std::move(rec);
+    cached_epoch_ = schedule_epoch();
   }
   std::vector<std::vector<Group>>& pos = cached_pos_;
   t_groups = ms();
@@ -1968,6 +2001,102 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
     for (const auto& mk : marks) line += " " + mk.first + " " + std::to_string(mk.second) + " ms;";
     std::fprintf(stderr, "%s\n", line.c_str());
   }
+}
+
+std::string Batch::tune(const std::string& cache_path, int trial_steps) {
+  if (trial_steps < 1) throw Error(SO_ERR_INVALID, "tuning needs at least one step per candidate");
+  // the schedule classes present: (kind, n, mode) from one recorded step pair of every member
+  std::map<std::tuple<int, int64_t, int>, std::vector<std::pair<int, int>>> cands;
+  for (Propagation* p : props_)
+    for (const RecordedPass& r : p->record_steps(2)) {
+      if (r.kind == RecordedPass::TensorCore) {
+        const int mode = (r.threads >> 17) & 3;
+        // (CTAs per SM, blocked order); the first candidate is the built-in default
+        cands[{1, r.p.g.n, mode}] = {{2, 0}, {2, 1}, {1, 0}, {1, 1}};
+      } else if (r.kind == RecordedPass::Generic && r.p.fused && !r.fp64) {
+        // (threads per CTA, radix); lanes of n points need 16 threads >= n
+        std::vector<std::pair<int, int>> v{{fft_pair_threads(r.p.g), 16}};
+        for (int t : {128, 256, 512})
+          for (int rd : {16, 8})
+            if ((int64_t)16 * t >= r.p.g.n && !(t == v[0].first && rd == 16)) v.push_back({t, rd});
+        cands[{0, r.p.g.n, 0}] = v;
+      }
+    }
+  if (cands.empty()) throw Error(SO_ERR_UNSUPPORTED, "the batch has no FFT-pair or tensor-core passes to tune");
+  size_t trials = 0;
+  for (const auto& kv : cands) trials = std::max(trials, kv.second.size());
+  // the members' states, restored once the trials are done
+  std::vector<std::vector<unsigned char>> saved;
+  for (Propagation* p : props_) saved.push_back(p->checkpoint());
+  std::map<std::tuple<int, int64_t, int>, std::vector<double>> ms;  // per class, per candidate
+  const bool timing_was = timing_;
+  auto apply = [&](const std::tuple<int, int64_t, int>& k, std::pair<int, int> c) {
+    if (std::get<0>(k) == 1)
+      set_tc_schedule(std::get<1>(k), std::get<2>(k), TcSchedule{c.first, c.second});
+    else
+      set_pair_schedule(std::get<1>(k), false, PairSchedule{c.first, c.second});
+  };
+  try {
+    for (size_t t = 0; t < trials; ++t) {
+      for (const auto& kv : cands) apply(kv.first, kv.second[t % kv.second.size()]);
+      timing_ = true;
+      timed_.clear();
+      steps(1);  // the new launch shapes are built and warm
+      kernel_times();
+      steps((uint64_t)trial_steps);
+      cuda_check(cudaStreamSynchronize(stream_), "batch sync");
+      std::map<std::tuple<int, int64_t, int>, double> acc;
+      for (Timed& tm : timed_) {
+        float e = 0.f;
+        cuda_check(cudaEventElapsedTime(&e, tm.a, tm.b), "event elapsed");
+        if (tm.cls_kind >= 0) acc[{tm.cls_kind, tm.cls_n, tm.cls_mode}] += e;
+        cudaEventDestroy(tm.a);
+        cudaEventDestroy(tm.b);
+      }
+      timed_.clear();
+      for (const auto& kv : cands)
+        if (t < kv.second.size()) ms[kv.first].push_back(acc[kv.first]);
+    }
+  } catch (...) {
+    timing_ = timing_was;
+    for (size_t i = 0; i < props_.size(); ++i) props_[i]->restore(saved[i].data(), saved[i].size());
+    throw;
+  }
+  timing_ = timing_was;
+  // winners, and the report
+  std::string rep = "{\"trial_steps\": " + std::to_string(trial_steps) + ", \"classes\": [";
+  double def_total = 0.0, best_total = 0.0;
+  bool first = true;
+  for (const auto& kv : cands) {
+    const std::vector<double>& v = ms[kv.first];
+    size_t best = 0;
+    for (size_t i = 1; i < v.size(); ++i)
+      if (v[i] < v[best]) best = i;
+    apply(kv.first, kv.second[best]);
+    def_total += v[0];
+    best_total += v[best];
+    const bool tc = std::get<0>(kv.first) == 1;
+    rep += std::string(first ? "" : ", ") + "{\"pass\": \"" + (tc ? "tensor_core" : "fft_pair") +
+           "\", \"n\": " + std::to_string(std::get<1>(kv.first)) + ", \"mode\": " +
+           std::to_string(std::get<2>(kv.first)) + ", \"candidates\": [";
+    for (size_t i = 0; i < v.size(); ++i)
+      rep += std::string(i ? ", " : "") + "{\"" + (tc ? "ctas_per_sm" : "threads") + "\": " +
+             std::to_string(kv.second[i].first) + ", \"" + (tc ? "blocked" : "radix") + "\": " +
+             std::to_string(kv.second[i].second) + ", \"ms\": " + std::to_string(v[i]) + "}";
+    rep += "], \"chosen\": " + std::to_string(best) + "}";
+    first = false;
+  }
+  rep += "], \"default_ms\": " + std::to_string(def_total) + ", \"tuned_ms\": " + std::to_string(best_total) +
+         ", \"schedules\": " + schedules_json() + "}";
+  for (size_t i = 0; i < props_.size(); ++i) props_[i]->restore(saved[i].data(), saved[i].size());
+  if (!cache_path.empty()) {
+    FILE* f = std::fopen(cache_path.c_str(), "w");
+    if (!f) throw Error(SO_ERR_IO, "cannot write the schedule cache " + cache_path);
+    const std::string js = schedules_json();
+    const bool ok = std::fwrite(js.data(), 1, js.size(), f) == js.size();
+    if (std::fclose(f) != 0 || !ok) throw Error(SO_ERR_IO, "cannot write the schedule cache " + cache_path);
+  }
+  return rep;
 }
 
 std::string Batch::kernel_times() {

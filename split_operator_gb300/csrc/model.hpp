@@ -151,7 +151,7 @@ class Engine {
   const void* matrices(const void* key, uint64_t version, const std::vector<cplx>& m, size_t n, size_t count,
                        bool& real);
   const double* weights(const Grid& g);
-  const void* twiddle(size_t n);
+  const void* twiddle(size_t n, int radix = 0);  // radix 0: the precision's default stage order
 
   // pass building
   void submit(const Action& a);
@@ -212,7 +212,7 @@ class Engine {
   static void shared_tc_images(const std::vector<double>& md, int n, int mode, cudaStream_t s,
                                std::shared_ptr<DeviceBuffer>& img, std::shared_ptr<DeviceBuffer>& par, int& kind);
   std::map<uint64_t, DeviceBuffer> weights_;
-  std::map<size_t, DeviceBuffer> twiddles_;
+  std::map<std::pair<size_t, int>, DeviceBuffer> twiddles_;  // by (n, stage radix)
   // open pass
   std::vector<DevOp> cur_;
   int cur_axis_ = -1;
@@ -486,9 +486,11 @@ class Batch {
     DeviceBuffer owners;  // tensor-core groups: (pass index, tile within the pass) per global tile
     std::string name;
     double bytes;
+    int64_t n = 0;  // lane extent of the members' passes (the schedule class)
   };
   std::vector<Group> build_groups(const std::vector<std::vector<RecordedPass>>& rec, size_t pos);
   std::vector<std::vector<RecordedPass>> cached_rec_;  // the passes the cached groups were built from
+  uint64_t cached_epoch_ = 0;                          // the launch schedules they were built with
   std::vector<std::vector<Group>> cached_pos_;
   struct Chunk {
     size_t first = 0, count = 0;
@@ -514,8 +516,19 @@ class Batch {
     std::string name;
     cudaEvent_t a, b;
     double bytes;
+    int cls_kind = -1;  // 0 FFT-pair pass, 1 tensor-core pass, -1 other
+    int64_t cls_n = 0;
+    int cls_mode = 0;   // FFT pair: 1 for FP64; tensor core: operand mode
   };
   std::vector<Timed> timed_;
+
+ public:
+  // Autotuner: times the candidate launch schedules of every lane extent of the batch's FFT-pair
+  // and tensor-core passes on the live workload (CUDA events, `trial_steps` steps per
+  // candidate), keeps the fastest per extent in the process-wide schedule table, writes the
+  // table to `cache_path` (JSON; empty: no file) and restores every member's state.
+  // Returns a JSON report: per extent, each candidate's milliseconds and the one chosen.
+  std::string tune(const std::string& cache_path, int trial_steps);
 };
 
 }  // namespace so

@@ -217,6 +217,26 @@ __device__ __forceinline__ void tmem_ld16x3(uint32_t taddr, uint32_t step, float
   }
 }
 
+// the same with 8 columns per region
+__device__ __forceinline__ void tmem_ld8x3(uint32_t taddr, uint32_t step, float* v0, float* v1, float* v2) {
+  uint32_t r[24];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(r[8 * k + 0]), "=r"(r[8 * k + 1]), "=r"(r[8 * k + 2]), "=r"(r[8 * k + 3]), "=r"(r[8 * k + 4]),
+          "=r"(r[8 * k + 5]), "=r"(r[8 * k + 6]), "=r"(r[8 * k + 7])
+        : "r"(taddr + (uint32_t)k * step)
+        : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    v0[i] = __uint_as_float(r[i]);
+    v1[i] = __uint_as_float(r[8 + i]);
+    v2[i] = __uint_as_float(r[16 + i]);
+  }
+}
+
 __device__ __forceinline__ float round_tf32(float x) {
   return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
