@@ -1,10 +1,11 @@
 // Multilayer perceptron for learned starting states of imaginary-time relaxation
 // (no counterpart in the reference crate).  Hand-written CUDA kernels:
 //   forward   Z = X W^T + b, tanh on hidden layers (BF16 weights, FP32 accumulate)
-//   backward  dW = dZ^T X, db = column sums of dZ, dX = dZ W  (FP32)
+//   backward  dW = dZ^T X, db = column sums of dZ, dX = dZ W
 //   Adam      on FP32 master weights, then a BF16 copy for the next forward pass
-// Every output element is summed by one thread in a fixed order, so training is
-// deterministic for a given launch configuration.
+// The three products run on the tensor cores (tcgen05.mma kind::f16, accumulators in
+// TMEM) with FP32 activations and gradients split into two BF16 parts.  Every product and
+// sum runs in a fixed order, so training is deterministic.
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -16,6 +17,7 @@
 
 #include "../../include/split_operator.h"
 #include "common.cuh"
+#include "tc_common.cuh"
 
 namespace so {
 
@@ -34,61 +36,128 @@ __device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 v) {
   return __bfloat162float(v);
 }
 
-// C[m][n] (+)= sum_k A(m, k) B(k, n); A(m,k) = TA ? A[k*lda+m] : A[m*lda+k], B(k,n) = TB ? B[n*ldb+k] : B[k*ldb+n]
-constexpr int kTile = 64, kTk = 16;
-template <typename TAt, typename TBt, bool TA, bool TB>
-__global__ void __launch_bounds__(256) gemm_kernel(int M, int N, int K, const TAt* __restrict__ A, int lda,
-                                                  const TBt* __restrict__ B, int ldb, float* __restrict__ C, int ldc,
-                                                  int accumulate) {
-  __shared__ float As[kTk][kTile + 1];
-  __shared__ float Bs[kTk][kTile + 1];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int m0 = blockIdx.y * kTile, n0 = blockIdx.x * kTile;
-  float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += kTk) {
-    for (int e = threadIdx.x; e < kTk * kTile; e += 256) {
-      const int kk = e / kTile, mm = e % kTile;
-      const int m = m0 + mm, k = k0 + kk;
-      float a = 0.f;
-      if (m < M && k < K) a = to_f(TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]);
-      As[kk][mm] = a;
-      const int n = n0 + mm;
-      float b = 0.f;
-      if (n < N && k < K) b = to_f(TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n]);
-      Bs[kk][mm] = b;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < kTk; ++kk) {
-      float a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        a[i] = As[kk][ty * 4 + i];
-        b[i] = Bs[kk][tx * 4 + i];
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int m = m0 + ty * 4 + i, n = n0 + tx * 4 + j;
-      if (m < M && n < N) {
-        float* c = C + (size_t)m * ldc + n;
-        *c = accumulate ? *c + acc[i][j] : acc[i][j];
-      }
-    }
+// ---- tensor-core GEMM (tcgen05.mma kind::f16, BF16 operands, FP32 accumulation in TMEM)
+// C[m][n] = sum_k A(m, k) B(n, k) over a 128 x 128 tile per CTA, K in chunks of 16.  The
+// 128 threads stage each chunk into shared memory in the K-major core-matrix layout (8 rows
+// x 16 bytes per core matrix, K core matrices 128 B apart, row groups 256 B apart), which
+// also does the transposes the backward products need (A and B are read through strides).
+// FP32 operands are split x = bf16(x) + bf16(x - bf16(x)) (16 significant bits together);
+// the BF16 weights are exact as they are.  Products: hi hi + lo hi (B exact) or
+// hi hi + hi lo + lo hi (both split); the remaining lo lo term is 2^-16 of the result.
+// Two shared-memory stages: thread 0 issues a chunk's MMAs and commits them to the stage's
+// mbarrier, which the threads wait on (bounded) before they overwrite that stage.
+constexpr int kGm = 128, kGn = 128, kGk = 16;
+constexpr uint32_t kGStage = 4u * kGm * kGk * 2u;  // A hi, A lo, B hi, B lo: 4 KB each
+constexpr uint64_t kGWait = 2000000000ull;         // 2 s
+
+struct GemmOperand {
+  const void* p;
+  int64_t s_row, s_k;  // element strides: A(m, k) = p[m s_row + k s_k] (B(n, k) likewise)
+  int bf16;            // 1: BF16 values (used as they are); 0: FP32 (split into hi + lo)
+};
+
+// byte offset of element (row r, k) in a 128 x 16 chunk image
+__device__ __forceinline__ uint32_t gemm_off(int r, int k) {
+  return (uint32_t)(r >> 3) * 256u + (uint32_t)(k >> 3) * 128u + (uint32_t)(r & 7) * 16u + (uint32_t)(k & 7) * 2u;
 }
 
-template <typename TAt, typename TBt, bool TA, bool TB>
-void gemm(int M, int N, int K, const TAt* A, int lda, const TBt* B, int ldb, float* C, int ldc, cudaStream_t s) {
-  dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
-  gemm_kernel<TAt, TBt, TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, 0);
+// row r of a chunk (16 K values) of one operand into its hi / lo images
+__device__ __forceinline__ void gemm_stage_row(const GemmOperand& o, int64_t row, int64_t rows, int64_t k0, int K,
+                                               int r, unsigned char* hi, unsigned char* lo) {
+  uint32_t h[8], l[8];
+#pragma unroll
+  for (int k = 0; k < kGk; ++k) {
+    float x = 0.0f;
+    if (row < rows && k0 + k < K) {
+      const int64_t e = row * o.s_row + (k0 + k) * o.s_k;
+      x = o.bf16 ? __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(o.p)[e])
+                 : reinterpret_cast<const float*>(o.p)[e];
+    }
+    uint16_t xh, xl;
+    tc::split_bf16(x, xh, xl);  // exact for a BF16 value: xl = 0
+    if (k & 1) {
+      h[k >> 1] |= (uint32_t)xh << 16;
+      l[k >> 1] |= (uint32_t)xl << 16;
+    } else {
+      h[k >> 1] = xh;
+      l[k >> 1] = xl;
+    }
+  }
+  // two 16-byte core-matrix rows (K 0-7 and 8-15) per image
+  *reinterpret_cast<uint4*>(hi + gemm_off(r, 0)) = make_uint4(h[0], h[1], h[2], h[3]);
+  *reinterpret_cast<uint4*>(hi + gemm_off(r, 8)) = make_uint4(h[4], h[5], h[6], h[7]);
+  *reinterpret_cast<uint4*>(lo + gemm_off(r, 0)) = make_uint4(l[0], l[1], l[2], l[3]);
+  *reinterpret_cast<uint4*>(lo + gemm_off(r, 8)) = make_uint4(l[4], l[5], l[6], l[7]);
+}
+
+__global__ void __launch_bounds__(128) tc_gemm_kernel(int M, int N, int K, GemmOperand A, GemmOperand B,
+                                                      float* __restrict__ C, int64_t ldc, int* err) {
+  using namespace tc;
+  __shared__ __align__(1024) unsigned char sm[2 * kGStage];
+  __shared__ __align__(8) uint64_t done[3];  // per stage: its MMAs completed; [2]: all MMAs
+  __shared__ uint32_t tmem_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t m0 = (int64_t)blockIdx.y * kGm, n0 = (int64_t)blockIdx.x * kGn;
+  if (tid == 0) {
+    for (int i = 0; i < 3; ++i) mbar_init(&done[i], 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(&tmem_s, kGn);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_s;
+  const uint32_t idesc = idesc_bf16(kGm, kGn);
+  const bool bsplit = !B.bf16, asplit = !A.bf16;
+  const int nk = (K + kGk - 1) / kGk;
+  bool ok = true;
+  for (int c = 0; c < nk; ++c) {
+    const int s = c & 1;
+    unsigned char* st = sm + (uint32_t)s * kGStage;
+    // the MMAs that read this stage two chunks ago have completed
+    if (c >= 2) ok = ok && mbar_wait(&done[s], (uint32_t)((c / 2 - 1) & 1), kGWait);
+    gemm_stage_row(A, m0 + tid, M, (int64_t)c * kGk, K, tid, st, st + 4096);
+    gemm_stage_row(B, n0 + tid, N, (int64_t)c * kGk, K, tid, st + 8192, st + 12288);
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t a = smem_u32(st);
+      const uint64_t ah = smem_desc_at(smem_desc_bits(128, 256), a), al = smem_desc_at(smem_desc_bits(128, 256), a + 4096);
+      const uint64_t bh = smem_desc_at(smem_desc_bits(128, 256), a + 8192),
+                     bl = smem_desc_at(smem_desc_bits(128, 256), a + 12288);
+      mma_bf16(tmem, ah, bh, idesc, c > 0 ? 1u : 0u);
+      if (asplit) mma_bf16(tmem, al, bh, idesc, 1u);
+      if (bsplit) mma_bf16(tmem, ah, bl, idesc, 1u);
+      mma_commit(&done[s]);
+    }
+  }
+  if (tid == 0) mma_commit(&done[2]);
+  ok = mbar_wait(&done[2], 0u, kGWait) && ok;
+  tc_fence_after();
+  if (!__syncthreads_and(ok)) {
+    if (tid == 0) atomicExch(err, 1);
+  } else {
+    // TMEM lane = row m0 + 32 warp + lane, 32 columns per load
+    const int64_t m = m0 + 32 * warp + lane;
+    for (int cb = 0; cb < kGn; cb += 32) {
+      float v[32];
+      tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)cb, v);
+      if (m < M)
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (n0 + cb + j < N) C[m * ldc + n0 + cb + j] = v[j];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, kGn);
+}
+
+// C (M x N, row stride ldc) = A B^T through the tensor-core kernel
+void tc_gemm(int M, int N, int K, GemmOperand A, GemmOperand B, float* C, int64_t ldc, int* err, cudaStream_t s) {
+  dim3 grid((N + kGn - 1) / kGn, (M + kGm - 1) / kGm);
+  tc_gemm_kernel<<<grid, 128, 0, s>>>(M, N, K, A, B, C, ldc, err);
   count_launch();
 }
 
@@ -190,6 +259,7 @@ struct Mlp {
   std::vector<DBuf<float>> act, grad;  // per layer output (activations) and its gradient
   DBuf<float> x, target;
   DBuf<double> partial;
+  DBuf<int> err;  // set by a tensor-core product whose bounded wait gave up
   int cap = 0;
   int64_t t = 0;  // Adam step
   cudaStream_t s = nullptr;
@@ -206,6 +276,18 @@ struct Mlp {
       grad[l].alloc((size_t)batch * layers[l]->out);
     }
     partial.alloc(4096);
+    if (!err.p) err.alloc(1);
+  }
+
+  // a bounded wait inside a tensor-core product gave up: report it (and clear the flag)
+  void check_err() {
+    int e = 0;
+    check(cudaMemcpyAsync(&e, err.p, sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    check(cudaStreamSynchronize(s), "sync");
+    if (e) {
+      check(cudaMemsetAsync(err.p, 0, sizeof(int), s), "memset");
+      throw std::runtime_error("a tensor-core product's bounded wait gave up");
+    }
   }
 
   void refresh_bf16() {
@@ -220,7 +302,9 @@ struct Mlp {
     const float* in = x.p;
     for (size_t l = 0; l < layers.size(); ++l) {
       Layer& L = *layers[l];
-      gemm<float, __nv_bfloat16, false, true>(batch, L.out, L.in, in, L.in, L.W16.p, L.in, act[l].p, L.out, s);
+      // Z[b][o] = sum_i X[b][i] W[o][i]
+      tc_gemm(batch, L.out, L.in, GemmOperand{in, L.in, 1, 0}, GemmOperand{L.W16.p, L.in, 1, 1}, act[l].p, L.out,
+              err.p, s);
       const int hidden = l + 1 < layers.size();
       bias_act_kernel<<<grid_for((int64_t)batch * L.out), 256, 0, s>>>(act[l].p, L.b.p, batch, L.out, hidden);
       count_launch();
@@ -243,18 +327,20 @@ struct Mlp {
       }
       const float* in = l == 0 ? x.p : act[l - 1].p;
       // dW[o][i] = sum_b dZ[b][o] X[b][i]
-      gemm<float, float, true, false>(L.out, L.in, batch, grad[l].p, L.out, in, L.in, L.gW.p, L.in, s);
+      tc_gemm(L.out, L.in, batch, GemmOperand{grad[l].p, 1, L.out, 0}, GemmOperand{in, 1, L.in, 0}, L.gW.p, L.in,
+              err.p, s);
       colsum_kernel<<<(L.out + 127) / 128, 128, 0, s>>>(grad[l].p, L.gb.p, batch, L.out);
       count_launch();
       if (l > 0) {
         // dX[b][i] = sum_o dZ[b][o] W[o][i]
-        gemm<float, __nv_bfloat16, false, false>(batch, L.in, L.out, grad[l].p, L.out, L.W16.p, L.in,
-                                                 grad[l - 1].p, L.in, s);
+        tc_gemm(batch, L.in, L.out, GemmOperand{grad[l].p, L.out, 1, 0}, GemmOperand{L.W16.p, 1, L.in, 1},
+                grad[l - 1].p, L.in, err.p, s);
       }
     }
     std::vector<double> h(gb);
     check(cudaMemcpyAsync(h.data(), partial.p, gb * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
     check(cudaStreamSynchronize(s), "sync");
+    check_err();
     double loss = 0.0;
     for (double v : h) loss += v;
     return loss / (double)nout;
@@ -375,6 +461,7 @@ int so_mlp_forward(so_mlp h, const float* x, size_t batch, float* y) {
     m.ensure((int)batch);
     so::check(cudaMemcpy(m.x.p, x, batch * m.w[0] * 4, cudaMemcpyHostToDevice), "copy");
     m.forward((int)batch);
+    m.check_err();
     so::check(cudaMemcpy(y, m.act.back().p, batch * m.w.back() * 4, cudaMemcpyDeviceToHost), "copy");
   });
 }

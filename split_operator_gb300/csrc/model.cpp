@@ -1655,13 +1655,15 @@ Batch::~Batch() {
 }
 
 std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<RecordedPass>>& rec, size_t pos) {
-  // group key: kind, precision, threads, shared memory
-  std::map<std::tuple<int, int, int, size_t>, std::vector<const RecordedPass*>> by;
+  // group key: kind, precision, threads, shared memory; FFT-pair passes also by lane extent
+  // (each extent has its own launch schedule, and the tuner times each extent's launches)
+  std::map<std::tuple<int, int, int, size_t, int64_t>, std::vector<const RecordedPass*>> by;
   for (const auto& r : rec) {
     const RecordedPass& rp = r[pos];
     if (rp.kind == RecordedPass::Scalar || rp.kind == RecordedPass::Resident)
       throw Error(SO_ERR_UNSUPPORTED, "pass kind cannot be batched");
-    by[{(int)rp.kind, rp.fp64 ? 1 : 0, rp.threads, rp.smem}].push_back(&rp);
+    const int64_t ext = (rp.kind == RecordedPass::Generic && rp.p.fused) ? rp.p.g.n : 0;
+    by[{(int)rp.kind, rp.fp64 ? 1 : 0, rp.threads, rp.smem, ext}].push_back(&rp);
   }
   std::vector<Group> out;
   for (auto& kv : by) {
