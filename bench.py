@@ -7,7 +7,8 @@ propagations of uneven sizes -- Nr drawn from {512..8192}, Ntheta from
 Morse D(1-e^{-a(r-re)})^2 + beta e^{-r/2} P2(cos th) with D, a, re, beta seeded per
 instance, mass 1000, dt = 0.5, border damping with a loss checker, stack
 [Damp, V/2, Legendre, Rot/2, FFT, K] -- stepped together by the batched executor
-(FP32 state, 3xTF32 tensor-core Legendre transforms, FP64 norms and loss).  The
+(FP32 state, split-BF16x6 tensor-core Legendre transforms -- three fixed-point bf16 slices
+per operand, exact FP32 sums -- FP64 norm folds and loss).  The
 states and tables (~4.2 GB) are far larger than L2, so no flush is needed.
 One bench step = one split-operator time step of all 512 instances.
 
@@ -39,7 +40,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch", choices=["batch", "single"])
     ap.add_argument("--instances", type=int, default=512)
-    ap.add_argument("--precision", default="fp32_tf32x3",
+    ap.add_argument("--precision", default="fp32_bf16x6",
                     choices=["fp64", "fp32_tf32x3", "fp32_bf16x3", "fp32_bf16x6", "fp32_simt"])
     ap.add_argument("--nr", type=int, default=4096)
     ap.add_argument("--nth", type=int, default=128)

@@ -180,9 +180,12 @@ class RadialBasis:
     sampled in the well's scaled coordinate xi (well_frame) on a fixed grid, so that the
     basis describes the shape of a ground state rather than its position and width."""
 
-    def __init__(self, states, params, g: Grid2D, modes=64, nxi=1024, xi_max=10.0):
+    def __init__(self, states, params, g: Grid2D, modes=64, nxi=1024, xi_max=10.0, u=None):
         self.modes, self.g = modes, g
         self.xi = np.linspace(-xi_max, xi_max, nxi)
+        if u is not None:  # a saved basis
+            self.u = np.asarray(u, dtype=np.float64)
+            return
         psil = np.stack([self.to_xi(g.to_l(s.astype(np.float64)), p) for s, p in zip(states, params)])
         self.u = np.empty((g.nth, nxi, modes))
         for l in range(g.nth):
@@ -256,6 +259,29 @@ class LearnedStart:
         coef = y * self.std + self.mean
         return [self.basis.state(c.reshape(self.basis.g.nth, self.basis.modes), p) for c, p in zip(coef, params)]
 
+    def save(self, path):
+        """The trained network (FP32 master parameters), its target scaling and the radial
+        basis (float32), with the grid they belong to, as one .npz file."""
+        g, b = self.basis.g, self.basis
+        np.savez_compressed(path, params=self.net.get_params(), widths=np.array(self.net.widths),
+                            mean=self.mean, std=self.std, u=b.u.astype(np.float32), xi=b.xi,
+                            grid=np.array([g.nr, g.nth, g.r_min, g.r_max]), modes=b.modes,
+                            features=int(self.inputs is physics_features), scaling=self.scaling)
+
+    @staticmethod
+    def load(path):
+        z = np.load(path, allow_pickle=False)
+        nr, nth, r_min, r_max = z["grid"]
+        g = Grid2D(int(nr), int(nth), float(r_min), float(r_max))
+        xi = z["xi"]
+        basis = RadialBasis(None, None, g, modes=int(z["modes"]), nxi=len(xi), xi_max=float(xi[-1]), u=z["u"])
+        widths = [int(w) for w in z["widths"]]
+        model = LearnedStart(basis, hidden=tuple(widths[1:-1]), features=bool(int(z["features"])),
+                             scaling=str(z["scaling"]))
+        model.net.set_params(z["params"])
+        model.mean, model.std = z["mean"], z["std"]
+        return model
+
 
 def evaluate(model: LearnedStart, params, g: Grid2D, every=5, max_steps=20000, tol=1e-10, diagnose=False):
     """Held-out comparison: plain solver energies E* first, then both starts to |E - E*| <= 1e-8.
@@ -302,6 +328,7 @@ def main():
     ap.add_argument("--nr", type=int, default=2048)
     ap.add_argument("--nth", type=int, default=64)
     ap.add_argument("--modes", type=int, default=64)
+    ap.add_argument("--nxi", type=int, default=1024, help="points of the basis's scaled radial grid")
     ap.add_argument("--epochs", type=int, default=3000)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--lr-end", type=float, default=None)
@@ -310,19 +337,23 @@ def main():
     ap.add_argument("--scaling", default="channel", choices=["channel", "coef"],
                     help="standardise the targets per l channel or per coefficient")
     ap.add_argument("--out", default="learned_start.json")
+    ap.add_argument("--model-out", default=None, help="write the trained model (.npz)")
     a = ap.parse_args()
     g = Grid2D(a.nr, a.nth)
     t0 = time.perf_counter()
     ptrain = param_sets(a.train, 5)
     states, energies, nsteps = ground_states(ptrain, g)
     t_data = time.perf_counter() - t0
-    basis = RadialBasis(states, ptrain, g, a.modes)
+    basis = RadialBasis(states, ptrain, g, a.modes, nxi=a.nxi)
     model = LearnedStart(basis, features=a.features, scaling=a.scaling)
     t0 = time.perf_counter()
     losses = model.fit(ptrain, states, steps=a.epochs, lr=a.lr, lr_end=a.lr_end)
     t_fit = time.perf_counter() - t0
+    if a.model_out:
+        model.save(a.model_out)
     res = evaluate(model, param_sets(a.heldout, 6), g, diagnose=a.diagnose)
-    res.update({"train": a.train, "grid": [a.nr, a.nth], "modes": a.modes, "train_loss_first": float(losses[0]),
+    res.update({"train": a.train, "grid": [a.nr, a.nth], "modes": a.modes, "nxi": a.nxi,
+                "train_loss_first": float(losses[0]),
                 "train_loss_last": float(losses[-1]), "data_generation_s": t_data, "fit_s": t_fit,
                 "epochs": a.epochs, "lr": a.lr, "lr_end": a.lr_end, "features": a.features, "scaling": a.scaling,
                 "train_steps_mean": float(np.mean(nsteps))})
