@@ -238,8 +238,43 @@ __host__ __device__ inline bool diag1d_across(const DevOp& op, int sweep_axis) {
   return op.kind == OP_DIAG1D && op.axis != sweep_axis;
 }
 
+// Packed tiles (PK > 1, lane extent n = 128 / PK): PK groups of bn columns side by side,
+// 128 tile columns in all.  Their passes (checked on the host) have one non-lane axis, every
+// norm with the same weights and every across-lane diagonal with the same table, so the
+// tables hold one row of 128 columns each, laid over the first rows of colw / colt.
+template <int PK>
+__device__ __forceinline__ float tab_w(const TileTabs& T, int red, int col) {
+  if constexpr (PK > 1)
+    return (&T.colw[0][0])[col];
+  else
+    return T.colw[red][col];
+}
+template <int PK>
+__device__ __forceinline__ float2 tab_t(const TileTabs& T, int slot, int col) {
+  if constexpr (PK > 1)
+    return (&T.colt[0][0])[col];
+  else
+    return T.colt[slot][col];
+}
+
+template <int PK>
 __device__ __forceinline__ void build_tile_tabs(const PassParams& p, TileTabs& T, int64_t o, int64_t i0, int bn) {
   const Geometry& g = p.g;
+  if constexpr (PK > 1) {
+    // bn = all PK x 32 tile columns, a single non-lane axis (inner index i0 + c)
+    for (int idx = threadIdx.x; idx < p.nops * bn; idx += kWorkThreads) {
+      const int oi = idx / bn, c = idx - oi * bn;
+      const DevOp& op = p.ops[oi];
+      const int64_t i = i0 + c;
+      if (op.kind == OP_NORM)
+        (&T.colw[0][0])[c] = __ldg(op.wf[g.perm[g.ndim - 1]] + i);
+      else if (op.kind == OP_DIAG1D && op.axis != g.sweep_axis)
+        (&T.colt[0][0])[c] = __ldg(reinterpret_cast<const float2*>(op.ptr) + i);
+      else if (op.kind == OP_SCALE && c == 0)
+        T.scale[oi] = (float)sqrt(__ldcg(p.slots + op.b) / __ldcg(p.slots + op.c));
+    }
+    return;
+  }
   if ((int)threadIdx.x < p.nops) {
     int k = 0;
     for (int q = 0; q < (int)threadIdx.x; ++q) k += diag1d_across(p.ops[q], g.sweep_axis);
@@ -266,7 +301,7 @@ __device__ __forceinline__ void build_tile_tabs(const PassParams& p, TileTabs& T
 // Point-wise ops [ob, oe) on the NB values of one lane-axis row j, tile columns
 // c0 .. c0 + NB - 1 (storage indices ix0 .. ix0 + NB - 1): the epilogue layout.
 // rw_val is this row's weight in the row-weight vector rw_ptr (loaded ahead of time).
-template <int NB>
+template <int NB, int PK = 1>
 __device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T, int ob, int oe, float2 (&v)[NB],
                                           int j, int c0, int64_t ix0, float* acc, const float* rw_ptr,
                                           float rw_val) {
@@ -281,7 +316,7 @@ __device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T
           for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], t);
         } else {
 #pragma unroll
-          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], T.colt[T.slot[oi]][c0 + u]);
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tab_t<PK>(T, T.slot[oi], c0 + u));
         }
         break;
       }
@@ -314,7 +349,8 @@ __device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T
       case OP_NORM: {
         float s = 0.0f;
 #pragma unroll
-        for (int u = 0; u < NB; ++u) s = fmaf(fmaf(v[u].x, v[u].x, v[u].y * v[u].y), T.colw[op.red][c0 + u], s);
+        for (int u = 0; u < NB; ++u)
+          s = fmaf(fmaf(v[u].x, v[u].x, v[u].y * v[u].y), tab_w<PK>(T, op.red, c0 + u), s);
         const float* wr = op.wf[g.sweep_axis];
         acc[op.red] += s * (wr == rw_ptr ? rw_val : __ldg(wr + j));
         break;
@@ -327,10 +363,71 @@ __device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T
 
 // Point-wise ops [ob, oe) on the NB values of one tile column c, lane-axis rows
 // j0 + u G (storage indices ix0 + u rstride): the prologue layout.
-template <int NB>
+// PK > 1 (packed tile): value u sits at virtual row R = j0 + u G, i.e. lane row R % nl of
+// column group R / nl (nl = the real lane extent), storage index base + (R % nl) inner +
+// (R / nl) bn + c; ix0 and rstride are then unused.
+template <int NB, int PK = 1>
 __device__ __forceinline__ void apply_col(const PassParams& p, const TileTabs& T, int ob, int oe, float2 (&v)[NB],
-                                          int j0, int G, int c, int64_t ix0, int64_t rstride, float* acc) {
+                                          int j0, int G, int c, int64_t ix0, int64_t rstride, float* acc,
+                                          int nl = 0, int bn = 0, int64_t base = 0) {
   const Geometry& g = p.g;
+  if constexpr (PK > 1) {
+    int jl[NB], col[NB];
+    int64_t ix[NB];
+#pragma unroll
+    for (int u = 0; u < NB; ++u) {
+      const int R = j0 + u * G;
+      jl[u] = R & (nl - 1);
+      col[u] = (R / nl) * bn + c;
+      ix[u] = base + (int64_t)jl[u] * g.inner + col[u];
+    }
+    for (int oi = ob; oi < oe; ++oi) {
+      const DevOp& op = p.ops[oi];
+      switch (op.kind) {
+        case OP_DIAG1D: {
+          const float2* t = reinterpret_cast<const float2*>(op.ptr);
+          if (op.axis == g.sweep_axis) {
+            float2 tv[NB];
+#pragma unroll
+            for (int u = 0; u < NB; ++u) tv[u] = __ldg(t + jl[u]);
+#pragma unroll
+            for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tv[u]);
+          } else {
+#pragma unroll
+            for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tab_t<PK>(T, 0, col[u]));
+          }
+          break;
+        }
+        case OP_DIAGND: {
+          const float2* t = reinterpret_cast<const float2*>(op.ptr);
+          float2 tv[NB];
+#pragma unroll
+          for (int u = 0; u < NB; ++u) tv[u] = __ldg(t + ix[u]);
+#pragma unroll
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tv[u]);
+          break;
+        }
+        case OP_SCALE: {
+          const float f = T.scale[oi];
+#pragma unroll
+          for (int u = 0; u < NB; ++u) v[u] = {v[u].x * f, v[u].y * f};
+          break;
+        }
+        case OP_NORM: {
+          const float* wr = op.wf[g.sweep_axis];
+          float s = 0.0f;
+#pragma unroll
+          for (int u = 0; u < NB; ++u)
+            s = fmaf(fmaf(v[u].x, v[u].x, v[u].y * v[u].y), __ldg(wr + jl[u]) * tab_w<PK>(T, 0, col[u]), s);
+          acc[op.red] += s;
+          break;
+        }
+        default:
+          break;
+      }
+    }
+    return;
+  }
   for (int oi = ob; oi < oe; ++oi) {
     const DevOp& op = p.ops[oi];
     switch (op.kind) {
@@ -499,11 +596,13 @@ __device__ __forceinline__ void store1(unsigned char* bh, unsigned char* bl, uin
 //   mode 1: sum / difference pairs, rows j < n/2 and n-1-j -> K row j of both halves (RB = 4)
 // OZ (split-BF16x6): the operand goes to three slice images (bh, bm, bl) with the quanta of
 // each column's largest value, gathered in cm (per-column maxima, zero on entry) first.
-template <int NK, int RB, int MODE, bool BF, bool OZ>
+// PK > 1: a packed tile (virtual rows: lane row j % nl of column group j / nl, bn columns a group).
+template <int NK, int RB, int MODE, bool BF, bool OZ, int PK = 1>
 __device__ __forceinline__ void prologue_vec(const PassParams& p, const TileTabs& T, int oe, const float2* psi,
                                              int64_t base, int c, int a, int G, int n, unsigned char* bh,
                                              unsigned char* bm, unsigned char* bl, uint32_t bhalf, uint32_t sbo_b,
-                                             float* acc, unsigned long long* loaded_mark, uint32_t* cm) {
+                                             float* acc, unsigned long long* loaded_mark, uint32_t* cm, int nl = 0,
+                                             int bn = 0) {
   const int64_t inner = p.g.inner;
   const int64_t bstride = (int64_t)RB * G;  // rows between a thread's row blocks
   float2 v[RB][NK];
@@ -513,7 +612,10 @@ __device__ __forceinline__ void prologue_vec(const PassParams& p, const TileTabs
 #pragma unroll
     for (int k = 0; k < NK; ++k) {
       const int64_t j = (int64_t)RB * a + r + bstride * k;
-      v[r][k] = psi[base + j * inner + c];
+      if constexpr (PK > 1)
+        v[r][k] = psi[base + (j & (nl - 1)) * inner + (j / nl) * bn + c];
+      else
+        v[r][k] = psi[base + j * inner + c];
       if constexpr (MODE == 1) w[r][k] = psi[base + (n - 1 - j) * inner + c];
     }
   if (loaded_mark) {
@@ -528,7 +630,8 @@ __device__ __forceinline__ void prologue_vec(const PassParams& p, const TileTabs
 #pragma unroll
   for (int r = 0; r < RB; ++r) {
     const int j0 = RB * a + r;
-    apply_col<NK>(p, T, 0, oe, v[r], j0, (int)bstride, c, base + (int64_t)j0 * inner + c, bstride * inner, acc);
+    apply_col<NK, PK>(p, T, 0, oe, v[r], j0, (int)bstride, c, base + (int64_t)j0 * inner + c, bstride * inner, acc,
+                      nl, bn, base);
     if constexpr (MODE == 1)
       apply_col<NK>(p, T, 0, oe, w[r], n - 1 - j0, -(int)bstride, c, base + (int64_t)(n - 1 - j0) * inner + c,
                     -bstride * inner, acc);
@@ -696,6 +799,7 @@ struct TcParams {
   int32_t error_slot;
   int32_t parity[2];          // per matrix: 0 plain; 1 sum / difference rows; 2 even / odd columns
   unsigned long long* trace;  // optional phase timestamps, kTraceSlots per tile (nullptr: off)
+  int32_t pack;               // column groups per tile (1; or 128 / n packed, images block-diagonal)
 };
 
 // Phase timestamps (%globaltimer, ns) of the optional trace, per tile (work thread 0).
@@ -901,7 +1005,10 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
 
 // The tiles blockIdx.x, blockIdx.x + gridDim.x, ... of a launch (every tile of a launch
 // has the same lane extent n).
-template <bool BF, bool OZ, typename Resolve>
+// PK > 1: packed tiles of lane extent 128 / PK (see tab_w): the tensor core sees one
+// 128-row tile whose row R is lane row R % nl of column group R / nl, with the lane matrix
+// block-diagonal (PK copies), so no accumulator row and no epilogue thread is idle.
+template <bool BF, bool OZ, int PK, typename Resolve>
 __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t total) {
   using namespace tc;
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -918,7 +1025,8 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (blockIdx.x >= total) return;
   const TcParams* first = resolve(blockIdx.x).prm;  // every tile of a launch shares n and parity mode
-  const int n = (int)first->p.g.n;
+  const int nl = (int)first->p.g.n;  // the lane extent; n: the tile's rows (nl PK)
+  const int n = nl * PK;
   const bool par = first->parity[0] != 0;
   const TcShape S = tc_shape(n, par, BF, OZ);
   const TcSmemLayout L = tc_layout(n, par, BF, OZ);
@@ -980,7 +1088,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       const Geometry& g = p.g;
       const int64_t tile = r.tile;
       const int64_t o = tile / g.tiles_per_outer;
-      const int64_t i0 = (tile - o * g.tiles_per_outer) * S.bn;
+      const int64_t i0 = (tile - o * g.tiles_per_outer) * S.bn * PK;
       const int64_t base = o * g.n * g.inner + i0;  // element (row 0, column 0) of the tile
       float2* psi = reinterpret_cast<float2*>(p.psi);
       if (tid == 0) trace_mark(tp, tile, TR_START);
@@ -988,7 +1096,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       // a pass that starts with its matrix needs the tables only after the first GEMM: they
       // are built while it runs (after the prologue) instead of ahead of the prologue
       const bool late_tabs = tp.mat_op[0] == 0;
-      if (!late_tabs) build_tile_tabs(p, tabs, o, i0, S.bn);
+      if (!late_tabs) build_tile_tabs<PK>(p, tabs, o, i0, S.bn * PK);
       // full-size tables read after the first lane matrix: start their tile rows toward L2
       for (int oi = tp.mat_op[0] + 1; oi < p.nops; ++oi) {
         const DevOp& op = p.ops[oi];
@@ -997,8 +1105,8 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         for (int q = tp.mat_op[0] + 1; q < oi; ++q) seen |= p.ops[q].kind == OP_DIAGND && p.ops[q].ptr == op.ptr;
         const float2* t = reinterpret_cast<const float2*>(op.ptr) + base;
         if (!seen && (reinterpret_cast<uintptr_t>(t) & 15u) == 0)
-          for (int jj = tid; jj < n; jj += kWorkThreads)
-            prefetch_lines_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * sizeof(float2)));
+          for (int jj = tid; jj < nl; jj += kWorkThreads)
+            prefetch_lines_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * PK * sizeof(float2)));
       }
       if constexpr (OZ)
         for (int k = tid; k < 128; k += kWorkThreads) s_colmax[k >> 6][k & 63] = 0u;
@@ -1022,7 +1130,8 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         else if (k0 == 2)
           prologue_vec<2, 8, 2, BF, OZ>(p, tabs, mo, psi, base, c, h, G, n, bhb, bmb, blb, bhb2, L.sbo_b, acc, lm, cm0);
         else if (n / G == 16)
-          prologue_vec<4, 4, 0, BF, OZ>(p, tabs, mo, psi, base, c, h, G, n, bhb, bmb, blb, 0, L.sbo_b, acc, lm, cm0);
+          prologue_vec<4, 4, 0, BF, OZ, PK>(p, tabs, mo, psi, base, c, h, G, n, bhb, bmb, blb, 0, L.sbo_b, acc, lm,
+                                            cm0, nl, S.bn);
         else if (n / G == 8)
           prologue_vec<2, 4, 0, BF, OZ>(p, tabs, mo, psi, base, c, h, G, n, bhb, bmb, blb, 0, L.sbo_b, acc, lm, cm0);
         else
@@ -1039,12 +1148,12 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         const Geometry& gn = rn.prm->p.g;
         const int64_t on = rn.tile / gn.tiles_per_outer;
         const float2* pn = reinterpret_cast<const float2*>(rn.prm->p.psi) + on * gn.n * gn.inner +
-                           (rn.tile - on * gn.tiles_per_outer) * S.bn;
-        for (int jj = tid; jj < n; jj += kWorkThreads)
-          prefetch_lines_l2(pn + (int64_t)jj * gn.inner, (uint32_t)(S.bn * sizeof(float2)));
+                           (rn.tile - on * gn.tiles_per_outer) * S.bn * PK;
+        for (int jj = tid; jj < nl; jj += kWorkThreads)
+          prefetch_lines_l2(pn + (int64_t)jj * gn.inner, (uint32_t)(S.bn * PK * sizeof(float2)));
       }
       // (the first drain's barrier orders these writes before the epilogue reads them)
-      if (late_tabs) build_tile_tabs(p, tabs, o, i0, S.bn);
+      if (late_tabs) build_tile_tabs<PK>(p, tabs, o, i0, S.bn * PK);
       // lane-axis weights of this thread's epilogue rows for the norms after the first
       // matrix, loaded now (they arrive while the GEMM runs)
       const float* rw_ptr = nullptr;
@@ -1052,7 +1161,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         if (p.ops[oi].kind == OP_NORM) rw_ptr = p.ops[oi].wf[g.sweep_axis];
       float rw_plain = 0.0f, rw_sum = 0.0f, rw_a = 0.0f, rw_b = 0.0f;
       if (rw_ptr) {
-        if (row_ok) rw_plain = __ldg(rw_ptr + j);
+        if (row_ok) rw_plain = __ldg(rw_ptr + (PK > 1 ? (j & (nl - 1)) : j));
         if (S.par) {
           rw_sum = __ldg(rw_ptr + 2 * i + up);
           rw_a = __ldg(rw_ptr + i);
@@ -1127,9 +1236,17 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             float2 x[kVals / 2];
 #pragma unroll
             for (int u = 0; u < kVals / 2; ++u) x[u] = valid ? float2{v[2 * u], v[2 * u + 1]} : float2{0.0f, 0.0f};
-            if (valid)
-              apply_row<kVals / 2>(p, tabs, sb, se, x, jr, c0, base + (int64_t)jr * g.inner + c0, acc, rw_ptr,
-                                   kind == 1 ? rw_sum : rw_plain);
+            if (valid) {
+              if constexpr (PK > 1) {
+                // packed: lane row jr % nl of column group jr / nl
+                const int jl = jr & (nl - 1), cg = (jr / nl) * S.bn + c0;
+                apply_row<kVals / 2, PK>(p, tabs, sb, se, x, jl, cg, base + (int64_t)jl * g.inner + cg, acc, rw_ptr,
+                                         rw_plain);
+              } else {
+                apply_row<kVals / 2>(p, tabs, sb, se, x, jr, c0, base + (int64_t)jr * g.inner + c0, acc, rw_ptr,
+                                     kind == 1 ? rw_sum : rw_plain);
+              }
+            }
             if (tid == 0 && m == 0) trace_mark(tp, tile, TR_APPLY0);
             if (last) {
               if (valid) stage_row<kVals / 2>(x, c0, jr, stg, S.stage_row);
@@ -1239,7 +1356,9 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             const int k = kb + u * G;
-            psi[base + (int64_t)k * g.inner + c] = *reinterpret_cast<const float2*>(stg + k * S.stage_row + 2 * c);
+            const int64_t ix = PK > 1 ? (int64_t)(k & (nl - 1)) * g.inner + (k / nl) * S.bn + c
+                                      : (int64_t)k * g.inner + c;
+            psi[base + ix] = *reinterpret_cast<const float2*>(stg + k * S.stage_row + 2 * c);
           }
         }
       }
@@ -1281,16 +1400,16 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
 }
 
 // OPM: operand mode, 0 = 3xTF32, 1 = split-BF16x3, 2 = split-BF16x6 (exact sums)
-template <int OPM>
+template <int OPM, int PK = 1>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel(const __grid_constant__ TcParams tp) {
   const TcParams* prm = &tp;
-  tc_persistent<OPM != 0, OPM == 2>([prm](int64_t t) { return TileRef{prm, t}; }, tp.p.g.tiles);
+  tc_persistent<OPM != 0, OPM == 2, PK>([prm](int64_t t) { return TileRef{prm, t}; }, tp.p.g.tiles);
 }
 
 // Many propagations' lane-matrix passes in one launch (all with the same lane extent):
 // global tile b is tile (b - offsets[i]) of params[i], offsets[i] <= b < offsets[i + 1];
 // offsets[count] is the total.
-template <int OPM>
+template <int OPM, int PK = 1>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel_batched(const TcParams* __restrict__ params,
                                                                         const uint2* __restrict__ owners,
                                                                         int64_t total) {
@@ -1301,7 +1420,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel_batche
     const uint2 o = __ldg(owners + b);
     return TileRef{params + o.x, (int64_t)o.y};
   };
-  tc_persistent<OPM != 0, OPM == 2>(resolve, total);
+  tc_persistent<OPM != 0, OPM == 2, PK>(resolve, total);
 }
 
 // ------------------------------------------------------------------ host side
@@ -1312,9 +1431,10 @@ int angular_tc_columns(int n) { return tc_shape(n).bn; }
 size_t tc_params_bytes() { return sizeof(TcParams); }
 
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
-                    const int* parity, void* out) {
+                    const int* parity, void* out, int pack) {
   TcParams tp{};
   tp.p = p;
+  tp.pack = pack;
   tp.nmat = nmat;
   for (int i = 0; i < nmat; ++i) {
     tp.mat_op[i] = mat_op[i];
@@ -1371,23 +1491,35 @@ static unsigned persistent_grid(int64_t tiles, int ctas_per_sm = 0) {
 
 int64_t angular_tc_grid(int64_t tiles, int ctas_per_sm) { return (int64_t)persistent_grid(tiles, ctas_per_sm); }
 
+// kernel variants: operand modes 0, 1, 2 unpacked, and split-BF16x6 packed 2 and 4 ways
+static int tc_variant(int mode, int pack) {
+  if (mode < 0 || mode > 2) return -1;
+  if (pack == 1) return mode;
+  if (mode == 2 && pack == 2) return 3;
+  if (mode == 2 && pack == 4) return 4;
+  return -1;
+}
+
 cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners_dev, int64_t blocks, size_t smem,
-                                      int mode, cudaStream_t s, int ctas_per_sm) {
-  static bool configured[3] = {false, false, false};
-  if (mode < 0 || mode > 2) return cudaErrorInvalidValue;
-  const void* kerns[3] = {(const void*)angular_tc_kernel_batched<0>, (const void*)angular_tc_kernel_batched<1>,
-                          (const void*)angular_tc_kernel_batched<2>};
-  if (!configure_once(kerns[mode], configured[mode])) return cudaGetLastError();
+                                      int mode, cudaStream_t s, int ctas_per_sm, int pack) {
+  static bool configured[5] = {false, false, false, false, false};
+  const int v = tc_variant(mode, pack);
+  if (v < 0) return cudaErrorInvalidValue;
+  const void* kerns[5] = {(const void*)angular_tc_kernel_batched<0>, (const void*)angular_tc_kernel_batched<1>,
+                          (const void*)angular_tc_kernel_batched<2>, (const void*)angular_tc_kernel_batched<2, 2>,
+                          (const void*)angular_tc_kernel_batched<2, 4>};
+  if (!configure_once(kerns[v], configured[v])) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
   const TcParams* prm = reinterpret_cast<const TcParams*>(params_dev);
   const uint2* own = reinterpret_cast<const uint2*>(owners_dev);
   const unsigned grid = persistent_grid(blocks, ctas_per_sm);
-  if (mode == 2)
-    angular_tc_kernel_batched<2><<<grid, kThreads, smem, s>>>(prm, own, blocks);
-  else if (mode == 1)
-    angular_tc_kernel_batched<1><<<grid, kThreads, smem, s>>>(prm, own, blocks);
-  else
-    angular_tc_kernel_batched<0><<<grid, kThreads, smem, s>>>(prm, own, blocks);
+  switch (v) {
+    case 4: angular_tc_kernel_batched<2, 4><<<grid, kThreads, smem, s>>>(prm, own, blocks); break;
+    case 3: angular_tc_kernel_batched<2, 2><<<grid, kThreads, smem, s>>>(prm, own, blocks); break;
+    case 2: angular_tc_kernel_batched<2><<<grid, kThreads, smem, s>>>(prm, own, blocks); break;
+    case 1: angular_tc_kernel_batched<1><<<grid, kThreads, smem, s>>>(prm, own, blocks); break;
+    default: angular_tc_kernel_batched<0><<<grid, kThreads, smem, s>>>(prm, own, blocks); break;
+  }
   count_launch();
   return cudaGetLastError();
 }
@@ -1396,6 +1528,34 @@ bool angular_tc_eligible(const Geometry& g) {
   if (!(g.n == 32 || g.n == 64 || g.n == 128 || g.n == 256)) return false;
   const int bn = tc_shape((int)g.n).bn;
   return g.inner >= bn && g.inner % bn == 0;
+}
+
+// Column groups a tile of this pass packs (split-BF16x6, lanes of 32 or 64 points): 128 / n
+// when the tile's 128 / n groups of 32 columns fit the inner axis and the pass's tables have
+// the packed form (two axes, the lane axis outermost; every norm with the same weights and
+// every across-lane diagonal with the same table), else 1.
+int angular_tc_pack(const Geometry& g, const DevOp* ops, int nops, int mode) {
+  if (mode != 2 || !(g.n == 32 || g.n == 64) || g.ndim != 2 || g.spos != 0 || g.outer != 1) return 1;
+  const int pk = (int)(128 / g.n), bn = tc_shape((int)g.n).bn;
+  if (g.inner % ((int64_t)pk * bn) != 0) return 1;
+  const float* w = nullptr;
+  const void* t = nullptr;
+  const int other = g.perm[1];
+  for (int i = 0; i < nops; ++i) {
+    const DevOp& o = ops[i];
+    if (o.kind == OP_NORM) {
+      if (w && w != o.wf[other]) return 1;
+      w = o.wf[other];
+    } else if (diag1d_across(o, g.sweep_axis)) {
+      if (t && t != o.ptr) return 1;
+      t = o.ptr;
+    } else if (!(o.kind == OP_MAT || o.kind == OP_DIAGND || o.kind == OP_SCALE || o.kind == OP_COPY ||
+                 o.kind == OP_LOSS || o.kind == OP_SETC || o.kind == OP_RECORD ||
+                 (o.kind == OP_DIAG1D && o.axis == g.sweep_axis))) {
+      return 1;
+    }
+  }
+  return pk;
 }
 
 bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis) {
@@ -1588,10 +1748,11 @@ cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_ou
 
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
                               int error_slot, const int* parity, int mode, cudaStream_t s,
-                              unsigned long long* trace, int ctas_per_sm) {
+                              unsigned long long* trace, int ctas_per_sm, int pack) {
   TcParams tp{};
   tp.trace = trace;
   tp.p = p;
+  tp.pack = pack;
   tp.nmat = nmat;
   for (int i = 0; i < nmat; ++i) {
     tp.mat_op[i] = mat_op[i];
@@ -1599,20 +1760,23 @@ cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, 
     tp.parity[i] = parity ? parity[i] : 0;
   }
   tp.error_slot = error_slot;
-  if (mode < 0 || mode > 2) return cudaErrorInvalidValue;
-  const size_t smem = angular_tc_smem_bytes((int)p.g.n, tp.parity[0] != 0, mode);
-  static bool configured[3] = {false, false, false};
-  const void* kerns[3] = {(const void*)angular_tc_kernel<0>, (const void*)angular_tc_kernel<1>,
-                          (const void*)angular_tc_kernel<2>};
-  if (!configure_once(kerns[mode], configured[mode])) return cudaGetLastError();
+  const int v = tc_variant(mode, pack);
+  if (v < 0) return cudaErrorInvalidValue;
+  const size_t smem = angular_tc_smem_bytes((int)p.g.n * pack, tp.parity[0] != 0, mode);
+  static bool configured[5] = {false, false, false, false, false};
+  const void* kerns[5] = {(const void*)angular_tc_kernel<0>, (const void*)angular_tc_kernel<1>,
+                          (const void*)angular_tc_kernel<2>, (const void*)angular_tc_kernel<2, 2>,
+                          (const void*)angular_tc_kernel<2, 4>};
+  if (!configure_once(kerns[v], configured[v])) return cudaGetLastError();
   if (smem > tc_max_dynamic_smem()) return cudaErrorInvalidValue;
   const unsigned grid = persistent_grid(p.g.tiles, ctas_per_sm);
-  if (mode == 2)
-    angular_tc_kernel<2><<<grid, kThreads, smem, s>>>(tp);
-  else if (mode == 1)
-    angular_tc_kernel<1><<<grid, kThreads, smem, s>>>(tp);
-  else
-    angular_tc_kernel<0><<<grid, kThreads, smem, s>>>(tp);
+  switch (v) {
+    case 4: angular_tc_kernel<2, 4><<<grid, kThreads, smem, s>>>(tp); break;
+    case 3: angular_tc_kernel<2, 2><<<grid, kThreads, smem, s>>>(tp); break;
+    case 2: angular_tc_kernel<2><<<grid, kThreads, smem, s>>>(tp); break;
+    case 1: angular_tc_kernel<1><<<grid, kThreads, smem, s>>>(tp); break;
+    default: angular_tc_kernel<0><<<grid, kThreads, smem, s>>>(tp); break;
+  }
   count_launch();
   return cudaGetLastError();
 }

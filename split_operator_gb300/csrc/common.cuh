@@ -180,6 +180,8 @@ void pass_choose_buffers(PassParams& p, bool fp64);
 // Tensor-core angular sweep (angular_tc.cu): FP32 state, real lane matrices as 3xTF32.
 int angular_tc_columns(int n);  // complex columns of the inner axis per CTA tile
 bool angular_tc_eligible(const Geometry& g);
+// column groups one tile of this pass packs into the tensor core's 128 rows (1: none)
+int angular_tc_pack(const Geometry& g, const DevOp* ops, int nops, int mode);
 // the pass's point-wise ops fit the per-tile tables of the tensor-core kernel
 bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis);
 // operand modes of the tensor-core pass: 0 3xTF32, 1 split-BF16x3, 2 split-BF16x6 (exact sums)
@@ -193,7 +195,7 @@ void angular_tc_parity_images(const double* m, int n, int kind, int mode, std::v
 // per-tile phase timestamps (angular_tc_trace_slots() per tile), nullptr: off
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
                               int error_slot, const int* parity, int mode, cudaStream_t s,
-                              unsigned long long* trace = nullptr, int ctas_per_sm = 0);
+                              unsigned long long* trace = nullptr, int ctas_per_sm = 0, int pack = 1);
 int angular_tc_trace_slots();
 // one CTA waits (limit_ns, both wait forms) on an mbarrier nothing completes; out[3]:
 // timed out (try_wait form), timed out (polling form), elapsed ns
@@ -206,13 +208,13 @@ cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassPar
 size_t tc_params_bytes();
 void tc_params_set_trace(void* params, unsigned long long* trace);  // the TcParams' trace field
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
-                    const int* parity, void* out);
+                    const int* parity, void* out, int pack = 1);
 // persistent CTAs a launch of `tiles` tensor-core tiles runs on (CTA k takes the tiles at
 // positions k, k + grid, k + 2 grid, ... of the owners table)
 int64_t angular_tc_grid(int64_t tiles, int ctas_per_sm = 0);
 // owners_dev: blocks pairs (pass index, tile within the pass), uint32 each, in global tile order
 cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners_dev, int64_t blocks, size_t smem,
-                                      int mode, cudaStream_t s, int ctas_per_sm = 0);
+                                      int mode, cudaStream_t s, int ctas_per_sm = 0, int pack = 1);
 
 // Auxiliary kernels (aux_kernels.cu)
 cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);

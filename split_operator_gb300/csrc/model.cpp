@@ -319,6 +319,18 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
     int kind = 0;
     shared_tc_images(md, (int)n, tc_mode(), stream, c.tc_images, c.tc_par_images, kind);
     tc_images_by_matrix_[c.buf.ptr] = c.tc_images->as<float>();
+    if (tc_mode() == 2 && (n == 32 || n == 64)) {
+      // packed tiles: 128 / n copies of the matrix on the diagonal of a 128 x 128 one
+      const size_t pk = 128 / n;
+      std::vector<double> bd(128 * 128, 0.0);
+      for (size_t b = 0; b < pk; ++b)
+        for (size_t r = 0; r < n; ++r)
+          for (size_t k = 0; k < n; ++k) bd[(b * n + r) * 128 + b * n + k] = md[r * n + k];
+      std::shared_ptr<DeviceBuffer> none;
+      int kind_bd = 0;
+      shared_tc_images(bd, 128, tc_mode(), stream, c.tc_pack_images, none, kind_bd);
+      tc_pack_by_matrix_[c.buf.ptr] = c.tc_pack_images->as<float>();
+    }
     // the parity-split form as well, when the matrix has the structure (Legendre pairs)
     if (kind)
       tc_parity_by_matrix_[c.buf.ptr] = {kind, c.tc_par_images->as<float>()};
@@ -408,7 +420,21 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
   } else {
     parity[0] = parity[1] = 0;
   }
-  const int bn = angular_tc_columns((int)g.n);
+  // packed tiles for short lanes: 128 / n column groups per tile, block-diagonal images
+  int pk = par ? 1 : angular_tc_pack(g, ops.data(), (int)ops.size(), tc_mode());
+  if (pk > 1) {
+    const float* pim[2] = {nullptr, nullptr};
+    for (int m = 0; m < nmat && pk > 1; ++m) {
+      auto it = tc_pack_by_matrix_.find(ops[mats[m]].ptr);
+      if (it == tc_pack_by_matrix_.end())
+        pk = 1;
+      else
+        pim[m] = it->second;
+    }
+    if (pk > 1)
+      for (int m = 0; m < nmat; ++m) images[m] = pim[m];
+  }
+  const int bn = angular_tc_columns((int)g.n) * pk;
   g.lanes_per_tile = bn;
   g.tiles_per_outer = (int32_t)(g.inner / bn);
   g.tiles = g.outer * g.tiles_per_outer;
@@ -419,7 +445,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     p.partials = partials_.as<double>();
   }
   static const char* const kTcNames[3] = {"f32 tc3xtf32", "f32 tcbf16x3", "f32 tcbf16x6"};
-  std::string name = std::string(kTcNames[tc_mode()]) + (par ? " parity axis" : " axis") +
+  std::string name = std::string(kTcNames[tc_mode()]) + (par ? " parity axis" : (pk > 1 ? " packed axis" : " axis")) +
                      std::to_string(axis) + ":";
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   const TcSchedule sched = tc_schedule(g.n, tc_mode());
@@ -428,9 +454,9 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     // SM, tile order): one batched launch serves one of each; the kernel's thread count is fixed
     RecordedPass r{RecordedPass::TensorCore, false, p, std::vector<unsigned char>(tc_params_bytes()),
                    (int)g.n | (par ? 1 << 16 : 0) | (tc_mode() << 17) | ((sched.ctas_per_sm & 3) << 20) |
-                       (sched.blocked ? 1 << 22 : 0),
-                   angular_tc_smem_bytes((int)g.n, par, tc_mode()), name, pass_bytes(ops, g)};
-    make_tc_params(p, mats, nmat, images, timeout_slot, parity, r.tcp.data());
+                       (sched.blocked ? 1 << 22 : 0) | ((pk == 4 ? 2 : pk == 2 ? 1 : 0) << 23),
+                   angular_tc_smem_bytes((int)g.n * pk, par, tc_mode()), name, pass_bytes(ops, g)};
+    make_tc_params(p, mats, nmat, images, timeout_slot, parity, r.tcp.data(), pk);
     recording->push_back(std::move(r));
     return true;
   }
@@ -446,7 +472,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     cuda_check(cudaMemsetAsync(trace.ptr, 0, trace.bytes, stream), "trace clear");
   }
   cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, parity, tc_mode(), stream,
-                               trace_path ? trace.as<unsigned long long>() : nullptr, sched.ctas_per_sm),
+                               trace_path ? trace.as<unsigned long long>() : nullptr, sched.ctas_per_sm, pk),
              "tensor-core pass launch");
   if (trace_path) {
     std::vector<unsigned long long> h(trace.bytes / sizeof(unsigned long long));
@@ -1761,7 +1787,7 @@ void Batch::run_groups(std::vector<Group>& gs) {
     }
     if (g.kind == RecordedPass::TensorCore)
       cuda_check(launch_angular_tc_batched(g.params.ptr, g.owners.ptr, g.blocks, g.smem, (g.threads >> 17) & 3,
-                                           stream_, (g.threads >> 20) & 3),
+                                           stream_, (g.threads >> 20) & 3, 1 << ((g.threads >> 23) & 3)),
                  "batched tensor-core pass");
     else
       cuda_check(launch_pass_batched(g.fp64, g.sweep, (g.threads >> 16) & 1, g.params.as<PassParams>(),

@@ -209,3 +209,22 @@ def test_real_lane_matrix_split_bf16x6(so, n, nr):
     bound = (np.abs(psi) @ np.abs(t).T)
     assert np.max(np.abs(got - ref) / bound) < 6e-7, np.max(np.abs(got - ref) / bound)
     assert rel_l2(got, ref) < 5e-7
+
+
+@pytest.mark.parametrize("nr,nth", [(512, 32), (1024, 64)])
+def test_packed_short_lanes_match_the_oracle(so, nr, nth):
+    """Split-BF16x6 with lanes of 32 or 64 points runs packed tiles: 128 / n column groups
+    share one 128-row tensor-core tile through a block-diagonal lane matrix.  Against the FP64
+    oracle step by step, and the packed pass is the one that ran."""
+    from split_operator_gb300 import workloads as W
+    steps = 6
+    prop, _ = W.radial_angular_2d(nr=nr, nth=nth, step_no=steps, seed=13, r0=25.0, precision="fp32_bf16x6")
+    oprop, _ = S.radial_angular_2d(nr=nr, nth=nth, step_no=steps, seed=13, r0=25.0)
+    prop.set_timing(True)
+    for k in range(steps):
+        prop.steps(1)
+        oprop.step()
+        assert rel_l2(prop.get_array(), oprop.wave_function.array) < 1e-6 * (k + 1), k
+    names = " ".join(t[0] for t in prop.kernel_times())
+    assert "tcbf16x6 packed" in names, names
+    assert abs(prop.all_losses()[0] - oprop.all_losses()[0][1]) < 1e-7

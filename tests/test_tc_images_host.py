@@ -38,10 +38,10 @@ int main(int argc, char** argv) {
   if (!o) return 6;
   const int kind = so::angular_tc_parity(m.data(), n);
   std::fwrite(&kind, 4, 1, o);
-  for (int bf = 0; bf < 2; ++bf) {
+  for (int bf = 0; bf < 3; ++bf) {  // operand modes: 3xTF32, split-BF16x3, split-BF16x6
     std::vector<float> img, par;
-    so::angular_tc_images(m.data(), n, bf != 0, img);
-    if (kind) so::angular_tc_parity_images(m.data(), n, kind, bf != 0, par);
+    so::angular_tc_images(m.data(), n, bf, img);
+    if (kind) so::angular_tc_parity_images(m.data(), n, kind, bf, par);
     for (auto* v : {&img, &par}) {
       const long long c = (long long)v->size();
       std::fwrite(&c, 8, 1, o);
@@ -81,7 +81,7 @@ def pack(tmp_path_factory):
         raw = fout.read_bytes()
         kind = int(np.frombuffer(raw, np.int32, 1, 0)[0])
         pos, res = 4, {}
-        for bf in (0, 1):
+        for bf in (0, 1, 2):
             for key in ("full", "par"):
                 c = int(np.frombuffer(raw, np.int64, 1, pos)[0])
                 pos += 8
@@ -207,3 +207,60 @@ def test_parity_images_reproduce_the_product(pack, bf, which):
         assert np.array_equal(hi[:hn], h_full[0::2, :hn]) and np.array_equal(hi[hn:], h_full[1::2, :hn])
     else:
         assert np.array_equal(hi[:hn], h_full[:hn, 0::2]) and np.array_equal(hi[hn:], h_full[:hn, 1::2])
+
+
+def decode_oz(img, n, par):
+    """Split-BF16x6 images: per K chunk three 8 KB bf16 slice images, same core-matrix order."""
+    rows, kdim, chunk_k, kc = shape(n, par, True)
+    nk = kdim // chunk_k
+    assert img.size == nk * 3 * CHUNK
+    sbo = (chunk_k // kc) * 128
+    r = np.arange(rows)[:, None]
+    kk = np.arange(chunk_k)[None, :]
+    off = (r >> 3) * sbo + (kk // kc) * 128 + (r & 7) * 16 + (kk % kc) * 2
+    sl = np.zeros((3, rows, kdim))
+    for q in range(nk):
+        for part in range(3):
+            buf = img[(q * 3 + part) * CHUNK:(q * 3 + part + 1) * CHUNK]
+            h = buf.view(np.uint16)[off // 2].astype(np.uint32) << 16
+            sl[part, :, q * chunk_k:(q + 1) * chunk_k] = h.view(np.float32)
+    return sl
+
+
+@pytest.mark.parametrize("n", [32, 64, 128, 256])
+def test_split_bf16x6_images_are_fixed_point_slices(pack, n):
+    """Each row of the A operand as three bf16 slices on the fixed-point grid of that row:
+    slice i a multiple of q_i = 2^(e - 8 - 8 i) (2^e just above the row's largest magnitude)
+    with |s_i / q_i| <= 256, and s0 + s1 + s2 within 2^-24 2^e of the value -- the form whose
+    products the tensor core sums exactly."""
+    rng = np.random.default_rng(3 * n)
+    m = rng.standard_normal((n, n)) * np.exp(rng.uniform(-6, 6, (n, 1))) * np.exp(rng.uniform(-2, 2, (n, n)))
+    _, res = pack(m)
+    sl = decode_oz(res[(2, "full")], n, False)
+    rows = sl.shape[1]
+    assert not sl[:, n:].any(), "rows beyond n are zero padding"
+    e = np.ceil(np.log2(np.abs(m).max(axis=1)))
+    e = np.where(np.abs(m).max(axis=1) >= 2.0 ** e, e + 1, e)  # 2^e strictly above the maximum
+    for i in range(3):
+        q = 2.0 ** (e - 8 - 8 * i)
+        k = sl[i, :n] / q[:, None]
+        assert np.array_equal(k, np.round(k)), i
+        assert np.abs(k).max() <= 256
+    assert np.all(np.abs(sl[:, :n].sum(axis=0) - m) <= 2.0 ** (e - 24)[:, None])
+
+
+def test_split_bf16x6_block_diagonal_images(pack):
+    """Packed tiles of lane extent 32: four copies of the 32 x 32 matrix on the diagonal of a
+    128 x 128 one, each row with its own quanta, zero off the diagonal blocks."""
+    t, _ = legendre(32)
+    bd = np.zeros((128, 128))
+    for b in range(4):
+        bd[32 * b:32 * b + 32, 32 * b:32 * b + 32] = t
+    _, res = pack(bd)
+    sl = decode_oz(res[(2, "full")], 128, False)
+    a = sl.sum(axis=0)
+    mask = np.kron(np.eye(4), np.ones((32, 32))).astype(bool)
+    assert not a[~mask].any()
+    assert np.abs(a - bd).max() <= 2.0 ** -23 * np.abs(t).max()
+    for b in range(4):
+        np.testing.assert_array_equal(sl[:, 32 * b:32 * b + 32, 32 * b:32 * b + 32], sl[:, :32, :32])
