@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
                     help="timed region only (no e2e, accuracy or CPU legs): the case profiled under ncu")
+    ap.add_argument("--no-ground-state", action="store_true", help="skip the time-to-ground-state leg")
+    ap.add_argument("--ground-state-sets", type=int, default=16,
+                    help="held-out parameter sets of the time-to-ground-state leg")
     ap.add_argument("--no-tune", action="store_true",
                     help="built-in launch schedules (the autotuner is skipped)")
     ap.add_argument("--tune-cache", default=None,
@@ -496,6 +499,18 @@ def run_ours(a):
             f64_ms = e0.elapsed_time(e1)
         acc["fp64_gpu_value"] = points64 * f64_steps / (f64_ms / 1e3)
         acc["speedup_vs_fp64_gpu"] = value / world / acc["fp64_gpu_value"]
+        del props64
+        if not single:
+            b64 = None
+
+    tgs = None
+    if rank == 0 and not single and not a.no_ground_state:
+        # the metric's second half: time to the ground state, learned start vs Gaussian start
+        from split_operator_gb300 import learned_start as LS
+        if os.path.exists(LS.MODEL_2048x64):
+            tgs = LS.time_to_ground_state(count=a.ground_state_sets)
+        else:
+            tgs = {"unavailable": "trained model file missing"}
 
     if rank != 0:
         return
@@ -512,7 +527,8 @@ def run_ours(a):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "global_batch": len(props) * world, "wall_s_timed_region": wall},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clocks.summary(), "accuracy_vs_fp64": acc, "autotune": tune, "passes": [list(t) for t in kt]}
+            "clocks": clocks.summary(), "accuracy_vs_fp64": acc, "autotune": tune, "time_to_ground_state": tgs,
+            "passes": [list(t) for t in kt]}
     print(json.dumps(line), flush=True)
 
 

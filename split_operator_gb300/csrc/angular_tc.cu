@@ -361,6 +361,90 @@ __device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T
   }
 }
 
+// The same ops on two rows ja, jb of the same NB columns (the even / odd epilogue holds rows
+// i and n-1-i): op by op for both rows, so each table's two row loads are in flight together.
+template <int NB>
+__device__ __forceinline__ void apply_row2(const PassParams& p, const TileTabs& T, int ob, int oe, float2 (&va)[NB],
+                                           float2 (&vb)[NB], int ja, int jb, int c0, int64_t ixa, int64_t ixb,
+                                           float* acc, const float* rw_ptr, float rwa, float rwb) {
+  const Geometry& g = p.g;
+  for (int oi = ob; oi < oe; ++oi) {
+    const DevOp& op = p.ops[oi];
+    switch (op.kind) {
+      case OP_DIAG1D: {
+        if (op.axis == g.sweep_axis) {
+          const float2 ta = __ldg(reinterpret_cast<const float2*>(op.ptr) + ja);
+          const float2 tb = __ldg(reinterpret_cast<const float2*>(op.ptr) + jb);
+#pragma unroll
+          for (int u = 0; u < NB; ++u) {
+            va[u] = cmulf(va[u], ta);
+            vb[u] = cmulf(vb[u], tb);
+          }
+        } else {
+#pragma unroll
+          for (int u = 0; u < NB; ++u) {
+            const float2 t = T.colt[T.slot[oi]][c0 + u];
+            va[u] = cmulf(va[u], t);
+            vb[u] = cmulf(vb[u], t);
+          }
+        }
+        break;
+      }
+      case OP_DIAGND: {
+        const float2* ta = reinterpret_cast<const float2*>(op.ptr) + ixa;
+        const float2* tb = reinterpret_cast<const float2*>(op.ptr) + ixb;
+        if (((reinterpret_cast<uintptr_t>(ta) | reinterpret_cast<uintptr_t>(tb)) & 15u) == 0) {
+          float4 qa[NB / 2], qb[NB / 2];
+#pragma unroll
+          for (int q = 0; q < NB / 2; ++q) {
+            qa[q] = __ldg(reinterpret_cast<const float4*>(ta) + q);
+            qb[q] = __ldg(reinterpret_cast<const float4*>(tb) + q);
+          }
+#pragma unroll
+          for (int q = 0; q < NB / 2; ++q) {
+            va[2 * q] = cmulf(va[2 * q], make_float2(qa[q].x, qa[q].y));
+            va[2 * q + 1] = cmulf(va[2 * q + 1], make_float2(qa[q].z, qa[q].w));
+            vb[2 * q] = cmulf(vb[2 * q], make_float2(qb[q].x, qb[q].y));
+            vb[2 * q + 1] = cmulf(vb[2 * q + 1], make_float2(qb[q].z, qb[q].w));
+          }
+        } else {
+#pragma unroll
+          for (int u = 0; u < NB; ++u) {
+            va[u] = cmulf(va[u], __ldg(ta + u));
+            vb[u] = cmulf(vb[u], __ldg(tb + u));
+          }
+        }
+        break;
+      }
+      case OP_SCALE: {
+        const float f = T.scale[oi];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+          va[u] = {va[u].x * f, va[u].y * f};
+          vb[u] = {vb[u].x * f, vb[u].y * f};
+        }
+        break;
+      }
+      case OP_NORM: {
+        float sa = 0.0f, sb = 0.0f;
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+          const float w = T.colw[op.red][c0 + u];
+          sa = fmaf(fmaf(va[u].x, va[u].x, va[u].y * va[u].y), w, sa);
+          sb = fmaf(fmaf(vb[u].x, vb[u].x, vb[u].y * vb[u].y), w, sb);
+        }
+        const float* wr = op.wf[g.sweep_axis];
+        const bool pre = wr == rw_ptr;
+        acc[op.red] += sa * (pre ? rwa : __ldg(wr + ja));
+        acc[op.red] += sb * (pre ? rwb : __ldg(wr + jb));
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
 // Point-wise ops [ob, oe) on the NB values of one tile column c, lane-axis rows
 // j0 + u G (storage indices ix0 + u rstride): the prologue layout.
 // PK > 1 (packed tile): value u sits at virtual row R = j0 + u G, i.e. lane row R % nl of
@@ -1286,8 +1370,8 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             xa[u] = {er + orr, ei + oi};
             xb[u] = {er - orr, ei - oi};
           }
-          apply_row<kVals / 4>(p, tabs, sb, se, xa, ja, cc0, base + (int64_t)ja * g.inner + cc0, acc, rw_ptr, rw_a);
-          apply_row<kVals / 4>(p, tabs, sb, se, xb, jb, cc0, base + (int64_t)jb * g.inner + cc0, acc, rw_ptr, rw_b);
+          apply_row2<kVals / 4>(p, tabs, sb, se, xa, xb, ja, jb, cc0, base + (int64_t)ja * g.inner + cc0,
+                                base + (int64_t)jb * g.inner + cc0, acc, rw_ptr, rw_a, rw_b);
           if (tid == 0 && m == 0) trace_mark(tp, tile, TR_APPLY0);
           if (last) {
             stage_row<kVals / 4>(xa, cc0, ja, stg, S.stage_row);

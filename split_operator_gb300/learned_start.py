@@ -28,6 +28,7 @@ and every network product runs in the library's kernels.
 import argparse
 import json
 import math
+import os
 import time
 
 import numpy as np
@@ -319,6 +320,37 @@ def evaluate(model: LearnedStart, params, g: Grid2D, every=5, max_steps=20000, t
             "wall_ratio_learned_over_gaussian": wall_l / wall_g,
             "steps_ratio_learned_over_gaussian": float(np.mean(steps_l) / np.mean(steps_g)),
             "converged_gaussian": int(np.sum(steps_g < max_steps)), "converged_learned": int(np.sum(steps_l < max_steps))}
+
+
+# the network and basis trained at the full configuration (4096 ground states on the 2048 x 64
+# grid, 64 radial modes per l), as written by `--model-out`
+MODEL_2048x64 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "learned_start_2048x64.npz")
+
+
+def time_to_ground_state(model_path=MODEL_2048x64, count=16, first=0, every=5, max_steps=20000):
+    """Time to the ground state on `count` held-out parameter sets (default_rng(6), the sets
+    first .. first + count - 1): the plain FP64 solver's converged energy E* first, then the
+    plain Gaussian start and the learned start, each relaxed until |E - E*| <= 1e-8.  Wall
+    times of both starts (the learned one including the network and the basis sum)."""
+    model = LearnedStart.load(model_path)
+    g = model.basis.g
+    params = param_sets(256, 6)[first:first + count]
+    t0 = time.perf_counter()
+    _, e_star, _ = ground_states(params, g, tol=1e-10, every=20, max_steps=max_steps)
+    t_star = time.perf_counter() - t0
+    _, steps_g, wall_g = relax([problem(p, g) for p in params], every=every, max_steps=max_steps, target=e_star)
+    t0 = time.perf_counter()
+    starts = model.predict(params)
+    t_predict = time.perf_counter() - t0
+    _, steps_l, wall_l = relax([problem(p, g, psi0=s) for p, s in zip(params, starts)], every=every,
+                               max_steps=max_steps, target=e_star)
+    wall_l += t_predict
+    return {"heldout_sets": [first, first + count], "grid": [g.nr, g.nth], "tolerance": 1e-8,
+            "judge": "E* of the plain FP64 imaginary-time solver run to |dE| <= 1e-10", "e_star_s": t_star,
+            "wall_s_gaussian": wall_g, "wall_s_learned": wall_l, "predict_s": t_predict,
+            "wall_ratio_learned_over_gaussian": wall_l / wall_g,
+            "steps_gaussian_mean": float(np.mean(steps_g)), "steps_learned_mean": float(np.mean(steps_l)),
+            "converged": [int(np.sum(steps_g < max_steps)), int(np.sum(steps_l < max_steps))]}
 
 
 def main():

@@ -32,3 +32,17 @@ def test_learned_start_beats_gaussian_start_small():
     res = LS.evaluate(model, LS.param_sets(8, 6), g, every=5)
     assert res["converged_learned"] == 8 and res["converged_gaussian"] == 8
     assert res["steps_learned_mean"] < res["steps_gaussian_mean"], res
+
+
+def test_committed_model_reaches_the_ground_state_in_a_third_of_the_time():
+    """The network and basis trained at the full configuration (4096 FP64 ground states on the
+    2048 x 64 grid, 64 radial modes per l, trained on the library's tensor-core MLP kernels) on
+    eight held-out parameter sets: relaxation from the learned start reaches |E - E*| <= 1e-8
+    (E* = the plain FP64 solver's converged energy) in at most a third of the wall time of the
+    plain Gaussian start, network and basis evaluation included."""
+    ensure_built()
+    from split_operator_gb300 import learned_start as LS
+    res = LS.time_to_ground_state(count=8, first=0)
+    assert res["converged"] == [8, 8], res
+    assert res["wall_ratio_learned_over_gaussian"] <= 1.0 / 3.0, res
+    assert res["steps_learned_mean"] < 0.5 * res["steps_gaussian_mean"], res
