@@ -152,12 +152,15 @@ def relax(props, every=20, max_steps=20000, tol=None, target=None, group=512):
     return energy, steps, time.perf_counter() - t0
 
 
-def ground_states(params, g: Grid2D, tol=1e-10, every=20, max_steps=20000, chunk=512):
+def ground_states(params, g: Grid2D, tol=1e-10, every=20, max_steps=20000, chunk=512, progress=False):
     """FP64 ground states (real parts, [count, nr, nth]), energies and step counts."""
     states = np.empty((len(params), g.nr, g.nth), dtype=np.float32)
     energies = np.empty(len(params))
     nsteps = np.empty(len(params), dtype=np.int64)
+    t0 = time.perf_counter()
     for s in range(0, len(params), chunk):
+        if progress:
+            print(f"ground states {s}/{len(params)} after {time.perf_counter() - t0:.0f} s", flush=True)
         props = [problem(p, g) for p in params[s:s + chunk]]
         e, st, _ = relax(props, every=every, max_steps=max_steps, tol=tol)
         for k, p in enumerate(props):
@@ -374,13 +377,15 @@ def main():
     g = Grid2D(a.nr, a.nth)
     t0 = time.perf_counter()
     ptrain = param_sets(a.train, 5)
-    states, energies, nsteps = ground_states(ptrain, g)
+    states, energies, nsteps = ground_states(ptrain, g, progress=True)
     t_data = time.perf_counter() - t0
+    print(f"training data: {t_data:.0f} s", flush=True)
     basis = RadialBasis(states, ptrain, g, a.modes, nxi=a.nxi)
     model = LearnedStart(basis, features=a.features, scaling=a.scaling)
     t0 = time.perf_counter()
     losses = model.fit(ptrain, states, steps=a.epochs, lr=a.lr, lr_end=a.lr_end)
     t_fit = time.perf_counter() - t0
+    print(f"fit: {t_fit:.0f} s, loss {losses[0]:.3e} -> {losses[-1]:.3e}", flush=True)
     if a.model_out:
         model.save(a.model_out)
     res = evaluate(model, param_sets(a.heldout, 6), g, diagnose=a.diagnose)
