@@ -720,6 +720,38 @@ __device__ __forceinline__ void prologue_vec(const PassParams& p, const TileTabs
       apply_col<NK>(p, T, 0, oe, w[r], n - 1 - j0, -(int)bstride, c, base + (int64_t)(n - 1 - j0) * inner + c,
                     -bstride * inner, acc);
   }
+  if constexpr (OZ && PK > 1) {
+    // packed tile: row block k lies in column group (RB a + bstride k) / nl, whose columns
+    // carry their own quanta (set g of cm: 64 entries, re and im of its 32 columns)
+    OzQ qr[NK], qi[NK];
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      float mr = 0.0f, mi = 0.0f;
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        mr = fmaxf(mr, fabsf(v[r][k].x));
+        mi = fmaxf(mi, fabsf(v[r][k].y));
+      }
+      const int grp = (RB * a + (int)bstride * k) / nl;
+      colmax_add(cm + grp * 64, 2 * c, mr);
+      colmax_add(cm + grp * 64, 2 * c + 1, mi);
+    }
+    work_sync();
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const int grp = (RB * a + (int)bstride * k) / nl;
+      qr[k] = oz_quanta(cm[grp * 64 + 2 * c]);
+      qi[k] = oz_quanta(cm[grp * 64 + 2 * c + 1]);
+    }
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+      const int j0 = RB * a + (int)bstride * k;
+      const uint32_t orr = boff<true>(2 * c, j0, sbo_b), oim = boff<true>(2 * c + 1, j0, sbo_b);
+      store4_oz(bh, bm, bl, orr, v[0][k].x, v[1][k].x, v[2][k].x, v[3][k].x, qr[k]);
+      store4_oz(bh, bm, bl, oim, v[0][k].y, v[1][k].y, v[2][k].y, v[3][k].y, qi[k]);
+    }
+    return;
+  }
   if constexpr (OZ) {
     // the column's largest stored magnitude (re and im are separate B columns); for the sum /
     // difference pairs |v| + |w| bounds both |v + w| and |v - w|
@@ -1104,7 +1136,11 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   __shared__ double totals[kMaxRed];
   __shared__ int s_last;
   __shared__ volatile int s_fail;
-  __shared__ uint32_t s_colmax[2][64];  // split-BF16x6: column maxima of the two B operands of a tile
+  // split-BF16x6: column maxima of the two B operands of a tile (re and im of each column; a
+  // packed tile keeps one set per column group: its block-diagonal matrix only sums products
+  // within a group, so each group's columns carry their own quanta)
+  constexpr int kCm = 64 * PK;
+  __shared__ uint32_t s_colmax[2][kCm];
   static_assert(sizeof(TcParams) % 4 == 0, "TcParams is copied as 32-bit words");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (blockIdx.x >= total) return;
@@ -1193,7 +1229,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             prefetch_lines_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * PK * sizeof(float2)));
       }
       if constexpr (OZ)
-        for (int k = tid; k < 128; k += kWorkThreads) s_colmax[k >> 6][k & 63] = 0u;
+        for (int k = tid; k < 2 * kCm; k += kWorkThreads) s_colmax[k / kCm][k % kCm] = 0u;
       work_sync();  // tabs complete; the previous tile's staging has been stored
       if (tid == 0) trace_mark(tp, tile, TR_TABS);
 
@@ -1336,13 +1372,16 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
               if (valid) stage_row<kVals / 2>(x, c0, jr, stg, S.stage_row);
             } else {
               // a warp whose rows all lie past the lane extent (n < 128) adds nothing
-              if (S.mh == 2 || 32 * lg < n) colmax_rows<kVals / 2>(x, c0, s_colmax[1]);
+              // (a packed tile's warp holds rows of one column group: its maxima go to that
+              // group's set)
+              uint32_t* cm1 = s_colmax[1] + (PK > 1 ? (jr / nl) * 64 : 0);
+              if (S.mh == 2 || 32 * lg < n) colmax_rows<kVals / 2>(x, c0, cm1);
               work_sync();
               if (tid == 0 && m == 0) trace_mark(tp, tile, TR_SYNC0);
               if (valid) {
                 const uint32_t ho = next == 2 ? (uint32_t)(jr & 1) * bhb2 : 0u;
                 write_b_row_oz<kVals / 2>(x, c0, next == 2 ? jr >> 1 : jr, bhb + ho, bmb + ho, blb + ho, L.sbo_b,
-                                          s_colmax[1]);
+                                          cm1);
               }
             }
           } else if (jr < n) {
