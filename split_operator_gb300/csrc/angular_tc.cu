@@ -916,6 +916,8 @@ struct TcParams {
   int32_t parity[2];          // per matrix: 0 plain; 1 sum / difference rows; 2 even / odd columns
   unsigned long long* trace;  // optional phase timestamps, kTraceSlots per tile (nullptr: off)
   int32_t pack;               // column groups per tile (1; or 128 / n packed, images block-diagonal)
+  int32_t npre;               // distinct full-size tables read after the first matrix (prefetched per tile)
+  const void* pre[4];
 };
 
 // Phase timestamps (%globaltimer, ns) of the optional trace, per tile (work thread 0).
@@ -1124,6 +1126,54 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
 // PK > 1: packed tiles of lane extent 128 / PK (see tab_w): the tensor core sees one
 // 128-row tile whose row R is lane row R % nl of column group R / nl, with the lane matrix
 // block-diagonal (PK copies), so no accumulator row and no epilogue thread is idle.
+// A finished tile's norm partials, waiting to be published: the work warps of the next tile
+// write them and draw the pass ticket while that tile's first GEMM runs (or after the CTA's
+// last tile), so the ticket's fence and atomic round trip stay off the tile chain.
+struct PendTicket {
+  const TcParams* prm;  // nullptr: nothing pending
+  double* partials;
+  unsigned int* counter;
+  int64_t tiles, tile;
+  int nred;
+  double red[kMaxRed];
+};
+
+// Warp 0 (all lanes): publish the pending partials; the CTA that draws a pass's last ticket
+// folds all of the pass's partials in FP64 in a fixed order and runs its scalar ops.
+__device__ __noinline__ void publish_pending(PendTicket& pd, double* totals, int lane) {
+  const TcParams* q = pd.prm;
+  if (q == nullptr) return;
+  double* const part = pd.partials;
+  const int64_t tiles = pd.tiles;
+  const int nred = pd.nred;
+  unsigned int last = 0u;
+  if (lane == 0) {
+    for (int k = 0; k < nred; ++k) part[(int64_t)k * tiles + pd.tile] = pd.red[k];
+    __threadfence();
+    last = atomicAdd(pd.counter, 1u) == (unsigned int)(tiles - 1) ? 1u : 0u;
+  }
+  last = __shfl_sync(0xffffffffu, last, 0);
+  __syncwarp();
+  if (lane == 0) pd.prm = nullptr;
+  if (!last) return;
+  __threadfence();
+  for (int k = 0; k < nred; ++k) {
+    double a = 0.0;
+    for (int64_t b = lane; b < tiles; b += 32) a += __ldcg(part + (int64_t)k * tiles + b);
+#pragma unroll
+    for (int o2 = 16; o2 > 0; o2 >>= 1) a += __shfl_down_sync(0xffffffffu, a, o2);
+    if (lane == 0) totals[k] = a;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    const PassParams& p = q->p;
+    for (int oi = 0; oi < p.nops; ++oi) run_scalar_tc(p, p.ops[oi], totals);
+    __threadfence();
+    *p.counter = 0u;
+  }
+  __syncwarp();
+}
+
 template <bool BF, bool OZ, int PK, typename Resolve>
 __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t total) {
   using namespace tc;
@@ -1134,7 +1184,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   __shared__ FF scratch[kMaxRed * (kWorkThreads / 32)];
   __shared__ double blk_red[kMaxRed];
   __shared__ double totals[kMaxRed];
-  __shared__ int s_last;
+  __shared__ PendTicket s_pend;
   __shared__ volatile int s_fail;
   // split-BF16x6: column maxima of the two B operands of a tile (re and im of each column; a
   // packed tile keeps one set per column group: its block-diagonal matrix only sums products
@@ -1167,6 +1217,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
     mbar_init(dbar + 3, 1);  // quiet
     fence_mbar_init();
     s_fail = 0;
+    s_pend.prm = nullptr;
   }
   if (warp == 0) tmem_alloc(&tmem_base_s, kTmemCols);
   tc_fence_before();
@@ -1217,14 +1268,11 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       // are built while it runs (after the prologue) instead of ahead of the prologue
       const bool late_tabs = tp.mat_op[0] == 0;
       if (!late_tabs) build_tile_tabs<PK>(p, tabs, o, i0, S.bn * PK);
-      // full-size tables read after the first lane matrix: start their tile rows toward L2
-      for (int oi = tp.mat_op[0] + 1; oi < p.nops; ++oi) {
-        const DevOp& op = p.ops[oi];
-        if (op.kind != OP_DIAGND) continue;
-        bool seen = false;
-        for (int q = tp.mat_op[0] + 1; q < oi; ++q) seen |= p.ops[q].kind == OP_DIAGND && p.ops[q].ptr == op.ptr;
-        const float2* t = reinterpret_cast<const float2*>(op.ptr) + base;
-        if (!seen && (reinterpret_cast<uintptr_t>(t) & 15u) == 0)
+      // full-size tables read after the first lane matrix (each distinct table once, listed on
+      // the host): start their tile rows toward L2
+      for (int q = 0; q < tp.npre; ++q) {
+        const float2* t = reinterpret_cast<const float2*>(tp.pre[q]) + base;
+        if ((reinterpret_cast<uintptr_t>(t) & 15u) == 0)
           for (int jj = tid; jj < nl; jj += kWorkThreads)
             prefetch_lines_l2(t + (int64_t)jj * g.inner, (uint32_t)(S.bn * PK * sizeof(float2)));
       }
@@ -1288,6 +1336,9 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
           rw_b = __ldg(rw_ptr + (n - 1 - i));
         }
       }
+
+      // the previous tile's partials and ticket, while this tile's first GEMM runs
+      if (warp == 0) publish_pending(s_pend, totals, lane);
 
       bool ok = true;
       for (int m = 0; m < tp.nmat && ok; ++m) {
@@ -1465,11 +1516,15 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
       // norm partials of this tile (float-float, fixed order) and the pass ticket first, so
       // the fence waits for no state store and the ticket's round trip overlaps the store
       block_sums(acc, p.nred, scratch, blk_red);
-      unsigned int ticket = 0u;
       if (tid == 0) {
-        for (int k = 0; k < p.nred; ++k) p.partials[(int64_t)k * g.tiles + tile] = blk_red[k];
-        __threadfence();
-        ticket = atomicAdd(p.counter, 1u);
+        // published by the next tile (or after the last one): see PendTicket
+        s_pend.partials = p.partials;
+        s_pend.counter = p.counter;
+        s_pend.tiles = g.tiles;
+        s_pend.tile = tile;
+        s_pend.nred = p.nred;
+        for (int k = 0; k < p.nred; ++k) s_pend.red[k] = blk_red[k];
+        s_pend.prm = r.prm;
       }
 
       // coalesced store of the staged tile: thread = complex column
@@ -1485,30 +1540,13 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
           }
         }
       }
-      if (tid == 0) {
-        trace_mark(tp, tile, TR_STORE);
-        s_last = ticket == (unsigned int)(g.tiles - 1);
-      }
-      // the last tile's FP64 fold of all of the pass's partials
-      work_sync();
-      if (s_last) {
-        __threadfence();
-        for (int k = warp; k < p.nred; k += kWorkThreads / 32) {
-          double a = 0.0;
-          for (int64_t b = lane; b < g.tiles; b += 32) a += __ldcg(p.partials + (int64_t)k * g.tiles + b);
-#pragma unroll
-          for (int o2 = 16; o2 > 0; o2 >>= 1) a += __shfl_down_sync(0xffffffffu, a, o2);
-          if (lane == 0) totals[k] = a;
-        }
-        work_sync();
-        if (tid == 0) {
-          for (int oi = 0; oi < p.nops; ++oi) run_scalar_tc(p, p.ops[oi], totals);
-          __threadfence();
-          *p.counter = 0u;
-        }
-      }
+      if (tid == 0) trace_mark(tp, tile, TR_STORE);
+      work_sync();  // the staging and the pass copy are free for the next tile
       if (tid == 0) trace_mark(tp, tile, TR_END);
     }
+    // the last tile's partials (a CTA that stopped on a failed wait publishes nothing: the
+    // pass has recorded its error)
+    if (warp == 0 && !s_fail) publish_pending(s_pend, totals, lane);
   }
   __syncthreads();
   if (tid == 0 && s_fail) {
@@ -1565,6 +1603,13 @@ void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const floa
     tp.parity[i] = parity ? parity[i] : 0;
   }
   tp.error_slot = error_slot;
+  // the distinct full-size tables after the first matrix (the kernel prefetches their tile rows)
+  for (int oi = nmat > 0 ? mat_op[0] + 1 : p.nops; oi < p.nops && tp.npre < 4; ++oi) {
+    if (p.ops[oi].kind != OP_DIAGND) continue;
+    bool seen = false;
+    for (int q = 0; q < tp.npre; ++q) seen = seen || tp.pre[q] == p.ops[oi].ptr;
+    if (!seen) tp.pre[tp.npre++] = p.ops[oi].ptr;
+  }
   std::memcpy(out, &tp, sizeof(TcParams));
 }
 

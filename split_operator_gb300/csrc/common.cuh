@@ -89,6 +89,7 @@ struct PassParams {
   int32_t sweep;                // 1: only point-wise ops, norms, scalars and power-of-two FFTs
   int32_t fused;                // 1: an FFT pair with point-wise ops, run by fft_pair_kernel
   int32_t radix;                // fused: radix of the Stockham stages (16 or 8; the twiddle table's order)
+  int32_t ct;                   // fused FP32: log2 n of the fixed-shape kernel (0: the general-shape kernel)
   DevOp ops[kMaxOps];
 };
 
@@ -204,7 +205,9 @@ cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_ou
 // Batched launches over many propagations' passes (block -> (instance, tile) by offsets)
 cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassParams* params_dev,
                                 const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
-                                cudaStream_t s, int radix = 0);
+                                cudaStream_t s, int radix = 0, int ct_lgn = 0);
+// log2 n when a planned FP32 FFT-pair pass can run the fixed-shape kernel, else 0
+int fft_pair_ct_lgn(const PassParams& p, bool fp64);
 size_t tc_params_bytes();
 void tc_params_set_trace(void* params, unsigned long long* trace);  // the TcParams' trace field
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,

@@ -945,6 +945,246 @@ __global__ void __launch_bounds__(512, 2) fft_pair_kernel_batched_r8(const PassP
   fft_pair_batched_tile<float, 8>(params, offsets, count);
 }
 
+static size_t fft_pair_smem(const Geometry& g, bool fp64);
+
+// ------------------------------------------------------------------ FFT pair, fixed shape
+// The same FP32 pass for lanes of 2^LGN points (512 .. 8192: the radial extents of the batched
+// step) with the shape fixed at compile time: every stage's radix, span and twiddle offset,
+// and the shared-memory lane stride, are constants.  A butterfly's 16 shared-memory, global
+// and twiddle addresses are then one base plus immediate offsets, and the two directions (a
+// forward transform, then an inverse one) fold into the butterflies' signs.  The arithmetic
+// and its order are those of fft_pair_tile, so the results are the same.
+__host__ __device__ constexpr int lg2c(int x) { return x <= 1 ? 0 : 1 + lg2c(x / 2); }
+
+template <int LGN>
+struct PairShape {
+  static constexpr int kN = 1 << LGN;
+  static constexpr int kS = (LGN + 3) / 4;              // stages of radix 16, the last one rl
+  static constexpr int kRl = 1 << (LGN - 4 * (kS - 1));  // closing radix
+  static constexpr int kLs = ((kN + (kN >> 4)) % 2 == 0) ? kN + (kN >> 4) + 1 : kN + (kN >> 4);
+  // stage s of the forward order (16, ..., rl) and of the reversed order (rl, 16, ...)
+  __host__ __device__ static constexpr int rs(bool rev, int s) { return rev ? (s == 0 ? kRl : 16) : (s + 1 < kS ? 16 : kRl); }
+  __host__ __device__ static constexpr int span(bool rev, int s) { return s == 0 ? 1 : span(rev, s - 1) * rs(rev, s - 1); }
+  // first entry of stage s in the stage-major twiddle table (reversed order: from entry n)
+  __host__ __device__ static constexpr int twoff(bool rev, int s) {
+    return s == 0 ? (rev ? kN : 0) : twoff(rev, s - 1) + (span(rev, s - 1) > 1 ? (rs(rev, s - 1) - 1) * span(rev, s - 1) : 0);
+  }
+};
+
+// point-wise ops [ob, oe) on the outputs of a last stage (span P = n / RS): value j RS + q
+// sits at lane b >> lg P, point k + q P, k = b & (P - 1)
+template <int LGN, int RS>
+__device__ __forceinline__ void pair_pointwise_ct(float2 (&v)[kPairV], const PassParams& pp, int ob, int oe, int t,
+                                                  int T, int64_t lane0, int nl, float sc) {
+  constexpr int kN = 1 << LGN, kP = kN / RS, kLgP = LGN - lg2c(RS);
+#pragma unroll
+  for (int e = 0; e < kPairV; ++e) v[e] = float2{v[e].x * sc, v[e].y * sc};
+  for (int oi = ob; oi < oe; ++oi) {
+    const DevOp& op = pp.ops[oi];
+    const bool nd = op.kind == OP_DIAGND;
+    const float2* tab = reinterpret_cast<const float2*>(op.ptr) + (nd ? lane0 * kN : 0);
+#pragma unroll
+    for (int j = 0; j < kPairV / RS; ++j) {
+      const int b = t + j * T, l = b >> kLgP, k = b & (kP - 1);
+      if (!nd || l < nl) {
+        const float2* tr = tab + (nd ? l * kN : 0) + k;
+#pragma unroll
+        for (int q = 0; q < RS; ++q) v[j * RS + q] = cmul(v[j * RS + q], __ldg(tr + q * kP));
+      }
+    }
+  }
+}
+
+// one stage: radix RS, span P, twiddles from entry OFF; IN / OUT as in pair_stage_rs
+template <int LGN, int RS, int P, int OFF, int IN, int OUT, int DIR>
+__device__ __forceinline__ void pair_stage_ct(float2 (&v)[kPairV], float2* buf, const PassParams& pp,
+                                              float2* tile_psi, const float2* __restrict__ tw, int ob, int oe,
+                                              int64_t lane0, int nl, float sc) {
+  constexpr int kN = 1 << LGN, kNb = kN / RS, kLgNb = LGN - lg2c(RS), kLs = PairShape<LGN>::kLs;
+  const int t = threadIdx.x, T = blockDim.x;
+  if constexpr (IN == PIN_GLOBAL) {
+#pragma unroll
+    for (int j = 0; j < kPairV / RS; ++j) {
+      const int b = t + j * T, l = b >> kLgNb, i = b & (kNb - 1);
+      const float2* src = tile_psi + l * kN + i;
+      const bool ok = l < nl;
+#pragma unroll
+      for (int r = 0; r < RS; ++r) v[j * RS + r] = ok ? src[r * kNb] : float2{0.0f, 0.0f};
+    }
+  } else if constexpr (IN == PIN_SMEM) {
+    // element l ls + x + (x >> 4) of x = i + r nb: the padding term splits as (i >> 4) + (r nb >> 4)
+#pragma unroll
+    for (int j = 0; j < kPairV / RS; ++j) {
+      const int b = t + j * T, l = b >> kLgNb, i = b & (kNb - 1);
+      const float2* src = buf + l * kLs + i + (i >> 4);
+#pragma unroll
+      for (int r = 0; r < RS; ++r) v[j * RS + r] = src[r * kNb + ((r * kNb) >> 4)];
+    }
+    __syncthreads();  // every read of the stage before any write (in place)
+  }
+#pragma unroll
+  for (int j = 0; j < kPairV / RS; ++j) {
+    if constexpr (P > 1) {
+      // k = i & (P - 1) = b & (P - 1) (P <= nb); entry 0 of every twiddle row is exactly 1
+      const float2* w = tw + OFF + ((t + j * T) & (P - 1));
+#pragma unroll
+      for (int r = 1; r < RS; ++r) {
+        float2 wv = __ldg(w + (r - 1) * P);
+        if (DIR > 0) wv.y = -wv.y;
+        v[j * RS + r] = cmul(v[j * RS + r], wv);
+      }
+    }
+    dft_r<RS>(&v[j * RS], DIR);
+  }
+  if constexpr (OUT == POUT_SMEM) {
+    // outputs base + q P, base = (i - k) RS + k: the padding term splits as (base >> 4) + (q P >> 4)
+#pragma unroll
+    for (int j = 0; j < kPairV / RS; ++j) {
+      const int b = t + j * T, l = b >> kLgNb, i = b & (kNb - 1), k = i & (P - 1);
+      const int base = (i - k) * RS + k;
+      float2* dst = buf + l * kLs + base + (base >> 4);
+#pragma unroll
+      for (int q = 0; q < RS; ++q) dst[q * P + ((q * P) >> 4)] = v[j * RS + q];
+    }
+    __syncthreads();
+  } else {
+    pair_pointwise_ct<LGN, RS>(v, pp, ob, oe, t, T, lane0, nl, sc);
+    if constexpr (OUT == POUT_GLOBAL) {
+#pragma unroll
+      for (int j = 0; j < kPairV / RS; ++j) {
+        const int b = t + j * T, l = b >> kLgNb, k = b & (kNb - 1);
+        if (l < nl) {
+          float2* dst = tile_psi + l * kN + k;
+#pragma unroll
+          for (int q = 0; q < RS; ++q) dst[q * kNb] = v[j * RS + q];
+        }
+      }
+    }
+  }
+}
+
+// the stages S .. of one transform (REV: the reversed order of the second transform)
+template <int LGN, bool REV, int S, int DIR>
+__device__ __forceinline__ void pair_fft_ct(float2 (&v)[kPairV], float2* buf, const PassParams& pp, float2* tile_psi,
+                                            const float2* tw, int ob, int oe, int64_t lane0, int nl, float sc) {
+  using Sh = PairShape<LGN>;
+  constexpr int kIn = S == 0 ? (REV ? PIN_REGS : PIN_GLOBAL) : PIN_SMEM;
+  constexpr int kOut = S + 1 < Sh::kS ? POUT_SMEM : (REV ? POUT_GLOBAL : POUT_REGS);
+  pair_stage_ct<LGN, Sh::rs(REV, S), Sh::span(REV, S), Sh::twoff(REV, S), kIn, kOut, DIR>(v, buf, pp, tile_psi, tw, ob,
+                                                                                         oe, lane0, nl, sc);
+  if constexpr (S + 1 < Sh::kS) pair_fft_ct<LGN, REV, S + 1, DIR>(v, buf, pp, tile_psi, tw, ob, oe, lane0, nl, sc);
+}
+
+// [F (forward), point-wise, F^-1, point-wise] on the tile's lanes of 2^LGN points
+template <int LGN>
+__device__ __forceinline__ void fft_pair_tile_ct(const PassParams& pp, int64_t tile) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* buf = reinterpret_cast<float2*>(smem_raw);
+  const Geometry& g = pp.g;
+  const int64_t lane0 = tile * g.lanes_per_tile;
+  const int64_t rem = g.outer - lane0;
+  const int nl = rem < g.lanes_per_tile ? (int)rem : g.lanes_per_tile;
+  float2* tile_psi = reinterpret_cast<float2*>(pp.psi) + lane0 * (1 << LGN);
+  const float2* tw = reinterpret_cast<const float2*>(pp.twiddle);
+  const float sc = inv_sqrt_pow2<float>(LGN);
+  int f1 = 1;
+  while (f1 < pp.nops && pp.ops[f1].kind != OP_FFT) ++f1;
+  float2 v[kPairV];
+  pair_fft_ct<LGN, false, 0, -1>(v, buf, pp, tile_psi, tw, 1, f1, lane0, nl, sc);
+  pair_fft_ct<LGN, true, 0, 1>(v, buf, pp, tile_psi, tw, f1 + 1, pp.nops, lane0, nl, sc);
+}
+
+template <int LGN>
+__global__ void __launch_bounds__(512, 2) fft_pair_kernel_ct(const __grid_constant__ PassParams p) {
+  fft_pair_tile_ct<LGN>(p, blockIdx.x);
+}
+
+template <int LGN>
+__global__ void __launch_bounds__(512, 2) fft_pair_kernel_batched_ct(const PassParams* __restrict__ params,
+                                                                     const int64_t* __restrict__ offsets, int count) {
+  const int64_t b = blockIdx.x;
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (offsets[mid] <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  __shared__ __align__(16) PassParams sp;
+  for (int k = threadIdx.x; k < (int)(sizeof(PassParams) / 4); k += blockDim.x)
+    reinterpret_cast<uint32_t*>(&sp)[k] = reinterpret_cast<const uint32_t*>(params + lo)[k];
+  __syncthreads();
+  fft_pair_tile_ct<LGN>(sp, b - offsets[lo]);
+}
+
+// log2 n when a planned FP32 pair can run the fixed-shape kernel (radix 16, n = 512 .. 8192,
+// the padded lane stride of the geometry, a forward transform then an inverse one), else 0
+int fft_pair_ct_lgn(const PassParams& p, bool fp64) {
+  if (fp64 || !p.fused || p.radix != 16) return 0;
+  const int64_t n = p.g.n;
+  if (n < 512 || n > 8192 || (n & (n - 1)) != 0) return 0;
+  int64_t ls = n + (n >> 4);
+  if (ls % 2 == 0) ls += 1;
+  if (p.g.lane_stride != ls || p.nops < 2 || p.ops[0].kind != OP_FFT || p.ops[0].dir != -1) return 0;
+  int f1 = 1;
+  while (f1 < p.nops && p.ops[f1].kind != OP_FFT) ++f1;
+  if (f1 >= p.nops || p.ops[f1].dir != 1) return 0;
+  int lg = 0;
+  while ((int64_t)1 << lg < n) ++lg;
+  return lg;
+}
+
+template <typename K>
+static cudaError_t configure_once(K kern, bool& done) {
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
+template <int LGN>
+static cudaError_t launch_pair_ct(const PassParams& p, cudaStream_t s) {
+  static bool done = false;
+  cudaError_t e = configure_once(fft_pair_kernel_ct<LGN>, done);
+  if (e != cudaSuccess) return e;
+  fft_pair_kernel_ct<LGN><<<(unsigned)p.g.tiles, fft_pair_block(p.g), fft_pair_smem(p.g, false), s>>>(p);
+  return cudaGetLastError();
+}
+
+template <int LGN>
+static cudaError_t launch_pair_batched_ct(const PassParams* params_dev, const int64_t* offsets_dev, int count,
+                                          int64_t blocks, int threads, size_t smem, cudaStream_t s) {
+  static bool done = false;
+  cudaError_t e = configure_once(fft_pair_kernel_batched_ct<LGN>, done);
+  if (e != cudaSuccess) return e;
+  fft_pair_kernel_batched_ct<LGN><<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_pair_ct_any(int lgn, const PassParams& p, cudaStream_t s) {
+  switch (lgn) {
+    case 9: return launch_pair_ct<9>(p, s);
+    case 10: return launch_pair_ct<10>(p, s);
+    case 11: return launch_pair_ct<11>(p, s);
+    case 12: return launch_pair_ct<12>(p, s);
+    case 13: return launch_pair_ct<13>(p, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+static cudaError_t launch_pair_batched_ct_any(int lgn, const PassParams* params_dev, const int64_t* offsets_dev,
+                                              int count, int64_t blocks, int threads, size_t smem, cudaStream_t s) {
+  switch (lgn) {
+    case 9: return launch_pair_batched_ct<9>(params_dev, offsets_dev, count, blocks, threads, smem, s);
+    case 10: return launch_pair_batched_ct<10>(params_dev, offsets_dev, count, blocks, threads, smem, s);
+    case 11: return launch_pair_batched_ct<11>(params_dev, offsets_dev, count, blocks, threads, smem, s);
+    case 12: return launch_pair_batched_ct<12>(params_dev, offsets_dev, count, blocks, threads, smem, s);
+    case 13: return launch_pair_batched_ct<13>(params_dev, offsets_dev, count, blocks, threads, smem, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 int fft_pair_threads(const Geometry& g) { return g.n >= 8192 ? 512 : 256; }
 
 int fft_pair_block(const Geometry& g) { return (int)((int64_t)g.lanes_per_tile * g.n / kPairV); }
@@ -1034,9 +1274,14 @@ static cudaError_t launch_batched_impl(const PassParams* params_dev, const int64
 
 cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassParams* params_dev,
                                 const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
-                                cudaStream_t s, int radix) {
+                                cudaStream_t s, int radix, int ct_lgn) {
   if (fused) {
     if (smem > 220 * 1024 || threads > 512) return cudaErrorInvalidValue;
+    if (ct_lgn > 0 && !fp64 && radix != 8) {
+      const cudaError_t e = launch_pair_batched_ct_any(ct_lgn, params_dev, offsets_dev, count, blocks, threads, smem, s);
+      if (e == cudaSuccess) count_launch();
+      return e;
+    }
     static bool configured[3] = {false, false, false};
     const int which = fp64 ? 1 : (radix == 8 ? 2 : 0);
     const void* kerns[3] = {(const void*)fft_pair_kernel_batched, (const void*)fft_pair_kernel_batched_f64,
@@ -1142,6 +1387,11 @@ cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s) {
     }
     const size_t smem = fft_pair_smem(p.g, false);
     if (smem > 220 * 1024) return cudaErrorInvalidValue;
+    if (p.ct > 0 && !r8) {
+      const cudaError_t e = launch_pair_ct_any(p.ct, p, s);
+      if (e == cudaSuccess) count_launch();
+      return e;
+    }
     if (r8)
       fft_pair_kernel_r8<<<(unsigned)p.g.tiles, fft_pair_block(p.g), smem, s>>>(p);
     else

@@ -596,6 +596,8 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   if ((fft_pair || (fp64 && p.g.n > 4096)) && fft_pair_plan(p, fp64, resident)) {
     name_tag = p.radix == 8 && !fp64 ? " fftpair r8" : " fftpair";
     if (p.radix != (fp64 ? 8 : 16)) p.twiddle = twiddle((size_t)p.g.n, p.radix);  // the table in its stage order
+    p.ct = fft_pair_ct ? fft_pair_ct_lgn(p, fp64) : 0;
+    if (p.ct) name_tag = " fftpair ct";
   }
   if (fp64 && p.g.n > 4096 && !p.fused)
     throw Error(SO_ERR_UNSUPPORTED, "FP64 lanes longer than 4096 points are not supported outside FFT-pair passes "
@@ -610,9 +612,10 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
     // fused FFT pairs: bit 16 of the thread count (their own launch group and kernel)
-    // radix-8 FP32 pairs: bit 19 (their own kernel)
-    const int threads =
-        p.fused ? (fft_pair_block(p.g) | (1 << 16) | (p.radix == 8 && !fp64 ? 1 << 19 : 0)) : pass_threads(p.g);
+    // radix-8 FP32 pairs: bit 19 (their own kernel); fixed-shape FP32 pairs: bit 20
+    const int threads = p.fused ? (fft_pair_block(p.g) | (1 << 16) | (p.radix == 8 && !fp64 ? 1 << 19 : 0) |
+                                   (p.ct ? 1 << 20 : 0))
+                                : pass_threads(p.g);
     RecordedPass r{resident ? RecordedPass::Resident : RecordedPass::Generic, fp64, p, {},
                    threads, pass_smem_bytes(p, fp64), name, pass_bytes(ops, p.g)};
     recording->push_back(std::move(r));
@@ -1213,6 +1216,8 @@ Propagation::Propagation(WaveFunction& src, so_time_grid time, std::shared_ptr<O
   {
     const char* fp = std::getenv("SO_FFT_PAIR");  // "0": FFT pairs run the general pass kernel
     wf_->eng->fft_pair = !(fp && fp[0] == '0');
+    const char* ct = std::getenv("SO_FFT_PAIR_CT");  // "0": FFT pairs keep the general-shape kernel
+    wf_->eng->fft_pair_ct = !(ct && ct[0] == '0');
   }
   wf_->last_grid_names = src.last_grid_names;
   wf_->possible_norm_change = src.possible_norm_change;
@@ -1674,6 +1679,12 @@ Batch::~Batch() {
     cudaEventDestroy(t.a);
     cudaEventDestroy(t.b);
   }
+  for (size_t k = 0; k < side_.size(); ++k) {
+    cudaStreamSynchronize(side_[k]);
+    cudaStreamDestroy(side_[k]);
+    cudaEventDestroy(joins_[k]);
+  }
+  if (fork_) cudaEventDestroy(fork_);
   if (own_stream_) {
     cudaStreamSynchronize(stream_);
     cudaStreamDestroy(stream_);
@@ -1702,6 +1713,7 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
     g.count = (int)v.size();
     g.name = "batched " + std::to_string(v.size()) + "x " + v[0]->name;
     g.n = v[0]->p.g.n;
+    if (g.kind == RecordedPass::Generic && ((g.threads >> 20) & 1)) g.ct_lgn = v[0]->p.ct;
     std::vector<int64_t> off(v.size() + 1, 0);
     const size_t pb = g.kind == RecordedPass::TensorCore ? tc_params_bytes() : sizeof(PassParams);
     std::vector<unsigned char> params(pb * v.size());
@@ -1767,8 +1779,30 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
   return out;
 }
 
-void Batch::run_groups(std::vector<Group>& gs) {
-  for (Group& g : gs) {
+void Batch::run_groups(std::vector<Group>& gs, bool concurrent) {
+  // the members of a position's groups are disjoint, so the groups may run side by side: the
+  // largest first on the batch stream, the others on forked streams joined before the next
+  // position (the results are those of the sequential order: no member is touched twice)
+  const bool fork = concurrent && !timing_ && gs.size() > 1;
+  std::vector<size_t> order(gs.size());
+  for (size_t k = 0; k < gs.size(); ++k) order[k] = k;
+  if (fork) {
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return gs[a].bytes > gs[b].bytes; });
+    if (fork_ == nullptr) cuda_check(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming), "fork event");
+    while (side_.size() + 1 < gs.size()) {
+      cudaStream_t st;
+      cudaEvent_t ev;
+      cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "side stream");
+      cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "join event");
+      side_.push_back(st);
+      joins_.push_back(ev);
+    }
+    cuda_check(cudaEventRecord(fork_, stream_), "fork record");
+    for (size_t k = 1; k < gs.size(); ++k) cuda_check(cudaStreamWaitEvent(side_[k - 1], fork_, 0), "fork wait");
+  }
+  for (size_t q = 0; q < gs.size(); ++q) {
+    Group& g = gs[order[q]];
+    cudaStream_t st = fork && q > 0 ? side_[q - 1] : stream_;
     Timed t{};
     if (timing_) {
       t.name = g.name;
@@ -1787,18 +1821,24 @@ void Batch::run_groups(std::vector<Group>& gs) {
     }
     if (g.kind == RecordedPass::TensorCore)
       cuda_check(launch_angular_tc_batched(g.params.ptr, g.owners.ptr, g.blocks, g.smem, (g.threads >> 17) & 3,
-                                           stream_, (g.threads >> 20) & 3, 1 << ((g.threads >> 23) & 3)),
+                                           st, (g.threads >> 20) & 3, 1 << ((g.threads >> 23) & 3)),
                  "batched tensor-core pass");
     else
       cuda_check(launch_pass_batched(g.fp64, g.sweep, (g.threads >> 16) & 1, g.params.as<PassParams>(),
-                                     g.offsets.as<int64_t>(), g.count, g.blocks, g.threads & 0xffff, g.smem, stream_,
-                                     ((g.threads >> 19) & 1) ? 8 : 0),
+                                     g.offsets.as<int64_t>(), g.count, g.blocks, g.threads & 0xffff, g.smem, st,
+                                     ((g.threads >> 19) & 1) ? 8 : 0,
+                                     g.ct_lgn),
                  "batched pass");
     if (timing_) {
       cuda_check(cudaEventRecord(t.b, stream_), "event record");
       timed_.push_back(t);
     }
   }
+  if (fork)
+    for (size_t k = 1; k < gs.size(); ++k) {
+      cuda_check(cudaEventRecord(joins_[k - 1], side_[k - 1]), "join record");
+      cuda_check(cudaStreamWaitEvent(stream_, joins_[k - 1], 0), "join wait");
+    }
 }
 
 void Batch::steps(uint64_t n, bool wait, bool sync_members) {
@@ -1870,7 +1910,7 @@ void Batch::steps(uint64_t n, bool wait, bool sync_members) {
   launches_per_step_ = 0;
   for (size_t i = per0; i < per0 + m; ++i) launches_per_step_ += pos[i].size();
   // first step (head)
-  for (size_t i = 0; i < (merged ? 1 : m); ++i) run_groups(pos[i]);
+  for (size_t i = 0; i < (merged ? 1 : m); ++i) run_groups(pos[i], true);
   // the period once per further step, captured once as a CUDA graph when timing is off
   const uint64_t reps = n - 1;
   if (reps > 0) {
@@ -1878,7 +1918,7 @@ void Batch::steps(uint64_t n, bool wait, bool sync_members) {
       cudaGraph_t graph;
       cudaGraphExec_t exec;
       cuda_check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
-      for (size_t i = per0; i < per0 + m; ++i) run_groups(pos[i]);
+      for (size_t i = per0; i < per0 + m; ++i) run_groups(pos[i], true);
       cuda_check(cudaStreamEndCapture(stream_, &graph), "end capture");
       cuda_check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
       for (uint64_t r = 0; r < reps; ++r) cuda_check(cudaGraphLaunch(exec, stream_), "graph launch");
@@ -1888,12 +1928,12 @@ void Batch::steps(uint64_t n, bool wait, bool sync_members) {
       cudaGraphDestroy(graph);
     } else {
       for (uint64_t r = 0; r < reps; ++r)
-        for (size_t i = per0; i < per0 + m; ++i) run_groups(pos[i]);
+        for (size_t i = per0; i < per0 + m; ++i) run_groups(pos[i], true);
     }
   }
   // tail: the last step's closing passes (merged form only)
   if (merged)
-    for (size_t i = m + 1; i < np; ++i) run_groups(pos[i]);
+    for (size_t i = m + 1; i < np; ++i) run_groups(pos[i], true);
   for (Propagation* p : props_) p->count_steps(n);
   if (trace)
     std::fprintf(stderr, "batch steps(%llu) of %zu: sync %.3f record %.3f groups%s %.3f launched %.3f ms\n",

@@ -132,6 +132,7 @@ class Engine {
   // operand mode of the tensor-core pass (0 3xTF32, 1 split-BF16x3, 2 split-BF16x6), -1: none
   int tc_mode() const { return tc_tf32 ? 0 : (tc_bf16 ? 1 : (tc_bf16x6 ? 2 : -1)); }
   bool fft_pair = true;  // FP32 FFT-pair passes run the fused register kernel (SO_FFT_PAIR=0: the general pass)
+  bool fft_pair_ct = true;  // ... its fixed-shape form where it applies (SO_FFT_PAIR_CT=0: the general shape)
 
   size_t points() const;
   size_t elem_bytes() const { return fp64 ? 16 : 8; }
@@ -489,6 +490,7 @@ class Batch {
     std::string name;
     double bytes;
     int64_t n = 0;  // lane extent of the members' passes (the schedule class)
+    int ct_lgn = 0;  // fixed-shape FFT-pair kernel: log2 of the lane extent (0: general shape)
   };
   std::vector<Group> build_groups(const std::vector<std::vector<RecordedPass>>& rec, size_t pos);
   std::vector<std::vector<RecordedPass>> cached_rec_;  // the passes the cached groups were built from
@@ -508,10 +510,15 @@ class Batch {
     std::string name;
   };
   std::vector<TraceBuf> traces_;  // SO_TC_TRACE_BATCH diagnostics
-  void run_groups(std::vector<Group>& gs);
+  // concurrent: the groups of one pass position (disjoint members) on forked streams, so
+  // that each launch's last wave overlaps the others' (untimed runs only)
+  void run_groups(std::vector<Group>& gs, bool concurrent = false);
   std::vector<Propagation*> props_;
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
+  std::vector<cudaStream_t> side_;  // forked streams of the concurrent groups
+  std::vector<cudaEvent_t> joins_;  // one per side stream
+  cudaEvent_t fork_ = nullptr;
   bool timing_ = false;
   size_t launches_per_step_ = 0;
   struct Timed {

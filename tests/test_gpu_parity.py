@@ -186,6 +186,52 @@ def test_fft_pair_pass_matches_general_pass(nr, nth, monkeypatch):
     assert abs(fused.norm() - general.norm()) < 1e-6
 
 
+@pytest.mark.parametrize("nr,nth", [(512, 32), (1024, 32), (2048, 32), (4096, 32), (8192, 32)])
+def test_fixed_shape_fft_pair_matches_general_shape(nr, nth, monkeypatch):
+    """The fixed-shape FFT-pair kernel (radices, spans, twiddle offsets and strides as
+    compile-time constants, directions folded into the butterflies) performs the same FP32
+    operations in the same order as the general-shape one: the results agree to rounding
+    (in practice bit for bit), single and batched."""
+    ensure_built()
+    import split_operator_gb300 as so
+    from split_operator_gb300 import workloads as W
+    kw = dict(nr=nr, nth=nth, step_no=20, seed=37, precision="fp32_tf32x3")
+    ct = [W.radial_angular_2d(**kw)[0] for _ in range(2)]
+    monkeypatch.setenv("SO_FFT_PAIR_CT", "0")
+    gen = [W.radial_angular_2d(**kw)[0] for _ in range(2)]
+    monkeypatch.delenv("SO_FFT_PAIR_CT")
+    for p in (ct[0], gen[0]):
+        p.set_timing(True)
+        p.steps(6)
+    names_ct = " ".join(k[0] for k in ct[0].kernel_times())
+    names_gen = " ".join(k[0] for k in gen[0].kernel_times())
+    assert "fftpair ct" in names_ct and "fftpair" in names_gen and "fftpair ct" not in names_gen
+    assert rel_l2(ct[0].get_array(), gen[0].get_array()) < 1e-6
+    assert abs(ct[0].norm() - gen[0].norm()) < 1e-7
+    # batched (a batch of one member each: the batched kernels)
+    so.Batch([ct[1]]).steps(6)
+    so.Batch([gen[1]]).steps(6)
+    assert rel_l2(ct[1].get_array(), gen[1].get_array()) < 1e-6
+    np.testing.assert_array_equal(ct[1].get_array(), ct[0].get_array())
+
+
+@pytest.mark.parametrize("nr", [512, 2048, 8192])
+def test_fixed_shape_fft_pair_step_matches_oracle(nr):
+    """The FP32 2-D step with the fixed-shape FFT pair against the FP64 oracle, 3 steps."""
+    ensure_built()
+    from split_operator_gb300 import workloads as W
+    nth = 32
+    kw = dict(nr=nr, nth=nth, step_no=20, seed=41)
+    prop = W.radial_angular_2d(precision="fp32_bf16x6", **kw)[0]
+    prop.set_timing(True)
+    oprop, _ = S.radial_angular_2d(**kw)
+    for k in range(3):
+        prop.steps(1)
+        oprop.step()
+        assert rel_l2(prop.get_array(), oprop.wave_function.array) < 2e-6 * (k + 1)
+    assert any("fftpair ct" in t[0] for t in prop.kernel_times())
+
+
 # ------------------------------------------------------------ lane-matrix operators
 def _unitary(rng, n, count):
     z = rng.standard_normal((count, n, n)) + 1j * rng.standard_normal((count, n, n))
