@@ -12,7 +12,7 @@
 // Treating (re, im) as two real columns, a lane-matrix product is the real GEMM
 // D[M x 2BN] = A[M x n] . B[n x 2BN], A the (zero-padded) matrix, B the tile:
 //   n <= 128: M = 128, BN = 32 (N = 64), A chunks of K = 16
-//   n = 256 : M = 256 as two 128-row halves, BN = 16 (N = 32), A chunks of K = 8; a
+//   n = 256 : M = 256 as two 128-row halves, BN = 16 (N = 32); a
 //             parity-structured Legendre pair as two K = 128 GEMMs (see tc_shape)
 // 3xTF32: A = A_hi + A_lo (split once from the FP64 matrix on the host), B = B_hi +
 // B_lo (split on the fly), both parts tf32-exact, D = A_hi B_hi + A_hi B_lo + A_lo B_hi.
@@ -21,8 +21,8 @@
 //   warps 0-7  load the tile, run the point-wise ops, split it into the B operand,
 //              drain the accumulators, run the ops between / after the matrices,
 //              store, and fold the norms (named barrier 1 among themselves)
-//   warp 8     streams the A chunks of every tile, in order, through kStages
-//              shared-memory stages by bulk TMA (it runs ahead across tiles)
+//   warp 8     streams the A chunks (one MMA K step each) of every tile, in order,
+//              through 2-6 shared-memory stages by bulk TMA (it runs ahead across tiles)
 //   warp 9     issues tcgen05.mma (one lane) as chunks land and the B operand is ready
 // The tensor core truncates its FP32 accumulation, so the A_hi B_hi products go to
 // three TMEM regions a couple of K steps each and the work warps drain the
@@ -42,8 +42,12 @@ namespace so {
 
 namespace {
 
-constexpr int kChunkBytes = 8192;   // one of hi / lo: 128 rows x 16 K or 256 rows x 8 K
-constexpr int kStages = 2;          // A chunk stages (16 KB each) in flight per CTA
+// A chunks: one MMA K step (16 bf16 or 8 tf32 values) of every row of M, per operand slice
+// 4 KB per 128 rows.  The stages share 48 KB: 4 of 12 KB (split-BF16x6, M = 128), 6 of 8 KB
+// (two slices, M = 128), 2 or 3 for M = 256.  Small chunks free their stage after few MMAs,
+// so the next chunk's copy starts early.
+constexpr int kStageBudget = 48 * 1024;
+static_assert(kStageBudget == 12 * 4096, "tc_shape derives the stage count from this budget");
 constexpr int kLboB = 144;          // B: core matrices along K (16 B padding vs 128)
 constexpr uint64_t kWaitLimit = 2000000000ull;  // 2 s per wait
 constexpr int kWorkThreads = 256;               // warps 0-7
@@ -65,7 +69,9 @@ struct TcShape {
   int mh;        // 128-row halves of M
   int bn;        // complex columns per tile
   int nc;        // fp32 columns = MMA N
-  int chunk_k;   // K per A chunk
+  int chunk_k;   // K per A chunk (one MMA K step)
+  int chunk_bytes;  // bytes of one slice of an A chunk (128 rows x chunk_k per M half)
+  int stages;    // A chunk stages in flight
   int nk;        // chunks per matrix
   int ksteps;    // K steps of 8 per matrix
   int reg_cols;  // TMEM columns of one accumulator region (all M halves)
@@ -102,7 +108,9 @@ __host__ __device__ inline TcShape tc_shape(int n, bool par = false, bool bf = f
   s.mh = n == 256 ? 2 : 1;
   s.bn = n == 256 ? 16 : 32;
   s.nc = 2 * s.bn;
-  s.chunk_k = (bf ? 32 : 16) / s.mh;
+  s.chunk_k = s.km;
+  s.chunk_bytes = 4096 * s.mh;  // 128 rows x 32 bytes (16 bf16 or 8 tf32) per M half
+  s.stages = (s.mh == 2 ? 6 : 12) / s.slices;  // kStageBudget / (slices x chunk_bytes)
   s.kdim = s.par ? n / 2 : n;
   s.nk = s.kdim / s.chunk_k;
   s.ksteps = s.kdim / s.km;
@@ -120,8 +128,8 @@ struct TcSmemLayout {
   uint32_t stage0, stage_bytes, bhi, bmid, blo, bars, sbo_b, bhalf, bbytes, total;
 };
 
-// [kStages x A stages (slices x 8 KB each)][B_hi][B_mid (oz)][B_lo][mbarriers: full[kStages],
-// empty[kStages], dbar, freebar, bready, quiet].  With par each B slice holds two K = n/2
+// [stages x A stages (slices x chunk_bytes each)][B_hi][B_mid (oz)][B_lo][mbarriers:
+// full[stages], empty[stages], dbar, freebar, bready, quiet].  With par each B slice holds two K = n/2
 // operands, bhalf bytes apart (the even / odd or sum / difference halves).
 __host__ __device__ inline TcSmemLayout tc_layout(int n, bool par = false, bool bf = false, bool oz = false) {
   const TcShape s = tc_shape(n, par, bf, oz);
@@ -131,12 +139,12 @@ __host__ __device__ inline TcSmemLayout tc_layout(int n, bool par = false, bool 
   L.bbytes = (s.par ? 2u : 1u) * L.bhalf;
   L.bbytes = (L.bbytes + 127u) & ~127u;
   L.stage0 = 0;
-  L.stage_bytes = (uint32_t)s.slices * kChunkBytes;
-  L.bhi = kStages * L.stage_bytes;
+  L.stage_bytes = (uint32_t)(s.slices * s.chunk_bytes);
+  L.bhi = (uint32_t)s.stages * L.stage_bytes;
   L.bmid = L.bhi + L.bbytes;  // (oz only)
   L.blo = (s.oz ? L.bmid : L.bhi) + L.bbytes;
   L.bars = L.blo + L.bbytes;
-  L.total = L.bars + (2 * kStages + 4) * 8;
+  L.total = L.bars + (2 * s.stages + 4) * 8;
   return L;
 }
 
@@ -911,7 +919,7 @@ struct TcParams {
   PassParams p;
   int32_t mat_op[2];      // op indices of the (one or two) lane matrices
   int32_t nmat;
-  const float* images[2]; // A chunk images per matrix: nk x (hi 8 KB, lo 8 KB)
+  const float* images[2]; // A chunk images per matrix: nk x slices x chunk_bytes
   int32_t error_slot;
   int32_t parity[2];          // per matrix: 0 plain; 1 sum / difference rows; 2 even / odd columns
   unsigned long long* trace;  // optional phase timestamps, kTraceSlots per tile (nullptr: off)
@@ -962,8 +970,9 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
                                           const TcSmemLayout L, volatile int* fail) {
   using namespace tc;
   uint64_t* full = reinterpret_cast<uint64_t*>(sm_ptr(sm0 + L.bars));
-  uint64_t* empty = full + kStages;
+  uint64_t* empty = full + S.stages;
   const uint32_t stage_bytes = L.stage_bytes;
+  const int64_t ns = S.stages;
   int64_t cc = 0;  // chunks issued
   bool ok = true;
   for (int64_t gt = blockIdx.x; gt < total && ok && !*fail; gt += gridDim.x) {
@@ -972,8 +981,8 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
     for (int m = 0; m < nmat && ok; ++m) {
       const float* img = r.prm->images[m];
       for (int q = 0; q < S.nk; ++q) {
-        const int s = (int)(cc % kStages);
-        const uint32_t use = (uint32_t)(cc / kStages);
+        const int s = (int)(cc % ns);
+        const uint32_t use = (uint32_t)(cc / ns);
         if (use > 0 && !mbar_poll(&empty[s], (use - 1) & 1u, kWaitLimit)) {
           ok = false;
           break;
@@ -982,7 +991,7 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
         if (r.prm->trace && ct < 8) r.prm->trace[r.tile * kTraceSlots + TR_TMA + ct] = globaltimer_ns();
         mbar_expect_tx(&full[s], stage_bytes);
         bulk_g2s(sm_ptr(sm0 + L.stage0 + (uint32_t)s * stage_bytes),
-                 img + (size_t)q * S.slices * (kChunkBytes / 4), stage_bytes, &full[s]);
+                 img + (size_t)q * S.slices * (S.chunk_bytes / 4), stage_bytes, &full[s]);
         ++cc;
       }
     }
@@ -990,8 +999,8 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
   if (!ok) {
     *fail = 1;
     // let the copies in flight land before the CTA lets go of its shared memory
-    for (int64_t c = cc - kStages < 0 ? 0 : cc - kStages; c < cc; ++c)
-      mbar_poll(&full[c % kStages], (uint32_t)((c / kStages) & 1), kWaitLimit);
+    for (int64_t c = cc - ns < 0 ? 0 : cc - ns; c < cc; ++c)
+      mbar_poll(&full[c % ns], (uint32_t)((c / ns) & 1), kWaitLimit);
   }
 }
 
@@ -1008,8 +1017,9 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
                                         const TcSmemLayout L, uint32_t tmem, volatile int* fail) {
   using namespace tc;
   uint64_t* full = reinterpret_cast<uint64_t*>(sm_ptr(sm0 + L.bars));
-  uint64_t* empty = full + kStages;
-  uint64_t* dbar = full + 2 * kStages;
+  const int64_t ns = S.stages;
+  uint64_t* empty = full + ns;
+  uint64_t* dbar = full + 2 * ns;
   uint64_t* freebar = dbar + 1;
   uint64_t* bready = dbar + 2;
   uint64_t* quiet = dbar + 3;
@@ -1052,10 +1062,10 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
         uint32_t dm0 = tmem;
         const uint32_t dc0 = tmem + (uint32_t)(S.nmain * S.reg_cols);
         for (int t = fs.t0; t < fs.t1; ++t) {
-          const int ks = t & (kpc - 1);  // kpc is 1 or 2
+          const int ks = t & (kpc - 1);  // kpc = 1: every K step its own chunk
           if (ks == 0) {
-            s = (int)(cc % kStages);
-            ok = mbar_poll(&full[s], (uint32_t)((cc / kStages) & 1), kWaitLimit);
+            s = (int)(cc % ns);
+            ok = mbar_poll(&full[s], (uint32_t)((cc / ns) & 1), kWaitLimit);
             if (!ok) break;
             if (trace && (int)(cc - cc_tile) < 8) trace[TR_FULL + (int)(cc - cc_tile)] = globaltimer_ns();
             tc_fence_after();
@@ -1064,7 +1074,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
           const uint32_t first_main = newreg ? 0u : 1u;  // 0: the step starts the region
           const uint32_t first_corr = t == 0 ? 0u : 1u;
           if constexpr (OZ) {
-            constexpr uint64_t kSlice = (uint64_t)(kChunkBytes >> 4);  // descriptor step between A slices
+            const uint64_t kSlice = (uint64_t)(S.chunk_bytes >> 4);  // descriptor step between A slices
             for (int hh = 0; hh < S.mh; ++hh) {
               const uint64_t a0 = ahi + (uint64_t)(hh * S.a_half16), a1 = a0 + kSlice, a2 = a0 + 2 * kSlice;
               const uint64_t bo = (uint64_t)hh * bstep_half;
@@ -1084,11 +1094,11 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
             if constexpr (BF) {
               mma_bf16(dm0 + (uint32_t)(hh * S.nc), ah, bh + bo, idesc, first_main);
               mma_bf16(dc0 + (uint32_t)(hh * S.nc), ah, bl + bo, idesc, first_corr);
-              mma_bf16(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(kChunkBytes >> 4), bh + bo, idesc, 1u);
+              mma_bf16(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(S.chunk_bytes >> 4), bh + bo, idesc, 1u);
             } else {
               mma_tf32(dm0 + (uint32_t)(hh * S.nc), ah, bh + bo, idesc, first_main);
               mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah, bl + bo, idesc, first_corr);
-              mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(kChunkBytes >> 4), bh + bo, idesc, 1u);
+              mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(S.chunk_bytes >> 4), bh + bo, idesc, 1u);
             }
           }
           }
@@ -1201,7 +1211,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   const TcShape S = tc_shape(n, par, BF, OZ);
   const TcSmemLayout L = tc_layout(n, par, BF, OZ);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bars);
-  uint64_t* dbar = bars + 2 * kStages;  // MMAs of a fill completed (the work warps drain)
+  uint64_t* dbar = bars + 2 * S.stages;  // MMAs of a fill completed (the work warps drain)
   uint64_t* freebar = dbar + 1;         // the work warps drained a fill (regions free again)
   uint64_t* bready = dbar + 2;          // the B operand of the next matrix is written
   float* bhi = reinterpret_cast<float*>(sm + L.bhi);  // also the FP32 output staging
@@ -1210,7 +1220,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   unsigned char* blb = sm + L.blo;
 
   if (tid == 0) {
-    for (int k = 0; k < 2 * kStages; ++k) mbar_init(bars + k, 1);  // full[], empty[]
+    for (int k = 0; k < 2 * S.stages; ++k) mbar_init(bars + k, 1);  // full[], empty[]
     mbar_init(dbar, 1);
     mbar_init(freebar, kWorkThreads);
     mbar_init(bready, kWorkThreads);
@@ -1732,14 +1742,14 @@ bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis) {
   return across <= kColtSlots;
 }
 
-// Chunk images of the A operand: rows x kdim values a(r, k); per K chunk 8 KB of high
-// parts then 8 KB of remainders, both exact in the operand format, each in the K-major
+// Chunk images of the A operand: rows x kdim values a(r, k); per K chunk (one MMA K step)
+// chunk_bytes of high parts then chunk_bytes of remainders, both exact in the operand format, each in the K-major
 // core-matrix order (row-group stride sbo_a, K core-matrix stride 128 B).  3xTF32: tf32
 // values in 4-byte words; split-BF16x3: bf16 values in 2-byte halves of the same buffer.
 template <typename F>
 static void tc_images(const TcShape& S, bool bf, F a, std::vector<float>& out) {
   const int rows = 128 * S.mh;
-  out.assign((size_t)S.nk * 2 * (kChunkBytes / 4), 0.0f);
+  out.assign((size_t)S.nk * 2 * (S.chunk_bytes / 4), 0.0f);
   auto tf32 = [](float x) {
     uint32_t b;
     std::memcpy(&b, &x, 4);
@@ -1761,8 +1771,8 @@ static void tc_images(const TcShape& S, bool bf, F a, std::vector<float>& out) {
     return r;
   };
   for (int q = 0; q < S.nk; ++q) {
-    unsigned char* hi = reinterpret_cast<unsigned char*>(out.data() + (size_t)q * 2 * (kChunkBytes / 4));
-    unsigned char* lo = hi + kChunkBytes;
+    unsigned char* hi = reinterpret_cast<unsigned char*>(out.data() + (size_t)q * 2 * (S.chunk_bytes / 4));
+    unsigned char* lo = hi + S.chunk_bytes;
     for (int r = 0; r < rows; ++r)
       for (int kk = 0; kk < S.chunk_k; ++kk) {
         const double v = a(r, q * S.chunk_k + kk);
@@ -1783,14 +1793,14 @@ static void tc_images(const TcShape& S, bool bf, F a, std::vector<float>& out) {
   }
 }
 
-// Split-BF16x6 chunk images: per K chunk three 8 KB slice images s0, s1, s2 (bf16, the same
+// Split-BF16x6 chunk images: per K chunk three slice images s0, s1, s2 (bf16, the same
 // core-matrix order), each row cut at the power of two above its largest magnitude over all
 // of K: a = s0 + s1 + s2 + O(2^-24 max), s_i a multiple of 2^(e-8-8i) with |s_i| <= 2^(e-8i)
 // (see oz_quanta for the B side and why the sums are then exact).
 template <typename F>
 static void tc_images_oz(const TcShape& S, F a, std::vector<float>& out) {
   const int rows = 128 * S.mh;
-  out.assign((size_t)S.nk * 3 * (kChunkBytes / 4), 0.0f);
+  out.assign((size_t)S.nk * 3 * (S.chunk_bytes / 4), 0.0f);
   std::vector<double> q0(rows, 0.0);
   for (int r = 0; r < rows; ++r) {
     double amax = 0.0;
@@ -1806,7 +1816,7 @@ static void tc_images_oz(const TcShape& S, F a, std::vector<float>& out) {
     return (uint16_t)(b >> 16);
   };
   for (int q = 0; q < S.nk; ++q) {
-    unsigned char* base = reinterpret_cast<unsigned char*>(out.data() + (size_t)q * 3 * (kChunkBytes / 4));
+    unsigned char* base = reinterpret_cast<unsigned char*>(out.data() + (size_t)q * 3 * (S.chunk_bytes / 4));
     for (int r = 0; r < rows; ++r) {
       if (q0[r] == 0.0) continue;
       const double qs[3] = {q0[r], std::ldexp(q0[r], -8), std::ldexp(q0[r], -16)};
@@ -1818,7 +1828,7 @@ static void tc_images_oz(const TcShape& S, F a, std::vector<float>& out) {
           const double sv = std::nearbyint(rem / qs[sl]) * qs[sl];
           rem -= sv;
           const uint16_t h = bf16_bits(sv);
-          std::memcpy(base + (size_t)sl * kChunkBytes + off, &h, 2);
+          std::memcpy(base + (size_t)sl * S.chunk_bytes + off, &h, 2);
         }
       }
     }

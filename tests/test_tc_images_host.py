@@ -1,8 +1,8 @@
 """The tensor-core pass's A operands as the library builds them on the host
 (angular_tc_images, angular_tc_parity, angular_tc_parity_images in angular_tc.cu), decoded
 on the CPU with a numpy model of the K-major core-matrix layout the kernel's descriptors
-read: per K chunk 8 KB of high parts then 8 KB of remainders, row group r / 8 at stride
-sbo_a = (chunk_k / kc) 128 B, K core matrix kk / kc at 128 B, row r % 8 at 16 B, element
+read: per K chunk (one MMA K step: 16 bf16 or 8 tf32 values) 4 KB per 128 rows of high
+parts then as many of remainders, row group r / 8 at stride sbo_a = (chunk_k / kc) 128 B, K core matrix kk / kc at 128 B, row r % 8 at 16 B, element
 kk % kc.  A small driver linked with the library's own object files does the packing, so
 what is checked is the product code.  No GPU needed.
 
@@ -17,7 +17,6 @@ import pytest
 from oracle import split_operator_oracle as O
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-CHUNK = 8192
 
 DRIVER = r"""
 #include <cstdio>
@@ -96,9 +95,15 @@ def shape(n, par, bf):
     """The kernel's operand shape for lane extent n: rows, K, K per chunk, K per core row."""
     mh = 2 if n == 256 else 1
     kc = 8 if bf else 4
-    chunk_k = (32 if bf else 16) // mh
+    chunk_k = 16 if bf else 8
     kdim = n // 2 if (par and n == 256) else n
     return 128 * mh, kdim, chunk_k, kc
+
+
+def chunk_bytes(n, bf):
+    """Bytes of one slice of an A chunk: every row of M for one K step."""
+    rows, _, chunk_k, _ = shape(n, False, bf)
+    return rows * chunk_k * (2 if bf else 4)
 
 
 def decode(img, n, par, bf):
@@ -106,6 +111,7 @@ def decode(img, n, par, bf):
     rows, kdim, chunk_k, kc = shape(n, par, bf)
     nk = kdim // chunk_k
     es = 2 if bf else 4
+    CHUNK = chunk_bytes(n, bf)
     assert img.size == nk * 2 * CHUNK
     sbo = (chunk_k // kc) * 128
     r = np.arange(rows)[:, None]
@@ -210,9 +216,10 @@ def test_parity_images_reproduce_the_product(pack, bf, which):
 
 
 def decode_oz(img, n, par):
-    """Split-BF16x6 images: per K chunk three 8 KB bf16 slice images, same core-matrix order."""
+    """Split-BF16x6 images: per K chunk three bf16 slice images, same core-matrix order."""
     rows, kdim, chunk_k, kc = shape(n, par, True)
     nk = kdim // chunk_k
+    CHUNK = chunk_bytes(n, True)
     assert img.size == nk * 3 * CHUNK
     sbo = (chunk_k // kc) * 128
     r = np.arange(rows)[:, None]
