@@ -242,11 +242,27 @@ def run_reference(a):
 
 
 # ------------------------------------------------------------------ GPU leg
-def build_props(a, precision, count=None):
+def build_props(a, precision, count=None, world=1, rank=0):
+    """This rank's propagations.  Batched workload on N > 1 GPUs: the instance list holds N x
+    `instances` seeded instances and each rank takes its shard (longest processing time first
+    by Nr x Ntheta): per-GPU work stays fixed as N grows, with no exchange between ranks."""
     from split_operator_gb300 import workloads as W
     if a.workload == "single":
         return [W.radial_angular_2d(nr=a.nr, nth=a.nth, step_no=10 ** 6, precision=precision)[0]]
-    return W.batched_radial_angular(count or a.instances, precision=precision, step_no=10 ** 6)
+    n = count or a.instances
+    if world > 1:
+        from split_operator_gb300 import shards
+        mine, _ = shards.shard(W.batched_instance_params(n * world), world, rank)
+        return W.batched_radial_angular(len(mine), precision=precision, step_no=10 ** 6, params=mine)
+    return W.batched_radial_angular(n, precision=precision, step_no=10 ** 6)
+
+
+def global_points(a, world, points):
+    """Grid points of the whole job: the full instance list (N > 1, batched), else N replicas."""
+    if world == 1 or a.workload == "single":
+        return points * world
+    from split_operator_gb300 import workloads as W
+    return sum(p["nr"] * p["nth"] for p in W.batched_instance_params(a.instances * world))
 
 
 def roofline_from(times, total_ms):
@@ -283,10 +299,11 @@ def run_ours(a):
     import split_operator_gb300 as so
 
     stream = torch.cuda.Stream()
-    props = build_props(a, a.precision)
+    props = build_props(a, a.precision, world=world, rank=rank)
     for p in props:
         p.set_stream(stream.cuda_stream)
-    points = sum(int(np.prod(p.wave_function_shape())) for p in props)
+    points = sum(int(np.prod(p.wave_function_shape())) for p in props)  # this rank's
+    job_points = global_points(a, world, points)
     single = a.workload == "single"
     batch = None if single else so.Batch(props)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda") if single else None
@@ -349,7 +366,7 @@ def run_ours(a):
     launches = so.launch_count() - n0
     clocks.stop()
     ms_max = allmax(world, ms)
-    value = points * a.steps * world / (ms_max / 1e3)
+    value = job_points * a.steps / (ms_max / 1e3)
     if not single:
         # per-launch breakdown of the same K steps with CUDA events on every batched launch
         ms_t, kt = run_steps(a.steps, True)
@@ -408,7 +425,7 @@ def run_ours(a):
     else:
         batch.get_arrays_ptr(out_ptrs)
     ph.append(time.perf_counter() - t)
-    e2e = {"value": points * e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": points * 16,
+    e2e = {"value": job_points * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": points * 16,
            "d2h_bytes_per_step": points * 16, "steps": e2e_steps,
            "unpipelined_phase_ms": {"set_arrays": ph[0] * 1e3, "steps": ph[1] * 1e3, "get_arrays": ph[2] * 1e3},
            "host_link_gbs": {"h2d": 211, "d2h": 193, "source": "cudaMemcpyAsync of 1 GiB pinned, measured on this "
@@ -524,8 +541,10 @@ def run_ours(a):
             "config": {"workload": workload_name(a), "precision": a.precision, "grid_points": points,
                        "l2": ("inputs larger than L2 (states + tables ~" + f"{points * 24 / 1e9:.1f} GB)")
                        if not single else "flushed before every timed step (256 MiB write, untimed)",
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "global_batch": len(props) * world, "wall_s_timed_region": wall},
+                       "parallelism": ("single GPU" if world == 1 else "replicas" if single else
+                                       "instance shards (longest processing time first by Nr x Ntheta)"),
+                       "global_batch": len(props) * world if single or world == 1 else a.instances * world,
+                       "job_grid_points": job_points, "wall_s_timed_region": wall},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks.summary(), "accuracy_vs_fp64": acc, "autotune": tune, "time_to_ground_state": tgs,
             "passes": [list(t) for t in kt]}

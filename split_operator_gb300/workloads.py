@@ -77,11 +77,13 @@ def batched_instance_params(count=512, seed_base=1000):
     return out
 
 
-def batched_radial_angular(count=512, seed_base=1000, precision="fp32_tf32x3", dt=0.5, step_no=2000):
+def batched_radial_angular(count=512, seed_base=1000, precision="fp32_tf32x3", dt=0.5, step_no=2000, params=None):
     """The batched workload: `count` independent radial x angular propagations of uneven
-    sizes, each with its own seeded potential and initial state (mass 1000)."""
+    sizes, each with its own seeded potential and initial state (mass 1000).  `params`
+    (a sub-list of batched_instance_params, e.g. one rank's shard) replaces the first
+    `count` instances."""
     props = []
-    for prm in batched_instance_params(count, seed_base):
+    for prm in (params if params is not None else batched_instance_params(count, seed_base)):
         p, _ = radial_angular_2d(nr=prm["nr"], nth=prm["nth"], dt=dt, step_no=step_no, seed=prm["seed"],
                                  precision=precision, d=prm["d"], a=prm["a"], re=prm["re"], beta=prm["beta"])
         props.append(p)
