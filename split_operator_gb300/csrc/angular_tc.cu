@@ -608,28 +608,30 @@ __device__ __forceinline__ void store4(unsigned char* bh, unsigned char* bl, uin
 // matrix multiplication by using fast routines of matrix multiplication and its
 // applications", Numer. Algorithms 59 (2012).
 struct OzQ {
-  float q0, q1, q2, i0, i1, i2;  // slice quanta and their reciprocals (powers of two)
+  float s0, s1, s2;  // 1.5 x 2^23 q_i: adding and subtracting one rounds to a multiple of q_i
 };
 
 // quanta of a column whose largest magnitude has the FP32 bits `maxbits`: q0 = 2^(E+1-8)
 // for max in [2^E, 2^(E+1)); columns below 2^-103 (and empty ones) share the smallest
-// quanta whose third slice is still a normal number
+// quanta whose third slice is still a normal number, columns of 2^111 or more (never a
+// finite state's) the largest whose rounding constant is finite
 __device__ __forceinline__ OzQ oz_quanta(uint32_t maxbits) {
   uint32_t e = maxbits >> 23;  // biased exponent of the (non-negative) maximum
-  e = e < 24u ? 24u : (e > 254u ? 254u : e);
-  const uint32_t e0 = e - 7u;  // biased exponent of q0
-  return {__uint_as_float(e0 << 23), __uint_as_float((e0 - 8u) << 23), __uint_as_float((e0 - 16u) << 23),
-          __uint_as_float((254u - e0) << 23), __uint_as_float((262u - e0) << 23),
-          __uint_as_float((270u - e0) << 23)};
+  e = e < 24u ? 24u : (e > 238u ? 238u : e);
+  const uint32_t es = e + 16u;  // biased exponent of 2^23 q0 (q0's is e - 7)
+  return {__uint_as_float((es << 23) | 0x400000u), __uint_as_float(((es - 8u) << 23) | 0x400000u),
+          __uint_as_float(((es - 16u) << 23) | 0x400000u)};
 }
 
-// x -> three bf16 slices (each exact: a bf16 value's FP32 bits end in 16 zero bits)
+// x -> three bf16 slices (each exact: a bf16 value's FP32 bits end in 16 zero bits).  For
+// |x| < 2^22 q, (x + 1.5 2^23 q) - 1.5 2^23 q is x rounded to a multiple of q (to nearest,
+// ties to even): the sum stays in the binade whose spacing is q.  Slice i: |x_i| <= 2^8 q_i.
 __device__ __forceinline__ void oz_split(float x, const OzQ& q, uint32_t& h0, uint32_t& h1, uint32_t& h2) {
-  const float s0 = rintf(x * q.i0) * q.q0;
-  float r = x - s0;
-  const float s1 = rintf(r * q.i1) * q.q1;
-  r -= s1;
-  const float s2 = rintf(r * q.i2) * q.q2;
+  const float s0 = __fsub_rn(__fadd_rn(x, q.s0), q.s0);
+  float r = __fsub_rn(x, s0);
+  const float s1 = __fsub_rn(__fadd_rn(r, q.s1), q.s1);
+  r = __fsub_rn(r, s1);
+  const float s2 = __fsub_rn(__fadd_rn(r, q.s2), q.s2);
   h0 = __float_as_uint(s0) >> 16;
   h1 = __float_as_uint(s1) >> 16;
   h2 = __float_as_uint(s2) >> 16;
