@@ -42,12 +42,11 @@ namespace so {
 
 namespace {
 
-// A chunks: one MMA K step (16 bf16 or 8 tf32 values) of every row of M, per operand slice
-// 4 KB per 128 rows.  The stages share 48 KB: 4 of 12 KB (split-BF16x6, M = 128), 6 of 8 KB
-// (two slices, M = 128), 2 or 3 for M = 256.  Small chunks free their stage after few MMAs,
-// so the next chunk's copy starts early.
+// A chunks: 8 KB per operand slice (128 rows x 32 bf16 / 16 tf32 K values, or 256 rows x
+// half that).  The stages share 48 KB: two of 24 KB for split-BF16x6, three of 16 KB for
+// the two-slice modes.
+constexpr int kChunkBytes = 8192;
 constexpr int kStageBudget = 48 * 1024;
-static_assert(kStageBudget == 12 * 4096, "tc_shape derives the stage count from this budget");
 constexpr int kLboB = 144;          // B: core matrices along K (16 B padding vs 128)
 constexpr uint64_t kWaitLimit = 2000000000ull;  // 2 s per wait
 constexpr int kWorkThreads = 256;               // warps 0-7
@@ -69,7 +68,7 @@ struct TcShape {
   int mh;        // 128-row halves of M
   int bn;        // complex columns per tile
   int nc;        // fp32 columns = MMA N
-  int chunk_k;   // K per A chunk (one MMA K step)
+  int chunk_k;   // K per A chunk
   int chunk_bytes;  // bytes of one slice of an A chunk (128 rows x chunk_k per M half)
   int stages;    // A chunk stages in flight
   int nk;        // chunks per matrix
@@ -108,9 +107,9 @@ __host__ __device__ inline TcShape tc_shape(int n, bool par = false, bool bf = f
   s.mh = n == 256 ? 2 : 1;
   s.bn = n == 256 ? 16 : 32;
   s.nc = 2 * s.bn;
-  s.chunk_k = s.km;
-  s.chunk_bytes = 4096 * s.mh;  // 128 rows x 32 bytes (16 bf16 or 8 tf32) per M half
-  s.stages = (s.mh == 2 ? 6 : 12) / s.slices;  // kStageBudget / (slices x chunk_bytes)
+  s.chunk_k = (bf ? 32 : 16) / s.mh;
+  s.chunk_bytes = kChunkBytes;
+  s.stages = kStageBudget / (kChunkBytes * s.slices);
   s.kdim = s.par ? n / 2 : n;
   s.nk = s.kdim / s.chunk_k;
   s.ksteps = s.kdim / s.km;
@@ -974,8 +973,10 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
   uint64_t* full = reinterpret_cast<uint64_t*>(sm_ptr(sm0 + L.bars));
   uint64_t* empty = full + S.stages;
   const uint32_t stage_bytes = L.stage_bytes;
-  const int64_t ns = S.stages;
+  const int ns = S.stages;
   int64_t cc = 0;  // chunks issued
+  int s = 0;       // its stage (cc mod ns) and the use count of that stage (cc / ns)
+  uint32_t use = 0;
   bool ok = true;
   for (int64_t gt = blockIdx.x; gt < total && ok && !*fail; gt += gridDim.x) {
     const TileRef r = resolve(gt);
@@ -983,8 +984,6 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
     for (int m = 0; m < nmat && ok; ++m) {
       const float* img = r.prm->images[m];
       for (int q = 0; q < S.nk; ++q) {
-        const int s = (int)(cc % ns);
-        const uint32_t use = (uint32_t)(cc / ns);
         if (use > 0 && !mbar_poll(&empty[s], (use - 1) & 1u, kWaitLimit)) {
           ok = false;
           break;
@@ -995,6 +994,10 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
         bulk_g2s(sm_ptr(sm0 + L.stage0 + (uint32_t)s * stage_bytes),
                  img + (size_t)q * S.slices * (S.chunk_bytes / 4), stage_bytes, &full[s]);
         ++cc;
+        if (++s == ns) {
+          s = 0;
+          ++use;
+        }
       }
     }
   }
@@ -1002,7 +1005,7 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
     *fail = 1;
     // let the copies in flight land before the CTA lets go of its shared memory
     for (int64_t c = cc - ns < 0 ? 0 : cc - ns; c < cc; ++c)
-      mbar_poll(&full[c % ns], (uint32_t)((c / ns) & 1), kWaitLimit);
+      mbar_poll(&full[(int)(c % ns)], (uint32_t)((c / ns) & 1), kWaitLimit);
   }
 }
 
@@ -1019,7 +1022,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
                                         const TcSmemLayout L, uint32_t tmem, volatile int* fail) {
   using namespace tc;
   uint64_t* full = reinterpret_cast<uint64_t*>(sm_ptr(sm0 + L.bars));
-  const int64_t ns = S.stages;
+  const int ns = S.stages;
   uint64_t* empty = full + ns;
   uint64_t* dbar = full + 2 * ns;
   uint64_t* freebar = dbar + 1;
@@ -1031,7 +1034,8 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
   const int kpc = S.chunk_k / S.km;  // K steps per chunk
   const uint64_t bstep_half = S.par ? (uint64_t)(L.bhalf >> 4) : 0u;
   int64_t cc = 0;                 // chunks consumed
-  int s = 0;                      // stage of the chunk being consumed
+  int s = 0;                      // stage of the chunk being consumed (cc mod ns)
+  uint32_t fphase = 0;            // its full barrier's phase ((cc / ns) & 1)
   uint64_t ahi = 0;               // A_hi descriptor of the current K step (a chunk may span two fills)
   uint32_t nready = 0, nfree = 0;
   bool ok = true;
@@ -1064,10 +1068,9 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
         uint32_t dm0 = tmem;
         const uint32_t dc0 = tmem + (uint32_t)(S.nmain * S.reg_cols);
         for (int t = fs.t0; t < fs.t1; ++t) {
-          const int ks = t & (kpc - 1);  // kpc = 1: every K step its own chunk
+          const int ks = t & (kpc - 1);  // kpc is 1 or 2
           if (ks == 0) {
-            s = (int)(cc % ns);
-            ok = mbar_poll(&full[s], (uint32_t)((cc / ns) & 1), kWaitLimit);
+            ok = mbar_poll(&full[s], fphase, kWaitLimit);
             if (!ok) break;
             if (trace && (int)(cc - cc_tile) < 8) trace[TR_FULL + (int)(cc - cc_tile)] = globaltimer_ns();
             tc_fence_after();
@@ -1119,6 +1122,10 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
             mma_commit(&empty[s]);
             if (trace && (int)(cc - cc_tile) < 8) trace[TR_MMA + (int)(cc - cc_tile)] = globaltimer_ns();
             ++cc;
+            if (++s == ns) {
+              s = 0;
+              fphase ^= 1u;
+            }
           }
         }
         if (ok) mma_commit(dbar);

@@ -828,29 +828,6 @@ void Engine::export_host(double* host, bool sync, bool copy_engine) {
   if (sync) cuda_check(cudaStreamSynchronize(stream), "export sync");
 }
 
-// Import / export by the SMs straight from / to mapped pinned host memory (no staging, no
-// copy engine): the layout kernels carry the host link.  False when the host range is not
-// mapped or the layout has no direct kernel; the caller then stages.
-bool Engine::import_mapped(const double* host) {
-  const size_t b = points() * 16;
-  const Geometry g = flat_geometry(*this);
-  if (!(identity_perm(perm) || layout_is_transpose2(g))) return false;
-  const char* d = mapped_range(host, b);
-  if (d == nullptr) return false;
-  cuda_check(launch_import(psi.ptr, fp64, reinterpret_cast<const double*>(d), g, stream), "import");
-  return true;
-}
-
-bool Engine::export_mapped(double* host) {
-  const size_t b = points() * 16;
-  const Geometry g = flat_geometry(*this);
-  if (!(identity_perm(perm) || layout_is_transpose2(g))) return false;
-  char* d = mapped_range(host, b);
-  if (d == nullptr) return false;
-  cuda_check(launch_export(reinterpret_cast<double*>(d), psi.ptr, fp64, g, stream), "export");
-  return true;
-}
-
 // The two halves of a staged copy-engine import / export, for callers that order the
 // copies (copy engines) and the layout kernels (SMs) separately.
 void Engine::stage_in(const double* host) {
@@ -2048,45 +2025,7 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
   auto mark = [&](const std::string& what) {
     if (trace) marks.emplace_back(what, std::chrono::duration<double, std::milli>(now() - t0).count());
   };
-  // SO_HOST_PIPE=sm: the layout kernels read and write the mapped pinned host arrays
-  // themselves (the SMs carry the host link, no copy engine, no staging), in the same chunk
-  // order; members whose arrays are not mapped are staged through the copy engines
-  const char* pipe = std::getenv("SO_HOST_PIPE");
-  const bool sm_link = pipe != nullptr && std::strcmp(pipe, "sm") == 0;
   try {
-    if (sm_link) {
-      std::vector<char> mapped_in(m, 0);
-      for (size_t c = 0; c < chunks_.size(); ++c) {
-        Chunk& ch = chunks_[c];
-        if (c > 0) cuda_check(cudaStreamWaitEvent(ch.stream, chunks_[c - 1].in_done, 0), "chunk order");
-        for (size_t i = ch.first; i < ch.first + ch.count; ++i) {
-          props_[i]->engine().flush();
-          mapped_in[i] = props_[i]->engine().import_mapped(in[i]) ? 1 : 0;
-          if (!mapped_in[i]) props_[i]->engine().stage_in(in[i]);
-        }
-        cuda_check(cudaEventRecord(ch.in_done, ch.stream), "chunk event");
-      }
-      for (size_t c = 0; c < chunks_.size(); ++c) {
-        Chunk& ch = chunks_[c];
-        if (c > 0) cuda_check(cudaStreamWaitEvent(ch.stream, chunks_[c - 1].sm_done, 0), "chunk order");
-        for (size_t i = ch.first; i < ch.first + ch.count; ++i) {
-          if (!mapped_in[i]) props_[i]->engine().unstage_in();
-          props_[i]->state_replaced();
-        }
-        ch.batch->steps(n, false, false);
-        cuda_check(cudaEventRecord(ch.sm_done, ch.stream), "chunk event");
-        if (c > 0) cuda_check(cudaStreamWaitEvent(ch.stream, chunks_[c - 1].out_done, 0), "chunk order");
-        for (size_t i = ch.first; i < ch.first + ch.count; ++i) {
-          props_[i]->engine().flush();
-          if (!props_[i]->engine().export_mapped(out[i])) {
-            props_[i]->engine().stage_out();
-            props_[i]->engine().unstage_out(out[i]);
-          }
-        }
-        cuda_check(cudaEventRecord(ch.out_done, ch.stream), "chunk event");
-      }
-      for (Chunk& ch : chunks_) cuda_check(cudaStreamSynchronize(ch.stream), "chunk sync");
-    } else {
     // Copy engines: every chunk's states in (host link H2D), in chunk order; later each
     // chunk's states out (D2H), in chunk order.  SMs, in chunk order: the chunk's layout
     // kernels in, its steps, its layout kernels out.  So chunk c computes while later
@@ -2119,7 +2058,6 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
     for (Chunk& ch : chunks_) {
       cuda_check(cudaStreamSynchronize(ch.stream), "chunk sync");
       mark("chunk done");
-    }
     }
   } catch (...) {
     for (size_t i = 0; i < m; ++i) props_[i]->engine().stream = own[i];

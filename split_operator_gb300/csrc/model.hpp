@@ -163,8 +163,6 @@ class Engine {
   // memory (no SMs busy on the host link, so the copy overlaps kernels of other streams)
   void import_host(const double* host, bool copy_engine = false);
   // import_host / export_host split at the staging buffer: copy engine and SM halves
-  bool import_mapped(const double* host);  // SMs read the mapped host array (false: not mapped)
-  bool export_mapped(double* host);
   void stage_in(const double* host);
   void unstage_in();
   void stage_out();

@@ -135,15 +135,10 @@ def test_single_host_array_ragged_transpose_tiles(so, precision):
     assert np.array_equal(out.numpy().view(np.complex128).reshape(nr, nth), want)
 
 
-@pytest.mark.parametrize("link", ["copy engines", "sm"])
-def test_batch_steps_host_pipeline_equals_separate_calls(so, link, monkeypatch):
+def test_batch_steps_host_pipeline_equals_separate_calls(so):
     """so_batch_steps_host (chunked, overlapped copies) gives the same states and losses as
-    set_arrays + steps + get_arrays, bit for bit; in and out may be the same buffers.  Both
-    host links: copy engines with device staging, and the layout kernels reading and
-    writing the mapped pinned arrays themselves (SO_HOST_PIPE=sm)."""
+    set_arrays + steps + get_arrays, bit for bit; in and out may be the same buffers."""
     torch = pytest.importorskip("torch")
-    if link == "sm":
-        monkeypatch.setenv("SO_HOST_PIPE", "sm")
     from split_operator_gb300 import workloads as W
     shapes = [(256, 32), (512, 64), (128, 128), (256, 256), (512, 32), (256, 64)]
     mk = lambda: [W.radial_angular_2d(nr=nr, nth=nth, step_no=10, seed=400 + k, precision="fp32_tf32x3")[0]

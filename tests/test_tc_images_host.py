@@ -1,8 +1,8 @@
 """The tensor-core pass's A operands as the library builds them on the host
 (angular_tc_images, angular_tc_parity, angular_tc_parity_images in angular_tc.cu), decoded
 on the CPU with a numpy model of the K-major core-matrix layout the kernel's descriptors
-read: per K chunk (one MMA K step: 16 bf16 or 8 tf32 values) 4 KB per 128 rows of high
-parts then as many of remainders, row group r / 8 at stride sbo_a = (chunk_k / kc) 128 B, K core matrix kk / kc at 128 B, row r % 8 at 16 B, element
+read: per K chunk 8 KB of high parts then 8 KB of remainders, row group r / 8 at stride
+sbo_a = (chunk_k / kc) 128 B, K core matrix kk / kc at 128 B, row r % 8 at 16 B, element
 kk % kc.  A small driver linked with the library's own object files does the packing, so
 what is checked is the product code.  No GPU needed.
 
@@ -95,13 +95,13 @@ def shape(n, par, bf):
     """The kernel's operand shape for lane extent n: rows, K, K per chunk, K per core row."""
     mh = 2 if n == 256 else 1
     kc = 8 if bf else 4
-    chunk_k = 16 if bf else 8
+    chunk_k = (32 if bf else 16) // mh
     kdim = n // 2 if (par and n == 256) else n
     return 128 * mh, kdim, chunk_k, kc
 
 
 def chunk_bytes(n, bf):
-    """Bytes of one slice of an A chunk: every row of M for one K step."""
+    """Bytes of one slice of an A chunk (every row of M, chunk_k K values): 8 KB."""
     rows, _, chunk_k, _ = shape(n, False, bf)
     return rows * chunk_k * (2 if bf else 4)
 
