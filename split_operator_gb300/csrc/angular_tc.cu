@@ -308,35 +308,22 @@ __device__ __forceinline__ void build_tile_tabs(const PassParams& p, TileTabs& T
 // Point-wise ops [ob, oe) on the NB values of one lane-axis row j, tile columns
 // c0 .. c0 + NB - 1 (storage indices ix0 .. ix0 + NB - 1): the epilogue layout.
 // rw_val is this row's weight in the row-weight vector rw_ptr (loaded ahead of time).
-// A diagonal along the lane axis and a scale are one factor for the whole row: they are
-// kept as a pending complex factor f of the row (the values in registers times f are the
-// state) and folded into the next per-value product, or applied once at the end.  A norm
-// is |f|^2 times the registers' weighted sum, and a norm with the same column weights as
-// the segment's previous one (flag 2, set on the host) reuses that sum while the registers
-// are unchanged: with the step's damping between two loss checks, two norms and two row
-// multiplies of every value become scalar work per row.
-__device__ __forceinline__ float2 fold_factor(float2 t, float2 f, bool pend) { return pend ? cmulf(t, f) : t; }
-
 template <int NB, int PK = 1>
 __device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T, int ob, int oe, float2 (&v)[NB],
                                           int j, int c0, int64_t ix0, float* acc, const float* rw_ptr,
                                           float rw_val) {
   const Geometry& g = p.g;
-  float2 f = {1.0f, 0.0f};
-  bool pend = false;     // f != 1 is owed to the registers
-  float s_last = 0.0f;   // the registers' column-weighted sum of |v|^2 at the last norm
-  bool have_s = false;   // ... and the registers have not changed since
   for (int oi = ob; oi < oe; ++oi) {
     const DevOp& op = p.ops[oi];
     switch (op.kind) {
       case OP_DIAG1D: {
         if (op.axis == g.sweep_axis) {
-          f = fold_factor(__ldg(reinterpret_cast<const float2*>(op.ptr) + j), f, pend);
-          pend = true;
+          const float2 t = __ldg(reinterpret_cast<const float2*>(op.ptr) + j);
+#pragma unroll
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], t);
         } else {
 #pragma unroll
-          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], fold_factor(tab_t<PK>(T, T.slot[oi], c0 + u), f, pend));
-          pend = have_s = false;
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tab_t<PK>(T, T.slot[oi], c0 + u));
         }
         break;
       }
@@ -348,36 +335,29 @@ __device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T
           for (int q = 0; q < NB / 2; ++q) tv[q] = __ldg(reinterpret_cast<const float4*>(t) + q);
 #pragma unroll
           for (int q = 0; q < NB / 2; ++q) {
-            v[2 * q] = cmulf(v[2 * q], fold_factor(make_float2(tv[q].x, tv[q].y), f, pend));
-            v[2 * q + 1] = cmulf(v[2 * q + 1], fold_factor(make_float2(tv[q].z, tv[q].w), f, pend));
+            v[2 * q] = cmulf(v[2 * q], make_float2(tv[q].x, tv[q].y));
+            v[2 * q + 1] = cmulf(v[2 * q + 1], make_float2(tv[q].z, tv[q].w));
           }
         } else {
           float2 tv[NB];
 #pragma unroll
           for (int u = 0; u < NB; ++u) tv[u] = __ldg(t + u);
 #pragma unroll
-          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], fold_factor(tv[u], f, pend));
+          for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], tv[u]);
         }
-        pend = have_s = false;
         break;
       }
       case OP_SCALE: {
-        const float sc = T.scale[oi];
-        f = pend ? float2{f.x * sc, f.y * sc} : float2{sc, 0.0f};
-        pend = true;
+        const float f = T.scale[oi];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) v[u] = {v[u].x * f, v[u].y * f};
         break;
       }
       case OP_NORM: {
-        float s = s_last;
-        if (!(have_s && (op.flags & 2))) {
-          s = 0.0f;
+        float s = 0.0f;
 #pragma unroll
-          for (int u = 0; u < NB; ++u)
-            s = fmaf(fmaf(v[u].x, v[u].x, v[u].y * v[u].y), tab_w<PK>(T, op.red, c0 + u), s);
-          s_last = s;
-          have_s = true;
-        }
-        if (pend) s *= fmaf(f.x, f.x, f.y * f.y);
+        for (int u = 0; u < NB; ++u)
+          s = fmaf(fmaf(v[u].x, v[u].x, v[u].y * v[u].y), tab_w<PK>(T, op.red, c0 + u), s);
         const float* wr = op.wf[g.sweep_axis];
         acc[op.red] += s * (wr == rw_ptr ? rw_val : __ldg(wr + j));
         break;
@@ -386,39 +366,34 @@ __device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T
         break;
     }
   }
-  if (pend)
-#pragma unroll
-    for (int u = 0; u < NB; ++u) v[u] = cmulf(v[u], f);
 }
 
 // The same ops on two rows ja, jb of the same NB columns (the even / odd epilogue holds rows
 // i and n-1-i): op by op for both rows, so each table's two row loads are in flight together.
-// Each row keeps its own pending factor (fa, fb); see apply_row.
 template <int NB>
 __device__ __forceinline__ void apply_row2(const PassParams& p, const TileTabs& T, int ob, int oe, float2 (&va)[NB],
                                            float2 (&vb)[NB], int ja, int jb, int c0, int64_t ixa, int64_t ixb,
                                            float* acc, const float* rw_ptr, float rwa, float rwb) {
   const Geometry& g = p.g;
-  float2 fa = {1.0f, 0.0f}, fb = {1.0f, 0.0f};
-  bool pend = false;
-  float sla = 0.0f, slb = 0.0f;
-  bool have_s = false;
   for (int oi = ob; oi < oe; ++oi) {
     const DevOp& op = p.ops[oi];
     switch (op.kind) {
       case OP_DIAG1D: {
         if (op.axis == g.sweep_axis) {
-          fa = fold_factor(__ldg(reinterpret_cast<const float2*>(op.ptr) + ja), fa, pend);
-          fb = fold_factor(__ldg(reinterpret_cast<const float2*>(op.ptr) + jb), fb, pend);
-          pend = true;
+          const float2 ta = __ldg(reinterpret_cast<const float2*>(op.ptr) + ja);
+          const float2 tb = __ldg(reinterpret_cast<const float2*>(op.ptr) + jb);
+#pragma unroll
+          for (int u = 0; u < NB; ++u) {
+            va[u] = cmulf(va[u], ta);
+            vb[u] = cmulf(vb[u], tb);
+          }
         } else {
 #pragma unroll
           for (int u = 0; u < NB; ++u) {
             const float2 t = T.colt[T.slot[oi]][c0 + u];
-            va[u] = cmulf(va[u], fold_factor(t, fa, pend));
-            vb[u] = cmulf(vb[u], fold_factor(t, fb, pend));
+            va[u] = cmulf(va[u], t);
+            vb[u] = cmulf(vb[u], t);
           }
-          pend = have_s = false;
         }
         break;
       }
@@ -434,46 +409,36 @@ __device__ __forceinline__ void apply_row2(const PassParams& p, const TileTabs& 
           }
 #pragma unroll
           for (int q = 0; q < NB / 2; ++q) {
-            va[2 * q] = cmulf(va[2 * q], fold_factor(make_float2(qa[q].x, qa[q].y), fa, pend));
-            va[2 * q + 1] = cmulf(va[2 * q + 1], fold_factor(make_float2(qa[q].z, qa[q].w), fa, pend));
-            vb[2 * q] = cmulf(vb[2 * q], fold_factor(make_float2(qb[q].x, qb[q].y), fb, pend));
-            vb[2 * q + 1] = cmulf(vb[2 * q + 1], fold_factor(make_float2(qb[q].z, qb[q].w), fb, pend));
+            va[2 * q] = cmulf(va[2 * q], make_float2(qa[q].x, qa[q].y));
+            va[2 * q + 1] = cmulf(va[2 * q + 1], make_float2(qa[q].z, qa[q].w));
+            vb[2 * q] = cmulf(vb[2 * q], make_float2(qb[q].x, qb[q].y));
+            vb[2 * q + 1] = cmulf(vb[2 * q + 1], make_float2(qb[q].z, qb[q].w));
           }
         } else {
 #pragma unroll
           for (int u = 0; u < NB; ++u) {
-            va[u] = cmulf(va[u], fold_factor(__ldg(ta + u), fa, pend));
-            vb[u] = cmulf(vb[u], fold_factor(__ldg(tb + u), fb, pend));
+            va[u] = cmulf(va[u], __ldg(ta + u));
+            vb[u] = cmulf(vb[u], __ldg(tb + u));
           }
         }
-        pend = have_s = false;
         break;
       }
       case OP_SCALE: {
-        const float sc = T.scale[oi];
-        fa = pend ? float2{fa.x * sc, fa.y * sc} : float2{sc, 0.0f};
-        fb = pend ? float2{fb.x * sc, fb.y * sc} : float2{sc, 0.0f};
-        pend = true;
+        const float f = T.scale[oi];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+          va[u] = {va[u].x * f, va[u].y * f};
+          vb[u] = {vb[u].x * f, vb[u].y * f};
+        }
         break;
       }
       case OP_NORM: {
-        float sa = sla, sb = slb;
-        if (!(have_s && (op.flags & 2))) {
-          sa = 0.0f;
-          sb = 0.0f;
+        float sa = 0.0f, sb = 0.0f;
 #pragma unroll
-          for (int u = 0; u < NB; ++u) {
-            const float w = T.colw[op.red][c0 + u];
-            sa = fmaf(fmaf(va[u].x, va[u].x, va[u].y * va[u].y), w, sa);
-            sb = fmaf(fmaf(vb[u].x, vb[u].x, vb[u].y * vb[u].y), w, sb);
-          }
-          sla = sa;
-          slb = sb;
-          have_s = true;
-        }
-        if (pend) {
-          sa *= fmaf(fa.x, fa.x, fa.y * fa.y);
-          sb *= fmaf(fb.x, fb.x, fb.y * fb.y);
+        for (int u = 0; u < NB; ++u) {
+          const float w = T.colw[op.red][c0 + u];
+          sa = fmaf(fmaf(va[u].x, va[u].x, va[u].y * va[u].y), w, sa);
+          sb = fmaf(fmaf(vb[u].x, vb[u].x, vb[u].y * vb[u].y), w, sb);
         }
         const float* wr = op.wf[g.sweep_axis];
         const bool pre = wr == rw_ptr;
@@ -485,12 +450,6 @@ __device__ __forceinline__ void apply_row2(const PassParams& p, const TileTabs& 
         break;
     }
   }
-  if (pend)
-#pragma unroll
-    for (int u = 0; u < NB; ++u) {
-      va[u] = cmulf(va[u], fa);
-      vb[u] = cmulf(vb[u], fb);
-    }
 }
 
 // Point-wise ops [ob, oe) on the NB values of one tile column c, lane-axis rows
@@ -1663,17 +1622,6 @@ void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const floa
     tp.parity[i] = parity ? parity[i] : 0;
   }
   tp.error_slot = error_slot;
-  // norms with the column weights of the pass's previous norm (every non-lane axis the same
-  // weights): flag 2, so the epilogue may reuse that norm's per-row sum (see apply_row)
-  for (int oi = 0, prev = -1; oi < tp.p.nops; ++oi) {
-    DevOp& op = tp.p.ops[oi];
-    if (op.kind != OP_NORM) continue;
-    bool same = prev >= 0;
-    for (int a = 0; same && a < tp.p.g.ndim; ++a)
-      if (a != tp.p.g.sweep_axis) same = op.wf[a] == tp.p.ops[prev].wf[a];
-    op.flags = same ? (op.flags | 2) : (op.flags & ~2);
-    prev = oi;
-  }
   // the distinct full-size tables after the first matrix (the kernel prefetches their tile rows)
   for (int oi = nmat > 0 ? mat_op[0] + 1 : p.nops; oi < p.nops && tp.npre < 4; ++oi) {
     if (p.ops[oi].kind != OP_DIAGND) continue;
