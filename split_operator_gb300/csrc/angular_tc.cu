@@ -927,6 +927,11 @@ struct TcParams {
   int32_t pack;               // column groups per tile (1; or 128 / n packed, images block-diagonal)
   int32_t npre;               // distinct full-size tables read after the first matrix (prefetched per tile)
   const void* pre[4];
+  int32_t slice_axis[2];      // state matrix: the logical axis whose coordinate picks the image (-1: one image)
+  int64_t slice_stride[2];    // floats between two coordinates' images
+  // ... the tile's coordinate along it: ((tile mod pre) / div) mod ext (pre 0: no first mod),
+  // 32-bit arithmetic worked out on the host (tiles of a pass < 2^32)
+  uint32_t slice_pre[2], slice_div[2], slice_ext[2];
 };
 
 // Phase timestamps (%globaltimer, ns) of the optional trace, per tile (work thread 0).
@@ -983,6 +988,12 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
     const int nmat = r.prm->nmat;
     for (int m = 0; m < nmat && ok; ++m) {
       const float* img = r.prm->images[m];
+      if (r.prm->slice_axis[m] >= 0) {
+        // a state matrix: the image of the tile's coordinate along the slice axis
+        uint32_t t = (uint32_t)r.tile;
+        if (r.prm->slice_pre[m]) t %= r.prm->slice_pre[m];
+        img += (int64_t)((t / r.prm->slice_div[m]) % r.prm->slice_ext[m]) * r.prm->slice_stride[m];
+      }
       for (int q = 0; q < S.nk; ++q) {
         if (use > 0 && !mbar_poll(&empty[s], (use - 1) & 1u, kWaitLimit)) {
           ok = false;
@@ -1611,15 +1622,38 @@ int angular_tc_columns(int n) { return tc_shape(n).bn; }
 size_t tc_params_bytes() { return sizeof(TcParams); }
 
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
-                    const int* parity, void* out, int pack) {
+                    const int* parity, void* out, int pack, const int* slice_axis, const int64_t* slice_stride) {
   TcParams tp{};
   tp.p = p;
   tp.pack = pack;
   tp.nmat = nmat;
+  tp.slice_axis[0] = tp.slice_axis[1] = -1;
   for (int i = 0; i < nmat; ++i) {
     tp.mat_op[i] = mat_op[i];
     tp.images[i] = images[i];
     tp.parity[i] = parity ? parity[i] : 0;
+    if (slice_axis && slice_axis[i] >= 0) {
+      // the tile's coordinate along the slice axis (storage position q): an outer axis from
+      // the tile's outer index o = tile / tiles_per_outer, an inner one from its first column
+      // i0 = (tile mod tiles_per_outer) x columns (the axis's stride a multiple of columns)
+      const Geometry& g = p.g;
+      int q = 0;
+      for (int a = 0; a < g.ndim; ++a)
+        if (g.perm[a] == slice_axis[i]) q = a;
+      int64_t div = 1;
+      if (q < g.spos) {
+        for (int a = q + 1; a < g.spos; ++a) div *= g.sshape[a];
+        tp.slice_pre[i] = 0;
+        tp.slice_div[i] = (uint32_t)(div * g.tiles_per_outer);
+      } else {
+        for (int a = q + 1; a < g.ndim; ++a) div *= g.sshape[a];
+        tp.slice_pre[i] = (uint32_t)g.tiles_per_outer;
+        tp.slice_div[i] = (uint32_t)(div / g.lanes_per_tile);
+      }
+      tp.slice_ext[i] = (uint32_t)g.sshape[q];
+      tp.slice_axis[i] = slice_axis[i];
+      tp.slice_stride[i] = slice_stride[i];
+    }
   }
   tp.error_slot = error_slot;
   // the distinct full-size tables after the first matrix (the kernel prefetches their tile rows)
@@ -1751,8 +1785,8 @@ bool angular_tc_ops_fit(const DevOp* ops, int nops, int sweep_axis) {
   return across <= kColtSlots;
 }
 
-// Chunk images of the A operand: rows x kdim values a(r, k); per K chunk (one MMA K step)
-// chunk_bytes of high parts then chunk_bytes of remainders, both exact in the operand format, each in the K-major
+// Chunk images of the A operand: rows x kdim values a(r, k); per K chunk chunk_bytes of
+// high parts then chunk_bytes of remainders, both exact in the operand format, each in the K-major
 // core-matrix order (row-group stride sbo_a, K core-matrix stride 128 B).  3xTF32: tf32
 // values in 4-byte words; split-BF16x3: bf16 values in 2-byte halves of the same buffer.
 template <typename F>
@@ -1935,18 +1969,11 @@ cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_ou
 
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
                               int error_slot, const int* parity, int mode, cudaStream_t s,
-                              unsigned long long* trace, int ctas_per_sm, int pack) {
-  TcParams tp{};
+                              unsigned long long* trace, int ctas_per_sm, int pack, const int* slice_axis,
+                              const int64_t* slice_stride) {
+  TcParams tp;
+  make_tc_params(p, mat_op, nmat, images, error_slot, parity, &tp, pack, slice_axis, slice_stride);
   tp.trace = trace;
-  tp.p = p;
-  tp.pack = pack;
-  tp.nmat = nmat;
-  for (int i = 0; i < nmat; ++i) {
-    tp.mat_op[i] = mat_op[i];
-    tp.images[i] = images[i];
-    tp.parity[i] = parity ? parity[i] : 0;
-  }
-  tp.error_slot = error_slot;
   const int v = tc_variant(mode, pack);
   if (v < 0) return cudaErrorInvalidValue;
   const size_t smem = angular_tc_smem_bytes((int)p.g.n * pack, tp.parity[0] != 0, mode);

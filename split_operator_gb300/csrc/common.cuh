@@ -196,7 +196,8 @@ void angular_tc_parity_images(const double* m, int n, int kind, int mode, std::v
 // per-tile phase timestamps (angular_tc_trace_slots() per tile), nullptr: off
 cudaError_t launch_angular_tc(const PassParams& p, const int* mat_op, int nmat, const float* const* images,
                               int error_slot, const int* parity, int mode, cudaStream_t s,
-                              unsigned long long* trace = nullptr, int ctas_per_sm = 0, int pack = 1);
+                              unsigned long long* trace = nullptr, int ctas_per_sm = 0, int pack = 1,
+                              const int* slice_axis = nullptr, const int64_t* slice_stride = nullptr);
 int angular_tc_trace_slots();
 // one CTA waits (limit_ns, both wait forms) on an mbarrier nothing completes; out[3]:
 // timed out (try_wait form), timed out (polling form), elapsed ns
@@ -210,8 +211,11 @@ cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassPar
 int fft_pair_ct_lgn(const PassParams& p, bool fp64);
 size_t tc_params_bytes();
 void tc_params_set_trace(void* params, unsigned long long* trace);  // the TcParams' trace field
+// slice_axis[m] >= 0: matrix m is a state matrix, one image per coordinate of that logical
+// axis, slice_stride[m] floats apart (the coordinate is constant over every tile)
 void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const float* const* images, int error_slot,
-                    const int* parity, void* out, int pack = 1);
+                    const int* parity, void* out, int pack = 1, const int* slice_axis = nullptr,
+                    const int64_t* slice_stride = nullptr);
 // persistent CTAs a launch of `tiles` tensor-core tiles runs on (CTA k takes the tiles at
 // positions k, k + grid, k + 2 grid, ... of the owners table)
 int64_t angular_tc_grid(int64_t tiles, int ctas_per_sm = 0);

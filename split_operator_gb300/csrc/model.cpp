@@ -337,6 +337,23 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
     else
       tc_parity_by_matrix_.erase(c.buf.ptr);
   }
+  if (!fp64 && tc_mode() >= 0 && real && count > 1 && (n == 32 || n == 64 || n == 128 || n == 256)) {
+    // state matrices (one per coordinate of a dependent axis): every matrix's images one
+    // after another; a tensor-core tile takes the image of its coordinate
+    std::vector<float> all, h;
+    std::vector<double> md(n * n);
+    int64_t stride = 0;
+    for (size_t b = 0; b < count; ++b) {
+      for (size_t i = 0; i < n * n; ++i) md[i] = m[b * n * n + i].real();
+      angular_tc_images(md.data(), (int)n, tc_mode(), h);
+      stride = (int64_t)h.size();
+      all.insert(all.end(), h.begin(), h.end());
+    }
+    upload(c.tc_slice_images, all, stream);
+    tc_slice_by_matrix_[c.buf.ptr] = {c.tc_slice_images.as<float>(), stride};
+  } else {
+    tc_slice_by_matrix_.erase(c.buf.ptr);
+  }
   return c.buf.ptr;
 }
 
@@ -389,14 +406,40 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
   if (!angular_tc_eligible(g)) return false;
   int mats[2], nmat = 0;
   const float* images[2] = {nullptr, nullptr};
+  int slice_axis[2] = {-1, -1};
+  int64_t slice_stride[2] = {0, 0};
+  bool sliced = false;
+  const int bn0 = angular_tc_columns((int)g.n);
   for (size_t i = 0; i < ops.size(); ++i) {
     const int k = ops[i].kind;
-    if (k == OP_FFT || k == OP_MAT_LANE || k == OP_MAT_SLICE || k == OP_DOT) return false;
+    if (k == OP_FFT || k == OP_MAT_LANE || k == OP_DOT) return false;
     if (k == OP_MAT) {
       if (nmat == 2 || !(ops[i].flags & 1)) return false;
       auto it = tc_images_by_matrix_.find(ops[i].ptr);
       if (it == tc_images_by_matrix_.end()) return false;
       images[nmat] = it->second;
+      mats[nmat++] = (int)i;
+    } else if (k == OP_MAT_SLICE) {
+      // a state matrix: one matrix per coordinate of the dependent axis, which must be
+      // constant over every tile (an outer axis, or an inner one whose stride is a multiple
+      // of the tile's columns), with a matrix for every coordinate
+      if (nmat == 2 || !(ops[i].flags & 1)) return false;
+      auto it = tc_slice_by_matrix_.find(ops[i].ptr);
+      if (it == tc_slice_by_matrix_.end()) return false;
+      const int dep = ops[i].axis;
+      int q = -1;
+      for (int a = 0; a < g.ndim; ++a)
+        if (g.perm[a] == dep) q = a;
+      if (q < 0 || q == g.spos || ops[i].count < g.sshape[q]) return false;
+      if (q > g.spos) {
+        int64_t stride = 1;
+        for (int a = q + 1; a < g.ndim; ++a) stride *= g.sshape[a];
+        if (stride % bn0 != 0) return false;
+      }
+      images[nmat] = it->second.first;
+      slice_axis[nmat] = dep;
+      slice_stride[nmat] = it->second.second;
+      sliced = true;
       mats[nmat++] = (int)i;
     }
   }
@@ -405,7 +448,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
   // difference matrix follows anything but an even / odd one (SO_TC_PARITY=0 turns it off)
   int parity[2] = {0, 0};
   const char* par_env = std::getenv("SO_TC_PARITY");
-  bool par = g.n == 256 && !(par_env && par_env[0] == '0');
+  bool par = g.n == 256 && !sliced && !(par_env && par_env[0] == '0');
   for (int m = 0; m < nmat && par; ++m) {
     auto it = tc_parity_by_matrix_.find(ops[mats[m]].ptr);
     if (it == tc_parity_by_matrix_.end()) {
@@ -421,7 +464,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     parity[0] = parity[1] = 0;
   }
   // packed tiles for short lanes: 128 / n column groups per tile, block-diagonal images
-  int pk = par ? 1 : angular_tc_pack(g, ops.data(), (int)ops.size(), tc_mode());
+  int pk = par || sliced ? 1 : angular_tc_pack(g, ops.data(), (int)ops.size(), tc_mode());
   if (pk > 1) {
     const float* pim[2] = {nullptr, nullptr};
     for (int m = 0; m < nmat && pk > 1; ++m) {
@@ -456,7 +499,7 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
                    (int)g.n | (par ? 1 << 16 : 0) | (tc_mode() << 17) | ((sched.ctas_per_sm & 3) << 20) |
                        (sched.blocked ? 1 << 22 : 0) | ((pk == 4 ? 2 : pk == 2 ? 1 : 0) << 23),
                    angular_tc_smem_bytes((int)g.n * pk, par, tc_mode()), name, pass_bytes(ops, g)};
-    make_tc_params(p, mats, nmat, images, timeout_slot, parity, r.tcp.data(), pk);
+    make_tc_params(p, mats, nmat, images, timeout_slot, parity, r.tcp.data(), pk, slice_axis, slice_stride);
     recording->push_back(std::move(r));
     return true;
   }
@@ -472,7 +515,8 @@ bool Engine::try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& 
     cuda_check(cudaMemsetAsync(trace.ptr, 0, trace.bytes, stream), "trace clear");
   }
   cuda_check(launch_angular_tc(p, mats, nmat, images, timeout_slot, parity, tc_mode(), stream,
-                               trace_path ? trace.as<unsigned long long>() : nullptr, sched.ctas_per_sm, pk),
+                               trace_path ? trace.as<unsigned long long>() : nullptr, sched.ctas_per_sm, pk,
+                               slice_axis, slice_stride),
              "tensor-core pass launch");
   if (trace_path) {
     std::vector<unsigned long long> h(trace.bytes / sizeof(unsigned long long));

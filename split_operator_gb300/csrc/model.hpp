@@ -206,11 +206,13 @@ class Engine {
     // the same values (all propagations on one polar grid), so one copy stays hot in L2
     std::shared_ptr<DeviceBuffer> tc_images, tc_par_images;
     std::shared_ptr<DeviceBuffer> tc_pack_images;  // block-diagonal 128 x 128 form (packed tiles of n < 128)
+    DeviceBuffer tc_slice_images;                  // state matrices: every matrix's images, one after another
   };
   std::map<std::pair<const void*, int>, Cached> tables_;
   std::map<const void*, const float*> tc_images_by_matrix_;
   std::map<const void*, const float*> tc_pack_by_matrix_;
   std::map<const void*, std::pair<int, const float*>> tc_parity_by_matrix_;  // parity kind, split images
+  std::map<const void*, std::pair<const float*, int64_t>> tc_slice_by_matrix_;  // images, floats per matrix
   bool try_launch_tc(const std::vector<DevOp>& ops, int axis, PassParams& p);
   static void shared_tc_images(const std::vector<double>& md, int n, int mode, cudaStream_t s,
                                std::shared_ptr<DeviceBuffer>& img, std::shared_ptr<DeviceBuffer>& par, int& kind);

@@ -66,6 +66,27 @@ def test_associated_legendre_operator_propagation_matches_oracle(so, precision, 
     assert abs(prop.norm() - oprop.wave_function.norm()) < tol * steps
 
 
+@pytest.mark.parametrize("precision,tol", [("fp32_bf16x6", 2e-6), ("fp32_tf32x3", 2e-6)])
+def test_associated_legendre_operator_on_tensor_cores_matches_oracle(so, precision, tol):
+    """The state-matrix transformation (one P_l^Omega matrix per Omega) as a grouped GEMM on
+    the tensor cores: every tile's columns share one Omega, and the tile streams that
+    Omega's operand images (state_matrix_transformation.rs:48-73,
+    legendre_diagonalization.rs:83-109)."""
+    nr, nth, nom, steps = 128, 64, 3, 4
+    wf, tg, st = _radial_polar_omega(so, nr, nth, nom, 50.0, 0.2)
+    owf, otg, ost = _radial_polar_omega(O, nr, nth, nom, 50.0, 0.2)
+    prop = so.Propagation(wf, tg, st, precision)
+    oprop = O.Propagation(owf, otg, ost)
+    prop.set_timing(True)
+    for k in range(steps):
+        prop.steps(1)
+        oprop.step()
+        assert rel_l2(prop.get_array(), oprop.wave_function.array) < tol * (k + 1), k
+    assert abs(prop.norm() - oprop.wave_function.norm()) < tol * steps
+    names = " ".join(t[0] for t in prop.kernel_times())
+    assert ("tcbf16x6" if precision == "fp32_bf16x6" else "tc3xtf32") in names and "mat_slice" in names, names
+
+
 def _radial_polar_fixed_omega(lib, nr, nth, omega, mass, dt):
     radial = lib.Grid.new_linear_continuos("radial", 1.0, 30.0, nr, 0)
     x, w = np.polynomial.legendre.leggauss(nth)
