@@ -2124,7 +2124,7 @@ std::string Batch::tune(const std::string& cache_path, int trial_steps) {
       if (r.kind == RecordedPass::TensorCore) {
         const int mode = (r.threads >> 17) & 3;
         // (CTAs per SM, blocked order); the first candidate is the built-in default
-        cands[{1, r.p.g.n, mode}] = {{2, 0}, {2, 1}, {1, 0}, {1, 1}};
+        cands[{1, r.p.g.n, mode}] = {{2, 1}, {2, 0}, {1, 1}, {1, 0}};
       } else if (r.kind == RecordedPass::Generic && r.p.fused && !r.fp64) {
         // (threads per CTA, radix); lanes of n points need 16 threads >= n
         std::vector<std::pair<int, int>> v{{fft_pair_threads(r.p.g), 16}};

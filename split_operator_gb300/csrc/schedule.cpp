@@ -34,7 +34,8 @@ PairSchedule pair_schedule(int64_t n, bool fp64) {
 TcSchedule tc_schedule(int64_t n, int mode) {
   std::lock_guard<std::mutex> l(g_mu);
   auto it = g_tc.find({n, mode});
-  return it == g_tc.end() ? TcSchedule{0, 0} : it->second;
+  // built in: the default CTAs per SM, blocked tile order (runs of one member's tiles)
+  return it == g_tc.end() ? TcSchedule{0, 1} : it->second;
 }
 
 void set_pair_schedule(int64_t n, bool fp64, PairSchedule s) {
