@@ -1827,7 +1827,9 @@ void Batch::run_groups(std::vector<Group>& gs, bool concurrent) {
   // the members of a position's groups are disjoint, so the groups may run side by side: the
   // largest first on the batch stream, the others on forked streams joined before the next
   // position (the results are those of the sequential order: no member is touched twice)
-  const bool fork = concurrent && !timing_ && gs.size() > 1;
+  // SO_BATCH_SERIAL=1: every group on the batch stream, one after another (for comparison)
+  const char* serial = std::getenv("SO_BATCH_SERIAL");
+  const bool fork = concurrent && !timing_ && gs.size() > 1 && !(serial && serial[0] == '1');
   std::vector<size_t> order(gs.size());
   for (size_t k = 0; k < gs.size(); ++k) order[k] = k;
   if (fork) {
