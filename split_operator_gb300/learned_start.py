@@ -349,7 +349,7 @@ def time_to_ground_state(model_path=MODEL_2048x64, count=16, first=0, every=5, m
                                max_steps=max_steps, target=e_star)
     wall_l += t_predict
     return {"heldout_sets": [first, first + count], "grid": [g.nr, g.nth], "tolerance": 1e-8,
-            "judge": "E* of the plain FP64 imaginary-time solver run to |dE| <= 1e-10", "e_star_s": t_star,
+            "criterion": "E* of the plain FP64 imaginary-time solver run to |dE| <= 1e-10", "e_star_s": t_star,
             "wall_s_gaussian": wall_g, "wall_s_learned": wall_l, "predict_s": t_predict,
             "wall_ratio_learned_over_gaussian": wall_l / wall_g,
             "steps_gaussian_mean": float(np.mean(steps_g)), "steps_learned_mean": float(np.mean(steps_l)),
