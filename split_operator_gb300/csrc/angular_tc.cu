@@ -1151,6 +1151,89 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
   }
 }
 
+// Warp 9, lane 0, split-BF16x6: the same schedule as mma_issuer with its invariants in
+// registers and the loops over the K steps of a chunk and the M halves unrolled (MH = 1:
+// chunks of two K steps; MH = 2: one), so the lane spends its time issuing products rather
+// than recomputing descriptors (a probe measured the product issue itself at ~51 cycles).
+template <int MH, typename Resolve>
+__device__ __noinline__ void mma_issuer_oz(Resolve resolve, int64_t total, const TcShape S, uint32_t sm0,
+                                           const TcSmemLayout L, uint32_t tmem, volatile int* fail) {
+  using namespace tc;
+  constexpr int KPC = MH == 1 ? 2 : 1;  // K steps per chunk
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm_ptr(sm0 + L.bars));
+  const int ns = S.stages;
+  uint64_t* empty = full + ns;
+  uint64_t* dbar = full + 2 * ns;
+  uint64_t* bready = dbar + 2;
+  uint64_t* quiet = dbar + 3;
+  const uint32_t idesc = idesc_bf16(128, (uint32_t)S.nc);
+  const uint64_t bbits = smem_desc_bits(kLboB, L.sbo_b), abits = smem_desc_bits(128, (uint32_t)S.sbo_a);
+  const uint64_t b0 = smem_desc_at(bbits, sm0 + L.bhi), b1 = smem_desc_at(bbits, sm0 + L.bmid),
+                 b2 = smem_desc_at(bbits, sm0 + L.blo);
+  const uint64_t a_first = smem_desc_at(abits, sm0 + L.stage0), a_stage = (uint64_t)(L.stage_bytes >> 4);
+  const uint64_t slice = (uint64_t)(S.chunk_bytes >> 4), ahalf = (uint64_t)S.a_half16;
+  const uint64_t bhalf = S.par ? (uint64_t)(L.bhalf >> 4) : 0u;
+  constexpr uint64_t kBStep = (uint64_t)(2 * kLboB >> 4), kAStep = (uint64_t)(256 >> 4);
+  const uint32_t rc = (uint32_t)S.reg_cols, nch = (uint32_t)S.nc;
+  const int ksteps = S.ksteps;
+  int64_t cc = 0;
+  int s = 0;
+  uint32_t fphase = 0, nready = 0;
+  bool ok = true;
+  for (int64_t gt = blockIdx.x; gt < total && ok; gt += gridDim.x) {
+    const TileRef tr = resolve(gt);
+    const int nmat = tr.prm->nmat;
+    unsigned long long* trace = tr.prm->trace ? tr.prm->trace + tr.tile * kTraceSlots : nullptr;
+    const int64_t cc_tile = cc;
+    for (int m = 0; m < nmat && ok; ++m) {
+      ok = mbar_poll(bready, nready & 1u, kWaitLimit);
+      ++nready;
+      tc_fence_after();
+      uint64_t bh = b0, bm = b1, bl = b2;
+      for (int t = 0; t < ksteps && ok; t += KPC) {
+        ok = mbar_poll(&full[s], fphase, kWaitLimit);
+        if (!ok) break;
+        if (trace && (int)(cc - cc_tile) < 8) trace[TR_FULL + (int)(cc - cc_tile)] = globaltimer_ns();
+        tc_fence_after();
+        uint64_t a = a_first + (uint64_t)s * a_stage;
+#pragma unroll
+        for (int kk = 0; kk < KPC; ++kk) {
+          const uint32_t acc = (t + kk) > 0 ? 1u : 0u;
+#pragma unroll
+          for (int hh = 0; hh < MH; ++hh) {
+            const uint64_t a0 = a + (uint64_t)hh * ahalf, bo = (uint64_t)hh * bhalf;
+            const uint32_t r0 = tmem + (uint32_t)hh * nch;
+            mma_bf16(r0, a0, bh + bo, idesc, acc);
+            mma_bf16(r0 + rc, a0, bm + bo, idesc, acc);
+            mma_bf16(r0 + rc, a0 + slice, bh + bo, idesc, 1u);
+            mma_bf16(r0 + 2u * rc, a0, bl + bo, idesc, acc);
+            mma_bf16(r0 + 2u * rc, a0 + slice, bm + bo, idesc, 1u);
+            mma_bf16(r0 + 2u * rc, a0 + 2u * slice, bh + bo, idesc, 1u);
+          }
+          bh += kBStep;
+          bm += kBStep;
+          bl += kBStep;
+          a += kAStep;
+        }
+        mma_commit(&empty[s]);
+        if (trace && (int)(cc - cc_tile) < 8) trace[TR_MMA + (int)(cc - cc_tile)] = globaltimer_ns();
+        ++cc;
+        if (++s == ns) {
+          s = 0;
+          fphase ^= 1u;
+        }
+      }
+      if (ok) mma_commit(dbar);
+    }
+  }
+  if (!ok) {
+    *fail = 1;
+    // every MMA already issued completes before the tensor memory is released
+    mma_commit(quiet);
+    mbar_poll(quiet, 0u, kWaitLimit);
+  }
+}
+
 // The tiles blockIdx.x, blockIdx.x + gridDim.x, ... of a launch (every tile of a launch
 // has the same lane extent n).
 // PK > 1: packed tiles of lane extent 128 / PK (see tab_w): the tensor core sees one
@@ -1259,7 +1342,16 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   if (warp == kWorkThreads / 32) {
     if (lane == 0) tma_producer(resolve, total, S, sm0, L, &s_fail);
   } else if (warp == kWorkThreads / 32 + 1) {
-    if (lane == 0) mma_issuer<BF, OZ>(resolve, total, S, sm0, L, tmem, &s_fail);
+    if (lane == 0) {
+      if constexpr (OZ) {
+        if (S.mh == 2)
+          mma_issuer_oz<2>(resolve, total, S, sm0, L, tmem, &s_fail);
+        else
+          mma_issuer_oz<1>(resolve, total, S, sm0, L, tmem, &s_fail);
+      } else {
+        mma_issuer<BF, OZ>(resolve, total, S, sm0, L, tmem, &s_fail);
+      }
+    }
   } else {
     // ================= work warps
     const int lg = warp & 3, up = warp >> 2;
