@@ -1024,11 +1024,9 @@ __device__ __noinline__ void tma_producer(Resolve resolve, int64_t total, const 
 // fill, the K steps of the fill -- step t puts A_hi B_hi into main region
 // (t - t0) nused / span and both corrections into the correction region -- then a
 // commit of the fill to dbar.  Each chunk's MMAs are committed to its stage's empty
-// barrier, which the TMA warp waits on before refilling the stage.
-// OZ (split-BF16x6): one fill over all K steps; step t issues the six slice products into
-// the regions R0 (A0 B0), R1 (A0 B1, A1 B0) and R2 (A0 B2, A1 B1, A2 B0), which accumulate
-// exactly, so the work warps drain them once per matrix.
-template <bool BF, bool OZ, typename Resolve>
+// barrier, which the TMA warp waits on before refilling the stage.  (Split-BF16x6 has its
+// own issuer, mma_issuer_oz.)
+template <bool BF, typename Resolve>
 __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const TcShape S, uint32_t sm0,
                                         const TcSmemLayout L, uint32_t tmem, volatile int* fail) {
   using namespace tc;
@@ -1072,7 +1070,6 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
         // B by 2 K core matrices (2 x kLboB bytes) per K step, A by 256 bytes per K step
         // within a chunk; the main region index moves when (t - t0) nused crosses span
         uint64_t bh = smem_desc_at(bbits, sm0 + L.bhi + (uint32_t)(fs.t0 * 2 * kLboB));
-        uint64_t bm = smem_desc_at(bbits, sm0 + L.bmid + (uint32_t)(fs.t0 * 2 * kLboB));
         uint64_t bl = smem_desc_at(bbits, sm0 + L.blo + (uint32_t)(fs.t0 * 2 * kLboB));
         int rm = 0, racc = 0;
         bool newreg = true;  // this step starts region rm
@@ -1089,21 +1086,6 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
           }
           const uint32_t first_main = newreg ? 0u : 1u;  // 0: the step starts the region
           const uint32_t first_corr = t == 0 ? 0u : 1u;
-          if constexpr (OZ) {
-            const uint64_t kSlice = (uint64_t)(S.chunk_bytes >> 4);  // descriptor step between A slices
-            for (int hh = 0; hh < S.mh; ++hh) {
-              const uint64_t a0 = ahi + (uint64_t)(hh * S.a_half16), a1 = a0 + kSlice, a2 = a0 + 2 * kSlice;
-              const uint64_t bo = (uint64_t)hh * bstep_half;
-              const uint32_t r0 = tmem + (uint32_t)(hh * S.nc), r1 = r0 + (uint32_t)S.reg_cols,
-                             r2 = r0 + 2u * (uint32_t)S.reg_cols;
-              mma_bf16(r0, a0, bh + bo, idesc, first_corr);
-              mma_bf16(r1, a0, bm + bo, idesc, first_corr);
-              mma_bf16(r1, a1, bh + bo, idesc, 1u);
-              mma_bf16(r2, a0, bl + bo, idesc, first_corr);
-              mma_bf16(r2, a1, bm + bo, idesc, 1u);
-              mma_bf16(r2, a2, bh + bo, idesc, 1u);
-            }
-          } else {
           for (int hh = 0; hh < S.mh; ++hh) {
             const uint64_t ah = ahi + (uint64_t)(hh * S.a_half16);
             const uint64_t bo = (uint64_t)hh * bstep_half;  // parity split: each half its own B
@@ -1117,9 +1099,7 @@ __device__ __noinline__ void mma_issuer(Resolve resolve, int64_t total, const Tc
               mma_tf32(dc0 + (uint32_t)(hh * S.nc), ah + (uint64_t)(S.chunk_bytes >> 4), bh + bo, idesc, 1u);
             }
           }
-          }
           bh += (uint64_t)(2 * kLboB >> 4);
-          bm += (uint64_t)(2 * kLboB >> 4);
           bl += (uint64_t)(2 * kLboB >> 4);
           ahi += (uint64_t)(256 >> 4);
           racc += fs.nused;
@@ -1349,7 +1329,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
         else
           mma_issuer_oz<1>(resolve, total, S, sm0, L, tmem, &s_fail);
       } else {
-        mma_issuer<BF, OZ>(resolve, total, S, sm0, L, tmem, &s_fail);
+        mma_issuer<BF>(resolve, total, S, sm0, L, tmem, &s_fail);
       }
     }
   } else {
