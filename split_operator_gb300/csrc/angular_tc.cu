@@ -173,17 +173,6 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
 
 // barrier among the work warps only (the TMA and MMA warps run their own loops)
 __device__ __forceinline__ void work_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kWorkThreads) : "memory"); }
-// named barrier 2 + g (g < 4) among COUNT work threads (immediate barrier numbers: a
-// register number would make the compiler reserve all sixteen)
-template <int COUNT>
-__device__ __forceinline__ void group_sync(int g) {
-  switch (g) {
-    case 0: asm volatile("bar.sync 2, %0;" ::"n"(COUNT) : "memory"); break;
-    case 1: asm volatile("bar.sync 3, %0;" ::"n"(COUNT) : "memory"); break;
-    case 2: asm volatile("bar.sync 4, %0;" ::"n"(COUNT) : "memory"); break;
-    default: asm volatile("bar.sync 5, %0;" ::"n"(COUNT) : "memory"); break;
-  }
-}
 
 // the same barrier, returning whether v holds in every work thread
 __device__ __forceinline__ bool work_all(bool v) {
@@ -1540,18 +1529,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
               // group's set)
               uint32_t* cm1 = s_colmax[1] + (PK > 1 ? (jr / nl) * 64 : 0);
               if (S.mh == 2 || 32 * lg < n) colmax_rows<kVals / 2>(x, c0, cm1);
-              // the maxima are complete once every warp holding rows of these columns has
-              // added its share: with M = 256 all eight work warps; with M = 128 the four
-              // warps of this column half, in a packed tile those of this column group (two
-              // warps for 64-point lanes, the warp itself for 32-point lanes)
-              if (S.mh == 2)
-                work_sync();
-              else if (PK == 4)
-                __syncwarp();
-              else if (PK == 2)
-                group_sync<64>(2 * up + (lg >> 1));
-              else
-                group_sync<128>(up);
+              work_sync();
               if (tid == 0 && m == 0) trace_mark(tp, tile, TR_SYNC0);
               if (valid) {
                 const uint32_t ho = next == 2 ? (uint32_t)(jr & 1) * bhb2 : 0u;
