@@ -2015,39 +2015,22 @@ static size_t host_chunks() {
   return (size_t)std::min<long>(16, std::max<long>(1, v));
 }
 
-// Relative sizes of the k chunks: the first and the last chunks small (the copies out start
-// after the first chunk's copy in and steps; the last chunk's steps and copy out run after
-// every copy in), the middle ones equal: weight min(c + 1, k - c, ramp).  SO_HOST_RAMP=r
-// (0: equal chunks) at a batch's first so_batch_steps_host call.
-static std::vector<double> host_chunk_weights(size_t k) {
-  const char* e = std::getenv("SO_HOST_RAMP");
-  const long ramp = e ? std::strtol(e, nullptr, 10) : 0;
-  std::vector<double> w(k, 1.0);
-  if (ramp > 0)
-    for (size_t c = 0; c < k; ++c) w[c] = (double)std::min<long>({(long)c + 1, (long)(k - c), ramp});
-  return w;
-}
-
 void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) {
   const size_t kHostChunks = host_chunks();
   const size_t m = props_.size();
   for (size_t i = 0; i < m; ++i)
     if (!in[i] || !out[i]) throw Error(SO_ERR_INVALID, "null state array in batch");
   if (chunks_.empty()) {
-    // chunks of consecutive members, their points in the proportions of
-    // host_chunk_weights, each a batch of its own on its own stream
+    // chunks of consecutive members with about equal points, each a batch of its own on
+    // its own stream
     double total = 0.0;
     for (Propagation* p : props_) total += (double)p->engine().points();
     const size_t k = std::min<size_t>(kHostChunks, m);
-    const std::vector<double> w = host_chunk_weights(k);
-    const double wsum = std::accumulate(w.begin(), w.end(), 0.0);
-    double wacc = 0.0;
     size_t first = 0;
     double acc = 0.0;
     for (size_t c = 0; c < k; ++c) {
       size_t last = first;
-      wacc += w[c];
-      const double goal = total * wacc / wsum;
+      const double goal = total * (double)(c + 1) / (double)k;
       while (last < m && (c + 1 == k || acc < goal || last == first)) acc += (double)props_[last++]->engine().points();
       if (last == first) break;
       Chunk ch;
