@@ -402,11 +402,16 @@ def run_ours(a):
     for _ in range(3):  # warm-up (the first calls set up the chunk pipeline's streams and launch groups)
         e2e_step()
     torch.cuda.synchronize()
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_s = allmax(world, time.perf_counter() - t0)
+    # three timed runs of e2e_steps steps each; the median run is the figure (the host link
+    # of a shared machine shows occasional stalls of a whole run)
+    reps = []
+    for _ in range(3):
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        reps.append(allmax(world, time.perf_counter() - t0))
+    e2e_s = sorted(reps)[1]
     # one more step as three separate calls (each waited on), for the breakdown only
     ph = []
     t = time.perf_counter()
@@ -426,13 +431,13 @@ def run_ours(a):
     else:
         batch.get_arrays_ptr(out_ptrs)
     ph.append(time.perf_counter() - t)
-    e2e = {"value": job_points * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": points * 16,
+    e2e = {"value": job_points * e2e_steps / e2e_s, "unit": UNIT, "runs_ms_per_step": [r / e2e_steps * 1e3 for r in reps], "h2d_bytes_per_step": points * 16,
            "d2h_bytes_per_step": points * 16, "steps": e2e_steps,
            "unpipelined_phase_ms": {"set_arrays": ph[0] * 1e3, "steps": ph[1] * 1e3, "get_arrays": ph[2] * 1e3},
            "host_link_gbs": {"h2d": 211, "d2h": 193, "source": "cudaMemcpyAsync of 1 GiB pinned, measured on this "
                                                                "GPU model"},
            "note": ("every step: one so_batch_steps_host call: pinned FP64 host states of all instances in, one "
-                    "step, states out to pinned host buffers, pipelined over 8 instance chunks on their own "
+                    "step, states out to pinned host buffers, pipelined over 16 instance chunks on their own "
                     "streams (copy engines both ways)") if not single else
                    "every step: so_propagation_set_array from a pinned FP64 host buffer, one step, "
                    "so_propagation_get_array into a pinned host buffer"}

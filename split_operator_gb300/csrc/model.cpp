@@ -2011,7 +2011,7 @@ void Batch::get_arrays(double* const* out) {
 // are formed at a batch's first steps_host call and kept)
 static size_t host_chunks() {
   const char* e = std::getenv("SO_HOST_CHUNKS");
-  const long v = e ? std::strtol(e, nullptr, 10) : 8;
+  const long v = e ? std::strtol(e, nullptr, 10) : 16;
   return (size_t)std::min<long>(16, std::max<long>(1, v));
 }
 
