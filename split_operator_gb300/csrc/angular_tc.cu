@@ -329,50 +329,6 @@ __device__ __forceinline__ void apply_row(const PassParams& p, const TileTabs& T
       }
       case OP_DIAGND: {
         const float2* t = reinterpret_cast<const float2*>(op.ptr) + ix0;
-        if ((op.flags & 4) && (reinterpret_cast<uintptr_t>(t) & 15u) == 0) {
-          // a table pair T ... T with only lane-axis diagonals, norms of the same column
-          // weights and scalar ops between (flag 4, partner op.c; see make_tc_params): the
-          // row factor F of the diagonals first, then one pass over the values with T loaded
-          // once, y = x T (the norms' values up to the row factors), x <- y (T F), and the
-          // norms from the row's sum S = sum |y|^2 w
-          const int pe = op.c;
-          float2 F = {1.0f, 0.0f};
-          int wred = -1;
-          for (int q = oi + 1; q < pe; ++q) {
-            const DevOp& o = p.ops[q];
-            if (o.kind == OP_DIAG1D)
-              F = cmulf(F, __ldg(reinterpret_cast<const float2*>(o.ptr) + j));
-            else if (o.kind == OP_NORM && wred < 0)
-              wred = o.red;
-          }
-          float4 tv[NB / 2];
-#pragma unroll
-          for (int q = 0; q < NB / 2; ++q) tv[q] = __ldg(reinterpret_cast<const float4*>(t) + q);
-          float S = 0.0f;
-#pragma unroll
-          for (int q = 0; q < NB / 2; ++q) {
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const int u = 2 * q + h;
-              const float2 tt = h ? make_float2(tv[q].z, tv[q].w) : make_float2(tv[q].x, tv[q].y);
-              const float2 y = cmulf(v[u], tt);
-              if (wred >= 0) S = fmaf(fmaf(y.x, y.x, y.y * y.y), tab_w<PK>(T, wred, c0 + u), S);
-              v[u] = cmulf(y, cmulf(tt, F));
-            }
-          }
-          float2 f = {1.0f, 0.0f};
-          for (int q = oi + 1; q < pe; ++q) {
-            const DevOp& o = p.ops[q];
-            if (o.kind == OP_DIAG1D) {
-              f = cmulf(f, __ldg(reinterpret_cast<const float2*>(o.ptr) + j));
-            } else if (o.kind == OP_NORM) {
-              const float* wr = o.wf[g.sweep_axis];
-              acc[o.red] += S * fmaf(f.x, f.x, f.y * f.y) * (wr == rw_ptr ? rw_val : __ldg(wr + j));
-            }
-          }
-          oi = pe;  // the partner's product is done
-          break;
-        }
         if ((reinterpret_cast<uintptr_t>(t) & 15u) == 0) {
           float4 tv[NB / 2];
 #pragma unroll
@@ -444,58 +400,6 @@ __device__ __forceinline__ void apply_row2(const PassParams& p, const TileTabs& 
       case OP_DIAGND: {
         const float2* ta = reinterpret_cast<const float2*>(op.ptr) + ixa;
         const float2* tb = reinterpret_cast<const float2*>(op.ptr) + ixb;
-        if ((op.flags & 4) && ((reinterpret_cast<uintptr_t>(ta) | reinterpret_cast<uintptr_t>(tb)) & 15u) == 0) {
-          // the fused table pair of apply_row, for both rows
-          const int pe = op.c;
-          float2 Fa = {1.0f, 0.0f}, Fb = {1.0f, 0.0f};
-          int wred = -1;
-          for (int q = oi + 1; q < pe; ++q) {
-            const DevOp& o = p.ops[q];
-            if (o.kind == OP_DIAG1D) {
-              Fa = cmulf(Fa, __ldg(reinterpret_cast<const float2*>(o.ptr) + ja));
-              Fb = cmulf(Fb, __ldg(reinterpret_cast<const float2*>(o.ptr) + jb));
-            } else if (o.kind == OP_NORM && wred < 0) {
-              wred = o.red;
-            }
-          }
-          float4 qa[NB / 2], qb[NB / 2];
-#pragma unroll
-          for (int q = 0; q < NB / 2; ++q) {
-            qa[q] = __ldg(reinterpret_cast<const float4*>(ta) + q);
-            qb[q] = __ldg(reinterpret_cast<const float4*>(tb) + q);
-          }
-          float Sa = 0.0f, Sb = 0.0f;
-#pragma unroll
-          for (int q = 0; q < NB / 2; ++q) {
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const int u = 2 * q + h;
-              const float w = wred >= 0 ? T.colw[wred][c0 + u] : 0.0f;
-              const float2 t1 = h ? make_float2(qa[q].z, qa[q].w) : make_float2(qa[q].x, qa[q].y);
-              const float2 t2 = h ? make_float2(qb[q].z, qb[q].w) : make_float2(qb[q].x, qb[q].y);
-              const float2 ya = cmulf(va[u], t1), yb = cmulf(vb[u], t2);
-              Sa = fmaf(fmaf(ya.x, ya.x, ya.y * ya.y), w, Sa);
-              Sb = fmaf(fmaf(yb.x, yb.x, yb.y * yb.y), w, Sb);
-              va[u] = cmulf(ya, cmulf(t1, Fa));
-              vb[u] = cmulf(yb, cmulf(t2, Fb));
-            }
-          }
-          float2 fa = {1.0f, 0.0f}, fb = {1.0f, 0.0f};
-          for (int q = oi + 1; q < pe; ++q) {
-            const DevOp& o = p.ops[q];
-            if (o.kind == OP_DIAG1D) {
-              fa = cmulf(fa, __ldg(reinterpret_cast<const float2*>(o.ptr) + ja));
-              fb = cmulf(fb, __ldg(reinterpret_cast<const float2*>(o.ptr) + jb));
-            } else if (o.kind == OP_NORM) {
-              const float* wr = o.wf[g.sweep_axis];
-              const bool pre = wr == rw_ptr;
-              acc[o.red] += Sa * fmaf(fa.x, fa.x, fa.y * fa.y) * (pre ? rwa : __ldg(wr + ja));
-              acc[o.red] += Sb * fmaf(fb.x, fb.x, fb.y * fb.y) * (pre ? rwb : __ldg(wr + jb));
-            }
-          }
-          oi = pe;
-          break;
-        }
         if (((reinterpret_cast<uintptr_t>(ta) | reinterpret_cast<uintptr_t>(tb)) & 15u) == 0) {
           float4 qa[NB / 2], qb[NB / 2];
 #pragma unroll
@@ -1824,41 +1728,6 @@ void make_tc_params(const PassParams& p, const int* mat_op, int nmat, const floa
     }
   }
   tp.error_slot = error_slot;
-  // table pairs T ... T inside one segment with only lane-axis diagonals, norms with the
-  // same column weights and scalar ops between: flag 4 on the first, its partner in c (the
-  // epilogue loads T once for both products; see apply_row)
-  {
-    const Geometry& gg = tp.p.g;
-    for (int i = 0; i < tp.p.nops; ++i) {
-      DevOp& op = tp.p.ops[i];
-      if (op.kind != OP_DIAGND) continue;
-      op.flags &= ~4;
-      int partner = -1;
-      bool ok = true;
-      const DevOp* nrm = nullptr;
-      for (int q = i + 1; q < tp.p.nops && ok; ++q) {
-        const DevOp& o = tp.p.ops[q];
-        if (o.kind == OP_DIAGND) {
-          if (o.ptr == op.ptr) partner = q;
-          break;
-        }
-        if (o.kind == OP_NORM) {
-          if (nrm)
-            for (int a = 0; a < gg.ndim; ++a)
-              if (a != gg.sweep_axis && o.wf[a] != nrm->wf[a]) ok = false;
-          nrm = &o;
-        } else if (!((o.kind == OP_DIAG1D && o.axis == gg.sweep_axis) || o.kind == OP_COPY || o.kind == OP_LOSS ||
-                     o.kind == OP_SETC)) {
-          ok = false;
-        }
-      }
-      if (ok && partner > i) {
-        op.flags |= 4;
-        op.c = partner;
-        i = partner;  // the partner starts no pair of its own
-      }
-    }
-  }
   // the distinct full-size tables after the first matrix (the kernel prefetches their tile rows)
   for (int oi = nmat > 0 ? mat_op[0] + 1 : p.nops; oi < p.nops && tp.npre < 4; ++oi) {
     if (p.ops[oi].kind != OP_DIAGND) continue;
