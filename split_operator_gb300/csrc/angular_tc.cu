@@ -857,26 +857,17 @@ __device__ __forceinline__ void write_b_row(const float2 (&x)[NV], int c0, int k
 }
 
 // The same row into the three slice images of split-BF16x6, with the quanta of its columns
-// (cm: per-column maxima of the whole operand, complete when this runs), in the MN-major
-// layout the epilogue's operands use: eight consecutive B columns (four complex columns) of
-// one K row are 16 contiguous bytes, K row k at (k / 8) 128 + (k % 8) 16 inside its column
-// group, column groups sbo_mn apart -- one 4-byte store per complex value (re and im side
-// by side) and slice, where the K-major layout takes a 2-byte store per real value.
+// (cm: per-column maxima of the whole operand, complete when this runs)
 template <int NV>
 __device__ __forceinline__ void write_b_row_oz(const float2 (&x)[NV], int c0, int k, unsigned char* b0,
-                                               unsigned char* b1, unsigned char* b2, uint32_t sbo_mn,
+                                               unsigned char* b1, unsigned char* b2, uint32_t sbo_b,
                                                const uint32_t* cm) {
-  const uint32_t kr = (uint32_t)(k >> 3) * 128u + (uint32_t)(k & 7) * 16u;
+  const uint32_t o0 = boff<true>(2 * c0, k, sbo_b);
 #pragma unroll
   for (int u = 0; u < NV; ++u) {
-    uint32_t r0, r1, r2, i0, i1, i2;
-    oz_split(x[u].x, oz_quanta(cm[2 * (c0 + u)]), r0, r1, r2);
-    oz_split(x[u].y, oz_quanta(cm[2 * (c0 + u) + 1]), i0, i1, i2);
-    // complex column c0 + u: group (c0 + u) / 4, bytes 4 ((c0 + u) % 4) of its 16-byte row
-    const uint32_t off = (uint32_t)((c0 + u) >> 2) * sbo_mn + kr + (uint32_t)((c0 + u) & 3) * 4u;
-    *reinterpret_cast<uint32_t*>(b0 + off) = r0 | (i0 << 16);
-    *reinterpret_cast<uint32_t*>(b1 + off) = r1 | (i1 << 16);
-    *reinterpret_cast<uint32_t*>(b2 + off) = r2 | (i2 << 16);
+    const uint32_t o = o0 + (uint32_t)(u >> 2) * sbo_b + (uint32_t)(u & 3) * 32u;
+    store1_oz(b0, b1, b2, o, x[u].x, oz_quanta(cm[2 * (c0 + u)]));
+    store1_oz(b0, b1, b2, o + 16, x[u].y, oz_quanta(cm[2 * (c0 + u) + 1]));
   }
 }
 
@@ -1155,24 +1146,14 @@ __device__ __noinline__ void mma_issuer_oz(Resolve resolve, int64_t total, const
   uint64_t* dbar = full + 2 * ns;
   uint64_t* bready = dbar + 2;
   uint64_t* quiet = dbar + 3;
-  // B of the first matrix (written by the prologue): K-major; of a later one (written by the
-  // epilogue): MN-major (instruction descriptor bit 16; LBO the 128-byte K-group stride, SBO
-  // the column-group stride), see write_b_row_oz
-  const uint32_t idesc_k = idesc_bf16(128, (uint32_t)S.nc), idesc_mn = idesc_k | (1u << 16);
+  const uint32_t idesc = idesc_bf16(128, (uint32_t)S.nc);
   const uint64_t bbits = smem_desc_bits(kLboB, L.sbo_b), abits = smem_desc_bits(128, (uint32_t)S.sbo_a);
-  // MN-major B (split-BF16x6 operands written by the epilogue): K rows of 16 bytes (eight bf16
-  // columns), 8-column groups kdim x 16 bytes apart (within bhalf)
-  const uint32_t sbo_mn = (uint32_t)S.kdim * 16u;
-  const uint64_t bbits_mn = smem_desc_bits(128, sbo_mn);
   const uint64_t b0 = smem_desc_at(bbits, sm0 + L.bhi), b1 = smem_desc_at(bbits, sm0 + L.bmid),
                  b2 = smem_desc_at(bbits, sm0 + L.blo);
-  const uint64_t b0m = smem_desc_at(bbits_mn, sm0 + L.bhi), b1m = smem_desc_at(bbits_mn, sm0 + L.bmid),
-                 b2m = smem_desc_at(bbits_mn, sm0 + L.blo);
   const uint64_t a_first = smem_desc_at(abits, sm0 + L.stage0), a_stage = (uint64_t)(L.stage_bytes >> 4);
   const uint64_t slice = (uint64_t)(S.chunk_bytes >> 4), ahalf = (uint64_t)S.a_half16;
   const uint64_t bhalf = S.par ? (uint64_t)(L.bhalf >> 4) : 0u;
-  constexpr uint64_t kBStepK = (uint64_t)(2 * kLboB >> 4), kBStepMn = (uint64_t)(256 >> 4),
-                     kAStep = (uint64_t)(256 >> 4);
+  constexpr uint64_t kBStep = (uint64_t)(2 * kLboB >> 4), kAStep = (uint64_t)(256 >> 4);
   const uint32_t rc = (uint32_t)S.reg_cols, nch = (uint32_t)S.nc;
   const int ksteps = S.ksteps;
   int64_t cc = 0;
@@ -1188,10 +1169,7 @@ __device__ __noinline__ void mma_issuer_oz(Resolve resolve, int64_t total, const
       ok = mbar_poll(bready, nready & 1u, kWaitLimit);
       ++nready;
       tc_fence_after();
-      const bool mn = m > 0;
-      uint64_t bh = mn ? b0m : b0, bm = mn ? b1m : b1, bl = mn ? b2m : b2;
-      const uint64_t bstep = mn ? kBStepMn : kBStepK;
-      const uint32_t idesc = mn ? idesc_mn : idesc_k;
+      uint64_t bh = b0, bm = b1, bl = b2;
       for (int t = 0; t < ksteps && ok; t += KPC) {
         ok = mbar_poll(&full[s], fphase, kWaitLimit);
         if (!ok) break;
@@ -1212,9 +1190,9 @@ __device__ __noinline__ void mma_issuer_oz(Resolve resolve, int64_t total, const
             mma_bf16(r0 + 2u * rc, a0 + slice, bm + bo, idesc, 1u);
             mma_bf16(r0 + 2u * rc, a0 + 2u * slice, bh + bo, idesc, 1u);
           }
-          bh += bstep;
-          bm += bstep;
-          bl += bstep;
+          bh += kBStep;
+          bm += kBStep;
+          bl += kBStep;
           a += kAStep;
         }
         mma_commit(&empty[s]);
@@ -1368,7 +1346,6 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
     const uint32_t lane_base = tmem + ((uint32_t)(lg * 32) << 16);
     constexpr int kLd = kVals / 32;  // 16-column loads per half of a thread's columns (even / odd form)
     const uint32_t bhb2 = L.bhalf;  // bytes between the two B halves
-    const uint32_t sbo_mn = (uint32_t)S.kdim * 16u;  // MN-major B written here (split-BF16x6)
     float* stg = bhi;  // output staging reuses the B_hi area once the last GEMM is done
     uint32_t drains = 0;
     const TcParams* cur = nullptr;
@@ -1556,7 +1533,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
               if (tid == 0 && m == 0) trace_mark(tp, tile, TR_SYNC0);
               if (valid) {
                 const uint32_t ho = next == 2 ? (uint32_t)(jr & 1) * bhb2 : 0u;
-                write_b_row_oz<kVals / 2>(x, c0, next == 2 ? jr >> 1 : jr, bhb + ho, bmb + ho, blb + ho, sbo_mn,
+                write_b_row_oz<kVals / 2>(x, c0, next == 2 ? jr >> 1 : jr, bhb + ho, bmb + ho, blb + ho, L.sbo_b,
                                           cm1);
               }
             }
@@ -1602,16 +1579,16 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
             colmax_rows<kVals / 4>(sm2, cc0, s_colmax[1]);
             work_sync();
             if (tid == 0 && m == 0) trace_mark(tp, tile, TR_SYNC0);
-            write_b_row_oz<kVals / 4>(sp, cc0, i, bhb, bmb, blb, sbo_mn, s_colmax[1]);
-            write_b_row_oz<kVals / 4>(sm2, cc0, i, bhb + bhb2, bmb + bhb2, blb + bhb2, sbo_mn, s_colmax[1]);
+            write_b_row_oz<kVals / 4>(sp, cc0, i, bhb, bmb, blb, L.sbo_b, s_colmax[1]);
+            write_b_row_oz<kVals / 4>(sm2, cc0, i, bhb + bhb2, bmb + bhb2, blb + bhb2, L.sbo_b, s_colmax[1]);
           } else if (OZ) {
             colmax_rows<kVals / 4>(xa, cc0, s_colmax[1]);
             colmax_rows<kVals / 4>(xb, cc0, s_colmax[1]);
             work_sync();
             if (tid == 0 && m == 0) trace_mark(tp, tile, TR_SYNC0);
             const uint32_t hoa = (uint32_t)(ja & 1) * bhb2, hob = (uint32_t)(jb & 1) * bhb2;
-            write_b_row_oz<kVals / 4>(xa, cc0, ja >> 1, bhb + hoa, bmb + hoa, blb + hoa, sbo_mn, s_colmax[1]);
-            write_b_row_oz<kVals / 4>(xb, cc0, jb >> 1, bhb + hob, bmb + hob, blb + hob, sbo_mn, s_colmax[1]);
+            write_b_row_oz<kVals / 4>(xa, cc0, ja >> 1, bhb + hoa, bmb + hoa, blb + hoa, L.sbo_b, s_colmax[1]);
+            write_b_row_oz<kVals / 4>(xb, cc0, jb >> 1, bhb + hob, bmb + hob, blb + hob, L.sbo_b, s_colmax[1]);
           } else if (next == 1) {
             // sum / difference operand of the next matrix, K row i
             float2 sd[kVals / 4];
