@@ -21,9 +21,9 @@
 //   warps 0-7  load the tile, run the point-wise ops, split it into the B operand,
 //              drain the accumulators, run the ops between / after the matrices,
 //              store, and fold the norms (named barrier 1 among themselves)
-//   warp 8     lane 0 streams the A chunks of every tile, in order, through the
-//              shared-memory stages by bulk TMA (it runs ahead across tiles); lane 1
-//              issues tcgen05.mma as chunks land and the B operand is ready
+//   warp 8     streams the A chunks (one MMA K step each) of every tile, in order,
+//              through 2-6 shared-memory stages by bulk TMA (it runs ahead across tiles)
+//   warp 9     issues tcgen05.mma (one lane) as chunks land and the B operand is ready
 // The tensor core truncates its FP32 accumulation, so the A_hi B_hi products go to
 // three TMEM regions a couple of K steps each and the work warps drain the
 // regions into registers (round-to-nearest adds) every kFillSteps K steps; the
@@ -50,15 +50,12 @@ constexpr int kStageBudget = 48 * 1024;
 constexpr int kLboB = 144;          // B: core matrices along K (16 B padding vs 128)
 constexpr uint64_t kWaitLimit = 2000000000ull;  // 2 s per wait
 constexpr int kWorkThreads = 256;               // warps 0-7
-constexpr int kThreads = kWorkThreads + 32;     // + warp 8: lane 0 the TMA stream, lane 1 the MMAs
+constexpr int kThreads = kWorkThreads + 64;     // + warp 8 (TMA) + warp 9 (MMA)
 constexpr uint32_t kTmemCols = 256;  // half of the SM's tensor memory: two CTAs per SM
 constexpr int kRegions = 4;          // 64-column accumulator regions in kTmemCols
 constexpr int kFillSteps = 6;        // K steps between two drains of the main regions
 constexpr int kVals = 32;            // FP32 accumulator columns a work thread drains
 constexpr int kCtasPerSm = 2;        // persistent CTAs per SM (each one's memory latency hides behind the other)
-// registers per thread: two CTAs of kThreads per SM within the SM's 65536 (multiple of 8)
-constexpr int kMaxRegs = (65536 / (kCtasPerSm * kThreads)) & ~7;
-static_assert(kMaxRegs == 112, "the register budget the epilogue is written for");
 constexpr int kColtSlots = 4;        // DIAG1D ops on a non-lane axis per pass
 
 struct TcShape {
@@ -1323,12 +1320,9 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
   const uint32_t sm0 = smem_u32(sm);
 
   if (warp == kWorkThreads / 32) {
-    // one warp for both single-lane roles (a ninth and tenth warp would take registers from
-    // the work warps: the kernel's budget is 65536 / (2 CTAs x its threads) per thread);
-    // the two lanes run their own loops, interleaved by the warp's scheduler
+    if (lane == 0) tma_producer(resolve, total, S, sm0, L, &s_fail);
+  } else if (warp == kWorkThreads / 32 + 1) {
     if (lane == 0) {
-      tma_producer(resolve, total, S, sm0, L, &s_fail);
-    } else if (lane == 1) {
       if constexpr (OZ) {
         if (S.mh == 2)
           mma_issuer_oz<2>(resolve, total, S, sm0, L, tmem, &s_fail);
@@ -1670,7 +1664,7 @@ __device__ __forceinline__ void tc_persistent(Resolve resolve, const int64_t tot
 
 // OPM: operand mode, 0 = 3xTF32, 1 = split-BF16x3, 2 = split-BF16x6 (exact sums)
 template <int OPM, int PK = 1>
-__global__ void __maxnreg__(kMaxRegs) angular_tc_kernel(const __grid_constant__ TcParams tp) {
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel(const __grid_constant__ TcParams tp) {
   const TcParams* prm = &tp;
   tc_persistent<OPM != 0, OPM == 2, PK>([prm](int64_t t) { return TileRef{prm, t}; }, tp.p.g.tiles);
 }
@@ -1679,7 +1673,7 @@ __global__ void __maxnreg__(kMaxRegs) angular_tc_kernel(const __grid_constant__ 
 // global tile b is tile (b - offsets[i]) of params[i], offsets[i] <= b < offsets[i + 1];
 // offsets[count] is the total.
 template <int OPM, int PK = 1>
-__global__ void __maxnreg__(kMaxRegs) angular_tc_kernel_batched(const TcParams* __restrict__ params,
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) angular_tc_kernel_batched(const TcParams* __restrict__ params,
                                                                         const uint2* __restrict__ owners,
                                                                         int64_t total) {
   // owners[b] = (pass index, tile within the pass) of global tile b, built on the host: one
