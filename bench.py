@@ -41,7 +41,7 @@ def parse():
     ap.add_argument("--workload", default="batch", choices=["batch", "single"])
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--precision", default="fp32_bf16x6",
-                    choices=["fp64", "fp32_tf32x3", "fp32_bf16x3", "fp32_bf16x6", "fp32_simt"])
+                    choices=["fp64", "fp32_tf32x3", "fp32_bf16x3", "fp32_bf16x6", "fp32_simt", "float_float"])
     ap.add_argument("--nr", type=int, default=4096)
     ap.add_argument("--nth", type=int, default=128)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -481,11 +481,16 @@ def run_ours(a):
                       beta=c["beta"])
             p64 = W.radial_angular_2d(precision="fp64", **kw)[0]
             pfx = W.radial_angular_2d(precision=a.precision, **kw)[0]
+            pff = W.radial_angular_2d(precision="float_float", **kw)[0]
             p64.steps(nchk)
             pfx.steps(nchk)
-            errs.append({"nr": c["nr"], "nth": c["nth"], "rel_l2": rel_l2(pfx.get_array(), p64.get_array()),
+            pff.steps(nchk)
+            x64 = p64.get_array()
+            errs.append({"nr": c["nr"], "nth": c["nth"], "rel_l2": rel_l2(pfx.get_array(), x64),
                          "norm_diff": abs(pfx.norm() - p64.norm()),
-                         "loss_diff": abs(pfx.all_losses()[0] - p64.all_losses()[0])})
+                         "loss_diff": abs(pfx.all_losses()[0] - p64.all_losses()[0]),
+                         "float_float_rel_l2": rel_l2(pff.get_array(), x64)})
+            del p64, pfx, pff
         acc.update({"steps": nchk, "instances": errs, "max_rel_l2": max(e["rel_l2"] for e in errs)})
         # plain FP64 GPU path throughput on the same workload (the 20x denominator): every instance
         del batch
@@ -525,6 +530,35 @@ def run_ours(a):
         del props64
         if not single:
             b64 = None
+        # the float-float state (FP64-like accuracy on the FP32 pipes) on the same instances
+        propsff = build_props(a, "float_float")
+        if single:
+            evs = []
+            for _ in range(f64_steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                propsff[0].steps(1)
+                e1.record()
+                evs.append((e0, e1))
+            propsff[0].synchronize()
+            torch.cuda.synchronize()
+            ff_ms = sum(x.elapsed_time(y) for x, y in evs)
+        else:
+            bff = so.Batch(propsff)
+            bff.steps(3)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            bff.steps(f64_steps)
+            e1.record()
+            torch.cuda.synchronize()
+            ff_ms = e0.elapsed_time(e1)
+            bff = None
+        acc["float_float_gpu_value"] = points64 * f64_steps / (ff_ms / 1e3)
+        acc["float_float_vs_fp64_gpu"] = acc["float_float_gpu_value"] / acc["fp64_gpu_value"]
+        acc["float_float_max_rel_l2"] = max(e["float_float_rel_l2"] for e in errs)
+        del propsff
 
     tgs = None
     if rank == 0 and not single and not a.no_ground_state:
@@ -543,7 +577,7 @@ def run_ours(a):
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if a.precision == "fp64" else "f32", "data": "synthetic",
+            "dtype": {"fp64": "f64", "float_float": "f32x2 (float-float)"}.get(a.precision, "f32"), "data": "synthetic",
             "config": {"workload": workload_name(a), "precision": a.precision, "grid_points": points,
                        "l2": ("inputs larger than L2 (states + tables ~" + f"{points * 24 / 1e9:.1f} GB)")
                        if not single else "flushed before every timed step (256 MiB write, untimed)",

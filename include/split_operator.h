@@ -63,8 +63,11 @@ enum {
   SO_PRECISION_FP32_TF32X3 = 1, /* FP32 state; real lane matrices as 3xTF32 tensor-core GEMM */
   SO_PRECISION_FP32_BF16X3 = 2, /* FP32 state; real lane matrices as split-BF16x3 tensor-core GEMM */
   SO_PRECISION_FP32_SIMT = 3,   /* FP32 state; lane matrices on FP32 CUDA cores */
-  SO_PRECISION_FP32_BF16X6 = 4  /* FP32 state; real lane matrices as split-BF16x6 tensor-core GEMM:
+  SO_PRECISION_FP32_BF16X6 = 4, /* FP32 state; real lane matrices as split-BF16x6 tensor-core GEMM:
                                    three fixed-point bf16 slices per operand, exact FP32 sums */
+  SO_PRECISION_FLOAT_FLOAT = 5  /* float-float state and tables (each real an unevaluated sum of two
+                                   FP32 numbers, ~48 significand bits); the FP64 path's kernels
+                                   with float-float arithmetic on the FP32 pipes */
 };
 
 /* ---- library ------------------------------------------------------------ */

@@ -18,7 +18,7 @@ FULL, HALF = 0, 1
 NORMAL, INVERSE_FIRST = 0, 1
 APPLY_NONE, FIRST_HALF, SECOND_HALF = 0, 1, 2
 
-PRECISION = {"fp64": 0, "fp32_tf32x3": 1, "fp32_bf16x3": 2, "fp32_simt": 3, "fp32_bf16x6": 4}
+PRECISION = {"fp64": 0, "fp32_tf32x3": 1, "fp32_bf16x3": 2, "fp32_simt": 3, "fp32_bf16x6": 4, "float_float": 5}
 
 
 def _dp(a):
@@ -556,7 +556,7 @@ class OperationStack(_Handle):
 
 class Propagation(_Handle):
     """propagation.rs:72-292 (``precision``: 'fp64', 'fp32_tf32x3', 'fp32_bf16x3', 'fp32_bf16x6',
-    'fp32_simt')."""
+    'fp32_simt', 'float_float')."""
 
     _free = "so_propagation_free"
 

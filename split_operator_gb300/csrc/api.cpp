@@ -183,7 +183,7 @@ int so_wave_function_new(const double* array, const size_t* shape, size_t ndim, 
       need(grids[a] != nullptr, "null grid");
       gs.push_back(grids[a]->g);
     }
-    auto wf = std::make_unique<so::WaveFunction>(shp, gs, ident(ndim), true);
+    auto wf = std::make_unique<so::WaveFunction>(shp, gs, ident(ndim), so::kRealF64);
     wf->eng->import_host(array);
     wf->eng->sync();
     *out = new so_wave_function_t{std::move(wf)};
@@ -194,7 +194,7 @@ int so_wave_function_clone(so_wave_function w, so_wave_function* out) {
   return guard([&] {
     need(w && out, "null argument");
     so::WaveFunction& s = *w->wf;
-    auto c = std::make_unique<so::WaveFunction>(s.shape, s.grids, s.eng->perm, s.eng->fp64);
+    auto c = std::make_unique<so::WaveFunction>(s.shape, s.grids, s.eng->perm, s.eng->real);
     c->last_grid_names = s.last_grid_names;
     c->possible_norm_change = s.possible_norm_change;
     c->eng->write_slot(c->cache_slot, s.eng->read_slot(s.cache_slot));
@@ -228,7 +228,7 @@ int so_wave_function_dot(so_wave_function a, so_wave_function b, double* out) {
     need(a && b && out, "null argument");
     so::WaveFunction& x = *a->wf;
     so::WaveFunction& y = *b->wf;
-    need(x.shape == y.shape && x.eng->perm == y.eng->perm && x.eng->fp64 == y.eng->fp64, "shapes differ",
+    need(x.shape == y.shape && x.eng->perm == y.eng->perm && x.eng->real == y.eng->real, "shapes differ",
          SO_ERR_SHAPE);
     for (size_t i = 0; i < x.grids.size(); ++i)
       need(x.grids[i].weights == y.grids[i].weights, "weight arrays differ (wave_function.rs:91)", SO_ERR_STATE);
@@ -278,11 +278,11 @@ static void density_impl(so::WaveFunction& wf, double* out, int axis) {
   size_t n = axis < 0 ? wf.points() : wf.shape[axis];
   so::DeviceBuffer d(n * sizeof(double));
   if (axis < 0) {
-    so::cuda_check(so::launch_density(d.as<double>(), e.psi.ptr, e.fp64, g, e.stream), "density");
+    so::cuda_check(so::launch_density(d.as<double>(), e.psi.ptr, e.real, g, e.stream), "density");
   } else {
     for (size_t a = 0; a < wf.grids.size(); ++a) wf.last_grid_names[a] = wf.grids[a].name;
     std::vector<const double*> w = wf.weight_ptrs();
-    so::cuda_check(so::launch_state_density(d.as<double>(), e.psi.ptr, e.fp64, g, axis, w.data(), nullptr, e.stream),
+    so::cuda_check(so::launch_state_density(d.as<double>(), e.psi.ptr, e.real, g, axis, w.data(), nullptr, e.stream),
                    "state density");
   }
   so::cuda_check(cudaMemcpyAsync(out, d.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, e.stream), "copy");

@@ -5,8 +5,19 @@
 #include <atomic>
 
 #include "common.cuh"
+#include "ff.cuh"
 
 namespace so {
+
+// f(T{}) with T the device complex type of a state precision
+template <typename F>
+static cudaError_t by_real(int real, F f) {
+  switch (real) {
+    case kRealF64: return f(double2{});
+    case kRealFF: return f(ffc{});
+    default: return f(float2{});
+  }
+}
 
 static std::atomic<uint64_t> g_launches{0};
 void count_launch(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
@@ -173,61 +184,62 @@ static unsigned blocks_for(int64_t total) {
   return (unsigned)b;
 }
 
-cudaError_t launch_import(void* dst, bool dst_fp64, const double* src, const Geometry& g, cudaStream_t st) {
+cudaError_t launch_import(void* dst, int dst_real, const double* src, const Geometry& g, cudaStream_t st) {
   const int64_t total = total_of(g);
   if (layout_is_transpose2(g)) {
     const dim3 grid = transpose_grid(g), block(kTT, 8);
     if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
-    if (dst_fp64)
-      import_transpose_kernel<double2><<<grid, block, 0, st>>>((double2*)dst, (const double2*)src, g.sshape[1],
-                                                               g.sshape[0]);
-    else
-      import_transpose_kernel<float2><<<grid, block, 0, st>>>((float2*)dst, (const double2*)src, g.sshape[1],
-                                                              g.sshape[0]);
+    const cudaError_t e = by_real(dst_real, [&](auto t) {
+      using D = decltype(t);
+      import_transpose_kernel<D><<<grid, block, 0, st>>>((D*)dst, (const double2*)src, g.sshape[1], g.sshape[0]);
+      return cudaGetLastError();
+    });
     count_launch();
-    return cudaGetLastError();
+    return e;
   }
   const Perm P = make_perm(g);
-  if (dst_fp64)
-    import_kernel<double2><<<blocks_for(total), 256, 0, st>>>((double2*)dst, (const double2*)src, P, total);
-  else
-    import_kernel<float2><<<blocks_for(total), 256, 0, st>>>((float2*)dst, (const double2*)src, P, total);
+  const cudaError_t e = by_real(dst_real, [&](auto t) {
+    using D = decltype(t);
+    import_kernel<D><<<blocks_for(total), 256, 0, st>>>((D*)dst, (const double2*)src, P, total);
+    return cudaGetLastError();
+  });
   count_launch();
-  return cudaGetLastError();
+  return e;
 }
 
-cudaError_t launch_export(double* dst, const void* src, bool src_fp64, const Geometry& g, cudaStream_t st) {
+cudaError_t launch_export(double* dst, const void* src, int src_real, const Geometry& g, cudaStream_t st) {
   const int64_t total = total_of(g);
   if (layout_is_transpose2(g)) {
     const dim3 grid = transpose_grid(g), block(kTT, 8);
     if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
-    if (src_fp64)
-      export_transpose_kernel<double2><<<grid, block, 0, st>>>((double2*)dst, (const double2*)src, g.sshape[1],
-                                                               g.sshape[0]);
-    else
-      export_transpose_kernel<float2><<<grid, block, 0, st>>>((double2*)dst, (const float2*)src, g.sshape[1],
-                                                              g.sshape[0]);
+    const cudaError_t e = by_real(src_real, [&](auto t) {
+      using S = decltype(t);
+      export_transpose_kernel<S><<<grid, block, 0, st>>>((double2*)dst, (const S*)src, g.sshape[1], g.sshape[0]);
+      return cudaGetLastError();
+    });
     count_launch();
-    return cudaGetLastError();
+    return e;
   }
   const Perm P = make_perm(g);
-  if (src_fp64)
-    export_kernel<double2><<<blocks_for(total), 256, 0, st>>>((double2*)dst, (const double2*)src, P, total);
-  else
-    export_kernel<float2><<<blocks_for(total), 256, 0, st>>>((double2*)dst, (const float2*)src, P, total);
+  const cudaError_t e = by_real(src_real, [&](auto t) {
+    using S = decltype(t);
+    export_kernel<S><<<blocks_for(total), 256, 0, st>>>((double2*)dst, (const S*)src, P, total);
+    return cudaGetLastError();
+  });
   count_launch();
-  return cudaGetLastError();
+  return e;
 }
 
-cudaError_t launch_density(double* dst, const void* src, bool fp64, const Geometry& g, cudaStream_t st) {
+cudaError_t launch_density(double* dst, const void* src, int real, const Geometry& g, cudaStream_t st) {
   const int64_t total = total_of(g);
   const Perm P = make_perm(g);
-  if (fp64)
-    density_kernel<double2><<<blocks_for(total), 256, 0, st>>>(dst, (const double2*)src, P, total);
-  else
-    density_kernel<float2><<<blocks_for(total), 256, 0, st>>>(dst, (const float2*)src, P, total);
+  const cudaError_t e = by_real(real, [&](auto t) {
+    using S = decltype(t);
+    density_kernel<S><<<blocks_for(total), 256, 0, st>>>(dst, (const S*)src, P, total);
+    return cudaGetLastError();
+  });
   count_launch();
-  return cudaGetLastError();
+  return e;
 }
 
 // state_density: out[i] = sum over all other axes of |psi|^2 prod_a w_a (wave_function.rs:121-148).
@@ -273,7 +285,7 @@ __global__ void state_density_kernel(double* dst, const S* src, Perm P, int axis
   }
 }
 
-cudaError_t launch_state_density(double* dst, const void* src, bool fp64, const Geometry& g, int axis,
+cudaError_t launch_state_density(double* dst, const void* src, int real, const Geometry& g, int axis,
                                  const double* const* w, double* /*partials*/, cudaStream_t st) {
   const int64_t total = total_of(g);
   const Perm P = make_perm(g);
@@ -282,12 +294,13 @@ cudaError_t launch_state_density(double* dst, const void* src, bool fp64, const 
   int64_t na = 1;
   for (int q = 0; q < g.ndim; ++q)
     if (g.perm[q] == axis) na = g.sshape[q];
-  if (fp64)
-    state_density_kernel<double2><<<(unsigned)na, 256, 0, st>>>(dst, (const double2*)src, P, axis, W, total);
-  else
-    state_density_kernel<float2><<<(unsigned)na, 256, 0, st>>>(dst, (const float2*)src, P, axis, W, total);
+  const cudaError_t e = by_real(real, [&](auto t) {
+    using S = decltype(t);
+    state_density_kernel<S><<<(unsigned)na, 256, 0, st>>>(dst, (const S*)src, P, axis, W, total);
+    return cudaGetLastError();
+  });
   count_launch();
-  return cudaGetLastError();
+  return e;
 }
 
 template <typename D, typename S>
@@ -296,18 +309,18 @@ __global__ void convert_kernel(D* dst, const S* src, int64_t n) {
     dst[i] = D{(decltype(dst->x))src[i].x, (decltype(dst->x))src[i].y};
 }
 
-cudaError_t launch_copy_convert(void* dst, bool dst_fp64, const void* src, bool src_fp64, int64_t n,
+cudaError_t launch_copy_convert(void* dst, int dst_real, const void* src, int src_real, int64_t n,
                                 cudaStream_t st) {
-  if (dst_fp64 && src_fp64)
-    convert_kernel<double2, double2><<<blocks_for(n), 256, 0, st>>>((double2*)dst, (const double2*)src, n);
-  else if (dst_fp64)
-    convert_kernel<double2, float2><<<blocks_for(n), 256, 0, st>>>((double2*)dst, (const float2*)src, n);
-  else if (src_fp64)
-    convert_kernel<float2, double2><<<blocks_for(n), 256, 0, st>>>((float2*)dst, (const double2*)src, n);
-  else
-    convert_kernel<float2, float2><<<blocks_for(n), 256, 0, st>>>((float2*)dst, (const float2*)src, n);
+  const cudaError_t e = by_real(dst_real, [&](auto td) {
+    return by_real(src_real, [&](auto ts) {
+      using D = decltype(td);
+      using S = decltype(ts);
+      convert_kernel<D, S><<<blocks_for(n), 256, 0, st>>>((D*)dst, (const S*)src, n);
+      return cudaGetLastError();
+    });
+  });
   count_launch();
-  return cudaGetLastError();
+  return e;
 }
 
 __global__ void table_convert_kernel(float* dst, const double* src, int64_t n) {

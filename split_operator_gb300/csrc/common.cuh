@@ -21,6 +21,9 @@
 namespace so {
 
 constexpr int kMaxDims = 4;
+// state precisions: FP32 (float2), FP64 (double2), float-float (two FP32 per real, 16 bytes
+// per complex value like FP64)
+constexpr int kRealF32 = 0, kRealF64 = 1, kRealFF = 2;
 constexpr int kMaxOps = 24;
 constexpr int kMaxRed = 8;      // norm reductions per pass
 constexpr int kNumSlots = 256;  // FP64 scalar slots per engine
@@ -172,6 +175,7 @@ int fft_pair_block(const Geometry& g);    // threads per CTA of a planned pass (
 
 // Host launchers (lane_sweep.cu)
 cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s);
+cudaError_t launch_pass_ff(const PassParams& p, cudaStream_t s);
 cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s);
 size_t pass_smem_bytes(const PassParams& p, bool fp64);
 int pass_threads(const Geometry& g);
@@ -204,7 +208,7 @@ int angular_tc_trace_slots();
 cudaError_t bounded_wait_selftest(uint64_t limit_ns, unsigned long long* host_out);
 
 // Batched launches over many propagations' passes (block -> (instance, tile) by offsets)
-cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassParams* params_dev,
+cudaError_t launch_pass_batched(int real, bool sweep, bool fused, const PassParams* params_dev,
                                 const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
                                 cudaStream_t s, int radix = 0, int ct_lgn = 0);
 // log2 n when a planned FP32 FFT-pair pass can run the fixed-shape kernel, else 0
@@ -225,19 +229,20 @@ cudaError_t launch_angular_tc_batched(const void* params_dev, const void* owners
 
 // Auxiliary kernels (aux_kernels.cu)
 cudaError_t launch_scalar_program(const PassParams& p, cudaStream_t s);
+// real: the state precision of the device side (kRealF32, kRealF64, kRealFF)
 // dst (storage order, precision of dst) <- src (logical row-major complex128)
-cudaError_t launch_import(void* dst, bool dst_fp64, const double* src, const Geometry& g, cudaStream_t s);
+cudaError_t launch_import(void* dst, int dst_real, const double* src, const Geometry& g, cudaStream_t s);
 // storage order is the logical order / the transpose of a two-axis logical order (the
 // layouts whose import and export stay coalesced on both sides)
 bool layout_is_identity(const Geometry& g);
 bool layout_is_transpose2(const Geometry& g);
 // dst (logical row-major complex128) <- src (storage order)
-cudaError_t launch_export(double* dst, const void* src, bool src_fp64, const Geometry& g, cudaStream_t s);
+cudaError_t launch_export(double* dst, const void* src, int src_real, const Geometry& g, cudaStream_t s);
 // density |psi|^2 in logical order, and its weighted marginal along one logical axis
-cudaError_t launch_density(double* dst, const void* src, bool fp64, const Geometry& g, cudaStream_t s);
-cudaError_t launch_state_density(double* dst, const void* src, bool fp64, const Geometry& g, int axis,
+cudaError_t launch_density(double* dst, const void* src, int real, const Geometry& g, cudaStream_t s);
+cudaError_t launch_state_density(double* dst, const void* src, int real, const Geometry& g, int axis,
                                  const double* const* w, double* partials, cudaStream_t s);
-cudaError_t launch_copy_convert(void* dst, bool dst_fp64, const void* src, bool src_fp64, int64_t n,
+cudaError_t launch_copy_convert(void* dst, int dst_real, const void* src, int src_real, int64_t n,
                                 cudaStream_t s);
 cudaError_t launch_table_convert(void* dst, bool dst_fp64, const double* src_dev, int64_t count, cudaStream_t s);
 

@@ -9,9 +9,12 @@
 // (state_matrix_transformation.rs:48-73) and the norm folds of WaveFunction::norm
 // (wave_function.rs:68-85) used by LossChecker / LeakControl.
 //
-// FFT: Stockham autosort between two shared-memory buffers (radix 8 stages for FP64,
-// radix 16 for FP32, one smaller closing stage), register butterflies, twiddles from
-// an FP64-built table, the 1/sqrt(N) of the reference folded into the last stage.
+// State precisions: FP32 (float2), FP64 (double2) and float-float (ffc, ff.cuh: FP64's
+// kernels with float-float arithmetic).
+// FFT: Stockham autosort between two shared-memory buffers (radix 8 stages for FP64 and
+// float-float, radix 16 for FP32, one smaller closing stage), register butterflies,
+// twiddles from an FP64-built table, the 1/sqrt(N) of the reference folded into the last
+// stage.
 // Lanes shorter than 16 or of non power-of-two length use a direct DFT with the natural
 // table.  The lane matrix product also writes into the second buffer.
 // Norms: per-thread sums (FP32 in FP32 passes, FP64 in FP64 ones), fixed-order warp/block
@@ -20,8 +23,10 @@
 // The radial pass of the 2-D step ([FFT] [point-wise] [FFT] [point-wise] on contiguous
 // power-of-two FP32 lanes) runs the separate register-resident FFT-pair kernel below.
 #include <cstdio>
+#include <type_traits>
 
 #include "common.cuh"
+#include "ff.cuh"
 
 namespace so {
 
@@ -35,6 +40,22 @@ template <>
 struct Cx<float> {
   using T = float2;
 };
+template <>
+struct Cx<ff> {
+  using T = ffc;
+};
+
+template <typename R>
+constexpr bool kIsFF = std::is_same<R, ff>::value;
+
+// read-only cached load of a state-precision value
+template <typename T>
+__device__ __forceinline__ T ldg_(const T* p) {
+  if constexpr (std::is_same<T, ff>::value || std::is_same<T, ffc>::value)
+    return ldg_ff(p);
+  else
+    return __ldg(p);
+}
 
 template <typename C>
 __device__ __forceinline__ C cmul(C a, C b) {
@@ -102,7 +123,9 @@ __device__ __forceinline__ RotConst<R> rot_const(int which) {
 // fused multiply-add in the state precision
 template <typename R>
 __device__ __forceinline__ R fmar(R a, R b, R c) {
-  if constexpr (sizeof(R) == 4)
+  if constexpr (kIsFF<R>)
+    return a * b + c;
+  else if constexpr (sizeof(R) == 4)
     return fmaf(a, b, c);
   else
     return fma(a, b, c);
@@ -303,14 +326,26 @@ __device__ void mat_apply(C*& buf, C*& alt, const Geometry& g, const DevOp& op, 
       res = buf[sidx(l, j, ls)];
     } else if (real) {
       const R* mt = reinterpret_cast<const R*>(op.ptr) + (int64_t)sel * n * n;
-      R sr = 0, si = 0;
-      for (int k = 0; k < n; ++k) {
-        const R m = __ldg(mt + (int64_t)k * n + j);
-        const C x = buf[sidx(l, k, ls)];
-        sr += m * x.x;
-        si += m * x.y;
+      if constexpr (kIsFF<R>) {
+        // float-float: compensated dot products (FfDot)
+        FfDot sr, si;
+        for (int k = 0; k < n; ++k) {
+          const R m = ldg_(mt + (int64_t)k * n + j);
+          const C x = buf[sidx(l, k, ls)];
+          sr.add(m, x.x);
+          si.add(m, x.y);
+        }
+        res = C{sr.value(), si.value()};
+      } else {
+        R sr = 0, si = 0;
+        for (int k = 0; k < n; ++k) {
+          const R m = __ldg(mt + (int64_t)k * n + j);
+          const C x = buf[sidx(l, k, ls)];
+          sr += m * x.x;
+          si += m * x.y;
+        }
+        res = C{sr, si};
       }
-      res = C{sr, si};
     } else {
       const C* mt = reinterpret_cast<const C*>(op.ptr) + (int64_t)sel * n * n;
       C s = C{(R)0, (R)0};
@@ -499,7 +534,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
             const int l = pow2 ? (pt >> lg) : pt / n, x = pt - l * n;
             const int k = along ? x : lane_coord[l * kMaxDims + op.axis];
             const int si = sidx(l, x, ls);
-            buf[si] = cmul(buf[si], __ldg(reinterpret_cast<const typename Cx<R>::T*>(t) + k));
+            buf[si] = cmul(buf[si], ldg_(reinterpret_cast<const typename Cx<R>::T*>(t) + k));
           }
           __syncthreads();
           break;
@@ -535,7 +570,14 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, const int64_t til
         }
         case OP_SCALE: {
           // one thread forms sqrt(target / norm) in FP64, the block reads it back
-          if (tid == 0) scale_s = (R)sqrt(ld_slot(p.slots, op.b) / ld_slot(p.slots, op.c));
+          if (tid == 0) {
+            // FP32 uses the factor rounded to FP32; FP64 and float-float the FP64 value
+            const double f = sqrt(ld_slot(p.slots, op.b) / ld_slot(p.slots, op.c));
+            if constexpr (sizeof(R) == 4)
+              scale_s = (double)(float)f;
+            else
+              scale_s = f;
+          }
           __syncthreads();
           const R fr = (R)scale_s;
           for (int pt = tid; pt < total; pt += T) {
@@ -763,7 +805,7 @@ __device__ __forceinline__ void pair_butterflies(C (&v)[kPairV], int t, int T, i
     if (k > 0) {
 #pragma unroll
       for (int r = 1; r < RS; ++r) {
-        C w = __ldg(tw + (r - 1) * p + k);
+        C w = ldg_(tw + (r - 1) * p + k);
         if (dir > 0) w.y = -w.y;
         v[j * RS + r] = cmul(v[j * RS + r], w);
       }
@@ -791,7 +833,7 @@ __device__ __forceinline__ void pair_pointwise(C (&v)[kPairV], const PassParams&
       if (!nd || l < nl) {
         const int row = nd ? l * n : 0;
 #pragma unroll
-        for (int q = 0; q < RS; ++q) v[j * RS + q] = cmul(v[j * RS + q], __ldg(tab + row + k + q * p));
+        for (int q = 0; q < RS; ++q) v[j * RS + q] = cmul(v[j * RS + q], ldg_(tab + row + k + q * p));
       }
     }
   }
@@ -911,6 +953,11 @@ __global__ void __launch_bounds__(512, 1) fft_pair_kernel_f64(const __grid_const
   fft_pair_tile<double, 8>(p, blockIdx.x);
 }
 
+// float-float lanes of 8192 points (as FP64)
+__global__ void __launch_bounds__(512, 1) fft_pair_kernel_ff(const __grid_constant__ PassParams p) {
+  fft_pair_tile<ff, 8>(p, blockIdx.x);
+}
+
 template <typename R, int RMAX>
 __device__ __forceinline__ void fft_pair_batched_tile(const PassParams* __restrict__ params,
                                                       const int64_t* __restrict__ offsets, int count) {
@@ -943,6 +990,11 @@ __global__ void __launch_bounds__(512, 1) fft_pair_kernel_batched_f64(const Pass
 __global__ void __launch_bounds__(512, 2) fft_pair_kernel_batched_r8(const PassParams* __restrict__ params,
                                                                      const int64_t* __restrict__ offsets, int count) {
   fft_pair_batched_tile<float, 8>(params, offsets, count);
+}
+
+__global__ void __launch_bounds__(512, 1) fft_pair_kernel_batched_ff(const PassParams* __restrict__ params,
+                                                                     const int64_t* __restrict__ offsets, int count) {
+  fft_pair_batched_tile<ff, 8>(params, offsets, count);
 }
 
 static size_t fft_pair_smem(const Geometry& g, bool fp64);
@@ -1272,9 +1324,27 @@ static cudaError_t launch_batched_impl(const PassParams* params_dev, const int64
   return cudaGetLastError();
 }
 
-cudaError_t launch_pass_batched(bool fp64, bool sweep, bool fused, const PassParams* params_dev,
+cudaError_t launch_pass_batched(int real, bool sweep, bool fused, const PassParams* params_dev,
                                 const int64_t* offsets_dev, int count, int64_t blocks, int threads, size_t smem,
                                 cudaStream_t s, int radix, int ct_lgn) {
+  const bool fp64 = real != kRealF32;
+  if (real == kRealFF) {
+    if (fused) {
+      if (smem > 220 * 1024 || threads > 512) return cudaErrorInvalidValue;
+      static bool configured = false;
+      if (!configured) {
+        cudaError_t e =
+            cudaFuncSetAttribute(fft_pair_kernel_batched_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+        if (e != cudaSuccess) return e;
+        configured = true;
+      }
+      fft_pair_kernel_batched_ff<<<(unsigned)blocks, threads, smem, s>>>(params_dev, offsets_dev, count);
+      count_launch();
+      return cudaGetLastError();
+    }
+    return sweep ? launch_batched_impl<ff, 8, true>(params_dev, offsets_dev, count, blocks, threads, smem, s)
+                 : launch_batched_impl<ff, 8, false>(params_dev, offsets_dev, count, blocks, threads, smem, s);
+  }
   if (fused) {
     if (smem > 220 * 1024 || threads > 512) return cudaErrorInvalidValue;
     if (ct_lgn > 0 && !fp64 && radix != 8) {
@@ -1374,6 +1444,22 @@ cudaError_t launch_pass_f64(const PassParams& p, cudaStream_t s) {
     return cudaGetLastError();
   }
   return p.sweep ? launch_impl<double, 8, true>(p, s) : launch_impl<double, 8, false>(p, s);
+}
+cudaError_t launch_pass_ff(const PassParams& p, cudaStream_t s) {
+  if (p.fused) {
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(fft_pair_kernel_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    const size_t smem = fft_pair_smem(p.g, true);
+    if (smem > 220 * 1024) return cudaErrorInvalidValue;
+    fft_pair_kernel_ff<<<(unsigned)p.g.tiles, fft_pair_block(p.g), smem, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+  }
+  return p.sweep ? launch_impl<ff, 8, true>(p, s) : launch_impl<ff, 8, false>(p, s);
 }
 cudaError_t launch_pass_f32(const PassParams& p, cudaStream_t s) {
   if (p.fused) {

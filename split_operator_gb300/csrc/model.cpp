@@ -82,8 +82,9 @@ void ScalarState::set(size_t i, double v) {
 const char* op_kind_name(int k);
 static bool is_scalar_kind(int k) { return k == OP_COPY || k == OP_LOSS || k == OP_SETC || k == OP_RECORD; }
 
-Engine::Engine(const std::vector<size_t>& shp, const std::vector<int>& prm, bool f64)
-    : fp64(f64), shape(shp), perm(prm) {
+Engine::Engine(const std::vector<size_t>& shp, const std::vector<int>& prm, int rl)
+    : real(rl), fp64(rl != kRealF32), shape(shp), perm(prm) {
+  if (real < kRealF32 || real > kRealFF) throw Error(SO_ERR_INVALID, "unknown state precision");
   if (shape.empty() || shape.size() > (size_t)kMaxDims)
     throw Error(SO_ERR_UNSUPPORTED, "wave functions of 1 to 4 dimensions are supported");
   int dev_count = 0;
@@ -230,8 +231,21 @@ static void upload(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) {
   cuda_check(cudaStreamSynchronize(s), "table upload sync");
 }
 
-static void upload_complex(DeviceBuffer& buf, const std::vector<cplx>& t, bool fp64, cudaStream_t s) {
-  if (fp64) {
+// the float-float pair of d: hi = d rounded to FP32, lo = the (exact) remainder rounded
+static void ff_pair(double d, float* out) {
+  out[0] = (float)d;
+  out[1] = (float)(d - (double)out[0]);
+}
+
+static void upload_complex(DeviceBuffer& buf, const std::vector<cplx>& t, int real, cudaStream_t s) {
+  if (real == kRealFF) {
+    std::vector<float> v(4 * t.size());
+    for (size_t i = 0; i < t.size(); ++i) {
+      ff_pair(t[i].real(), &v[4 * i]);
+      ff_pair(t[i].imag(), &v[4 * i + 2]);
+    }
+    upload(buf, v, s);
+  } else if (real == kRealF64) {
     std::vector<double> v(2 * t.size());
     for (size_t i = 0; i < t.size(); ++i) {
       v[2 * i] = t[i].real();
@@ -252,7 +266,7 @@ const void* Engine::table_1d(const void* key, uint64_t version, const std::vecto
   auto& c = tables_[{key, 0}];
   if (c.buf.ptr && c.version == version) return c.buf.ptr;
   if (c.buf.ptr) flush();  // replacing a table the open pass may reference (a first upload needs no flush)
-  upload_complex(c.buf, t, fp64, stream);
+  upload_complex(c.buf, t, real, stream);
   c.version = version;
   return c.buf.ptr;
 }
@@ -280,7 +294,7 @@ const void* Engine::table_nd(const void* key, uint64_t version, const std::vecto
     }
     st[s] = t[li];
   }
-  upload_complex(c.buf, st, fp64, stream);
+  upload_complex(c.buf, st, real, stream);
   c.version = version;
   return c.buf.ptr;
 }
@@ -299,7 +313,11 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
     for (size_t j = 0; j < n; ++j)
       for (size_t k = 0; k < n; ++k) mt[b * n * n + k * n + j] = m[b * n * n + j * n + k];
   if (real) {
-    if (fp64) {
+    if (this->real == kRealFF) {
+      std::vector<float> v(2 * mt.size());
+      for (size_t i = 0; i < mt.size(); ++i) ff_pair(mt[i].real(), &v[2 * i]);
+      upload(c.buf, v, stream);
+    } else if (fp64) {
       std::vector<double> v(mt.size());
       for (size_t i = 0; i < mt.size(); ++i) v[i] = mt[i].real();
       upload(c.buf, v, stream);
@@ -309,7 +327,7 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
       upload(c.buf, v, stream);
     }
   } else {
-    upload_complex(c.buf, mt, fp64, stream);
+    upload_complex(c.buf, mt, this->real, stream);
   }
   c.version = version;
   c.real = real;
@@ -574,7 +592,7 @@ const void* Engine::twiddle(size_t n, int radix) {
     }
     tw.swap(st);
   }
-  upload_complex(b, tw, fp64, stream);
+  upload_complex(b, tw, real, stream);
   const void* p = b.ptr;
   twiddles_.emplace(std::make_pair(n, rmax), std::move(b));
   return p;
@@ -651,7 +669,8 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
     partials_ = DeviceBuffer(partials_cap_ * kMaxRed * sizeof(double));
     p.partials = partials_.as<double>();
   }
-  std::string name = std::string(fp64 ? "f64" : "f32") + (resident ? " resident" : " sweep") + name_tag + " axis" +
+  std::string name = std::string(real == kRealFF ? "ff" : (fp64 ? "f64" : "f32")) + (resident ? " resident" : " sweep") +
+                     name_tag + " axis" +
                      std::to_string(axis) + ":";
   for (const DevOp& o : ops) name += std::string(" ") + op_kind_name(o.kind);
   if (recording) {
@@ -660,7 +679,7 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
     const int threads = p.fused ? (fft_pair_block(p.g) | (1 << 16) | (p.radix == 8 && !fp64 ? 1 << 19 : 0) |
                                    (p.ct ? 1 << 20 : 0))
                                 : pass_threads(p.g);
-    RecordedPass r{resident ? RecordedPass::Resident : RecordedPass::Generic, fp64, p, {},
+    RecordedPass r{resident ? RecordedPass::Resident : RecordedPass::Generic, real, p, {},
                    threads, pass_smem_bytes(p, fp64), name, pass_bytes(ops, p.g)};
     recording->push_back(std::move(r));
     return;
@@ -669,7 +688,8 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
     timed_begin(name);
     timed_.back().bytes = pass_bytes(ops, p.g);
   }
-  cuda_check(fp64 ? launch_pass_f64(p, stream) : launch_pass_f32(p, stream), "pass launch");
+  cuda_check(real == kRealFF ? launch_pass_ff(p, stream) : (fp64 ? launch_pass_f64(p, stream) : launch_pass_f32(p, stream)),
+             "pass launch");
   if (timing) timed_end();
 }
 
@@ -753,7 +773,7 @@ void Engine::flush() {
     p.nops = (int)ops.size();
     for (size_t i = 0; i < ops.size(); ++i) p.ops[i] = ops[i];
     if (recording) {
-      recording->push_back(RecordedPass{RecordedPass::Scalar, fp64, p, {}, 32, 0, "scalar", 0.0});
+      recording->push_back(RecordedPass{RecordedPass::Scalar, real, p, {}, 32, 0, "scalar", 0.0});
       return;
     }
     cuda_check(launch_scalar_program(p, stream), "scalar launch");
@@ -839,19 +859,19 @@ void Engine::import_host(const double* host, bool copy_engine) {
   flush();
   const size_t b = points() * 16;
   const Geometry g = flat_geometry(*this);
-  if (fp64 && identity_perm(perm)) {
+  if (real == kRealF64 && identity_perm(perm)) {
     cuda_check(cudaMemcpyAsync(psi.ptr, host, b, cudaMemcpyHostToDevice, stream), "import copy");
     return;
   }
   if (!copy_engine && (identity_perm(perm) || layout_is_transpose2(g))) {
     if (const char* d = mapped_range(host, b)) {
-      cuda_check(launch_import(psi.ptr, fp64, reinterpret_cast<const double*>(d), g, stream), "import");
+      cuda_check(launch_import(psi.ptr, real, reinterpret_cast<const double*>(d), g, stream), "import");
       return;
     }
   }
   if (staging_.bytes < b) staging_ = DeviceBuffer(b);
   cuda_check(cudaMemcpyAsync(staging_.ptr, host, b, cudaMemcpyHostToDevice, stream), "import copy");
-  cuda_check(launch_import(psi.ptr, fp64, staging_.as<double>(), g, stream), "import");
+  cuda_check(launch_import(psi.ptr, real, staging_.as<double>(), g, stream), "import");
 }
 
 void Engine::export_host(double* host, bool sync, bool copy_engine) {
@@ -859,14 +879,14 @@ void Engine::export_host(double* host, bool sync, bool copy_engine) {
   const size_t b = points() * 16;
   const Geometry g = flat_geometry(*this);
   char* d = nullptr;
-  if (fp64 && identity_perm(perm)) {
+  if (real == kRealF64 && identity_perm(perm)) {
     cuda_check(cudaMemcpyAsync(host, psi.ptr, b, cudaMemcpyDeviceToHost, stream), "export copy");
   } else if (!copy_engine && (identity_perm(perm) || layout_is_transpose2(g)) &&
              (d = mapped_range(host, b)) != nullptr) {
-    cuda_check(launch_export(reinterpret_cast<double*>(d), psi.ptr, fp64, g, stream), "export");
+    cuda_check(launch_export(reinterpret_cast<double*>(d), psi.ptr, real, g, stream), "export");
   } else {
     if (staging_.bytes < b) staging_ = DeviceBuffer(b);
-    cuda_check(launch_export(staging_.as<double>(), psi.ptr, fp64, g, stream), "export");
+    cuda_check(launch_export(staging_.as<double>(), psi.ptr, real, g, stream), "export");
     cuda_check(cudaMemcpyAsync(host, staging_.ptr, b, cudaMemcpyDeviceToHost, stream), "export copy");
   }
   if (sync) cuda_check(cudaStreamSynchronize(stream), "export sync");
@@ -877,7 +897,7 @@ void Engine::export_host(double* host, bool sync, bool copy_engine) {
 void Engine::stage_in(const double* host) {
   flush();
   const size_t b = points() * 16;
-  if (fp64 && identity_perm(perm)) {
+  if (real == kRealF64 && identity_perm(perm)) {
     cuda_check(cudaMemcpyAsync(psi.ptr, host, b, cudaMemcpyHostToDevice, stream), "import copy");
     return;
   }
@@ -886,33 +906,33 @@ void Engine::stage_in(const double* host) {
 }
 
 void Engine::unstage_in() {
-  if (fp64 && identity_perm(perm)) return;
-  cuda_check(launch_import(psi.ptr, fp64, staging_.as<double>(), flat_geometry(*this), stream), "import");
+  if (real == kRealF64 && identity_perm(perm)) return;
+  cuda_check(launch_import(psi.ptr, real, staging_.as<double>(), flat_geometry(*this), stream), "import");
 }
 
 void Engine::stage_out() {
   flush();
-  if (fp64 && identity_perm(perm)) return;
+  if (real == kRealF64 && identity_perm(perm)) return;
   const size_t b = points() * 16;
   if (staging_.bytes < b) staging_ = DeviceBuffer(b);
-  cuda_check(launch_export(staging_.as<double>(), psi.ptr, fp64, flat_geometry(*this), stream), "export");
+  cuda_check(launch_export(staging_.as<double>(), psi.ptr, real, flat_geometry(*this), stream), "export");
 }
 
 void Engine::unstage_out(double* host) {
   const size_t b = points() * 16;
-  const void* src = (fp64 && identity_perm(perm)) ? psi.ptr : staging_.ptr;
+  const void* src = (real == kRealF64 && identity_perm(perm)) ? psi.ptr : staging_.ptr;
   cuda_check(cudaMemcpyAsync(host, src, b, cudaMemcpyDeviceToHost, stream), "export copy");
 }
 
 // ----------------------------------------------------------------- WaveFunction
 WaveFunction::WaveFunction(const std::vector<size_t>& shp, const std::vector<Grid>& g, const std::vector<int>& perm,
-                           bool fp64)
+                           int real)
     : shape(shp), grids(g) {
   if (grids.size() != shape.size()) throw Error(SO_ERR_SHAPE, "one grid per axis is required");
   for (size_t a = 0; a < shape.size(); ++a)
     if (grids[a].size() != shape[a]) throw Error(SO_ERR_SHAPE, "grid size differs from the array axis");
   for (const Grid& gr : grids) last_grid_names.push_back(gr.name);
-  eng = std::make_unique<Engine>(shape, perm, fp64);
+  eng = std::make_unique<Engine>(shape, perm, real);
   cache_slot = eng->alloc_slot(1.0);
 }
 
@@ -1205,7 +1225,7 @@ void StateSaver::record_frame(WaveFunction& wf, size_t frame) {
   if (two_d || wf.shape.size() == 1) {
     if (wf.points() != points) throw Error(SO_ERR_SHAPE, "saver grid sizes differ from the wave function");
     DeviceBuffer d(points * sizeof(double));
-    cuda_check(launch_density(d.as<double>(), e.psi.ptr, e.fp64, g, e.stream), "density");
+    cuda_check(launch_density(d.as<double>(), e.psi.ptr, e.real, g, e.stream), "density");
     std::vector<double> h(points);
     cuda_check(cudaMemcpyAsync(h.data(), d.ptr, points * sizeof(double), cudaMemcpyDeviceToHost, e.stream), "copy");
     cuda_check(cudaStreamSynchronize(e.stream), "sync");
@@ -1216,7 +1236,7 @@ void StateSaver::record_frame(WaveFunction& wf, size_t frame) {
       throw Error(SO_ERR_SHAPE, "state grid differs from the wave function axis");
     std::vector<const double*> w = wf.weight_ptrs();
     DeviceBuffer d(points * sizeof(double));
-    cuda_check(launch_state_density(d.as<double>(), e.psi.ptr, e.fp64, g, (int)axis, w.data(), nullptr, e.stream),
+    cuda_check(launch_state_density(d.as<double>(), e.psi.ptr, e.real, g, (int)axis, w.data(), nullptr, e.stream),
                "state density");
     std::vector<double> h(points);
     cuda_check(cudaMemcpyAsync(h.data(), d.ptr, points * sizeof(double), cudaMemcpyDeviceToHost, e.stream), "copy");
@@ -1251,9 +1271,9 @@ static std::vector<int> choose_perm(size_t ndim, const OperationStack& st) {
 
 Propagation::Propagation(WaveFunction& src, so_time_grid time, std::shared_ptr<OperationStack> stack, int prec)
     : precision(prec), time_(time), stack_(std::move(stack)) {
-  if (prec < SO_PRECISION_FP64 || prec > SO_PRECISION_FP32_BF16X6) throw Error(SO_ERR_INVALID, "unknown precision");
-  const bool fp64 = prec == SO_PRECISION_FP64;
-  wf_ = std::make_unique<WaveFunction>(src.shape, src.grids, choose_perm(src.shape.size(), *stack_), fp64);
+  if (prec < SO_PRECISION_FP64 || prec > SO_PRECISION_FLOAT_FLOAT) throw Error(SO_ERR_INVALID, "unknown precision");
+  const int real = prec == SO_PRECISION_FP64 ? kRealF64 : (prec == SO_PRECISION_FLOAT_FLOAT ? kRealFF : kRealF32);
+  wf_ = std::make_unique<WaveFunction>(src.shape, src.grids, choose_perm(src.shape.size(), *stack_), real);
   wf_->eng->tc_tf32 = prec == SO_PRECISION_FP32_TF32X3;
   wf_->eng->tc_bf16 = prec == SO_PRECISION_FP32_BF16X3;
   wf_->eng->tc_bf16x6 = prec == SO_PRECISION_FP32_BF16X6;
@@ -1437,7 +1457,7 @@ void Propagation::reset_losses() {
 std::unique_ptr<WaveFunction> Propagation::snapshot() {
   std::vector<int> ident(wf_->shape.size());
   std::iota(ident.begin(), ident.end(), 0);
-  auto w = std::make_unique<WaveFunction>(wf_->shape, wf_->grids, ident, true);
+  auto w = std::make_unique<WaveFunction>(wf_->shape, wf_->grids, ident, kRealF64);
   w->last_grid_names = wf_->last_grid_names;
   w->possible_norm_change = wf_->possible_norm_change;
   w->eng->write_slot(w->cache_slot, wf_->eng->read_slot(wf_->cache_slot));
@@ -1454,7 +1474,9 @@ std::unique_ptr<WaveFunction> Propagation::snapshot() {
 //   possible_norm_change u8, norm cache f64, per axis: current grid name, last seen name;
 //   operator count u64, per operator: type name, scalar count u64, scalars f64 x count,
 //   saver flag u8 [current_frame u64, times, data]; then the state as complex128 in the
-//   logical row-major order (exact for both state precisions: FP32 values are FP64 values).
+//   logical row-major order (exact for FP64 and FP32 states: FP32 values are FP64 values);
+//   a float-float state adds its device words (storage order, FP32 hi / lo pairs) as a
+//   vector of 8-byte words, since hi + lo does not always fit one FP64 value.
 namespace {
 struct BlobWriter {
   std::vector<unsigned char> b;
@@ -1542,6 +1564,12 @@ std::vector<unsigned char> Propagation::checkpoint() {
   std::vector<double> host(wf_->points() * 2);
   e.export_host(host.data());
   w.vec(host);
+  if (e.real == kRealFF) {
+    std::vector<double> raw(wf_->points() * 2);
+    cuda_check(cudaMemcpyAsync(raw.data(), e.psi.ptr, e.psi.bytes, cudaMemcpyDeviceToHost, e.stream), "state copy");
+    cuda_check(cudaStreamSynchronize(e.stream), "state copy sync");
+    w.vec(raw);
+  }
   e.check_nonfinite();
   return std::move(w.b);
 }
@@ -1595,10 +1623,21 @@ void Propagation::restore(const unsigned char* data, size_t size) {
   }
   const std::vector<double> host = r.vec();
   if (host.size() != wf_->points() * 2) throw Error(SO_ERR_SHAPE, "checkpoint state has another size");
+  Engine& e = *wf_->eng;
+  std::vector<double> raw;
+  if (e.real == kRealFF) {
+    raw = r.vec();
+    if (raw.size() * sizeof(double) != e.psi.bytes) throw Error(SO_ERR_SHAPE, "checkpoint state has another size");
+  }
   if (r.off != size) throw Error(SO_ERR_INVALID, "checkpoint has trailing bytes");
   // apply
-  Engine& e = *wf_->eng;
-  e.import_host(host.data());
+  if (e.real == kRealFF) {
+    e.flush();
+    cuda_check(cudaMemcpyAsync(e.psi.ptr, raw.data(), e.psi.bytes, cudaMemcpyHostToDevice, e.stream), "state copy");
+    cuda_check(cudaStreamSynchronize(e.stream), "state copy sync");
+  } else {
+    e.import_host(host.data());
+  }
   e.write_slot(wf_->cache_slot, cached_norm);
   wf_->possible_norm_change = pnc;
   wf_->last_grid_names = last;
@@ -1744,14 +1783,14 @@ std::vector<Batch::Group> Batch::build_groups(const std::vector<std::vector<Reco
     if (rp.kind == RecordedPass::Scalar || rp.kind == RecordedPass::Resident)
       throw Error(SO_ERR_UNSUPPORTED, "pass kind cannot be batched");
     const int64_t ext = (rp.kind == RecordedPass::Generic && rp.p.fused) ? rp.p.g.n : 0;
-    by[{(int)rp.kind, rp.fp64 ? 1 : 0, rp.threads, rp.smem, ext}].push_back(&rp);
+    by[{(int)rp.kind, rp.real, rp.threads, rp.smem, ext}].push_back(&rp);
   }
   std::vector<Group> out;
   for (auto& kv : by) {
     const auto& v = kv.second;
     Group g{};
     g.kind = v[0]->kind;
-    g.fp64 = v[0]->fp64;
+    g.real = v[0]->real;
     g.threads = v[0]->threads;
     g.smem = v[0]->smem;
     g.count = (int)v.size();
@@ -1858,7 +1897,7 @@ void Batch::run_groups(std::vector<Group>& gs, bool concurrent) {
         t.cls_mode = (g.threads >> 17) & 3;
       } else if ((g.threads >> 16) & 1) {
         t.cls_kind = 0;
-        t.cls_mode = g.fp64 ? 1 : 0;
+        t.cls_mode = g.real != kRealF32 ? 1 : 0;
       }
       t.cls_n = g.n;
       cuda_check(cudaEventCreate(&t.a), "event");
@@ -1870,7 +1909,7 @@ void Batch::run_groups(std::vector<Group>& gs, bool concurrent) {
                                            st, (g.threads >> 20) & 3, 1 << ((g.threads >> 23) & 3)),
                  "batched tensor-core pass");
     else
-      cuda_check(launch_pass_batched(g.fp64, g.sweep, (g.threads >> 16) & 1, g.params.as<PassParams>(),
+      cuda_check(launch_pass_batched(g.real, g.sweep, (g.threads >> 16) & 1, g.params.as<PassParams>(),
                                      g.offsets.as<int64_t>(), g.count, g.blocks, g.threads & 0xffff, g.smem, st,
                                      ((g.threads >> 19) & 1) ? 8 : 0,
                                      g.ct_lgn),
@@ -2127,7 +2166,7 @@ std::string Batch::tune(const std::string& cache_path, int trial_steps) {
         const int mode = (r.threads >> 17) & 3;
         // (CTAs per SM, blocked order); the first candidate is the built-in default
         cands[{1, r.p.g.n, mode}] = {{2, 1}, {2, 0}, {1, 1}, {1, 0}};
-      } else if (r.kind == RecordedPass::Generic && r.p.fused && !r.fp64) {
+      } else if (r.kind == RecordedPass::Generic && r.p.fused && r.real == kRealF32) {
         // (threads per CTA, radix); lanes of n points need 16 threads >= n
         std::vector<std::pair<int, int>> v{{fft_pair_threads(r.p.g), 16}};
         for (int t : {128, 256, 512})

@@ -103,7 +103,7 @@ struct Action {
 // A pass captured instead of launched (batched execution of many propagations).
 struct RecordedPass {
   enum Kind { Generic, TensorCore, Scalar, Resident } kind;
-  bool fp64;
+  int real;  // state precision (kRealF32, kRealF64, kRealFF)
   PassParams p;
   std::vector<unsigned char> tcp;  // TcParams bytes (TensorCore)
   int threads;
@@ -114,10 +114,12 @@ struct RecordedPass {
 
 class Engine {
  public:
-  Engine(const std::vector<size_t>& shape, const std::vector<int>& perm, bool fp64);
+  // real: the state precision, kRealF32, kRealF64 or kRealFF (float-float)
+  Engine(const std::vector<size_t>& shape, const std::vector<int>& perm, int real);
   ~Engine();
 
-  bool fp64;
+  int real;
+  bool fp64;  // 16-byte complex values (FP64 or float-float): the FP64 kernels' shapes
   std::vector<size_t> shape;  // logical
   std::vector<int> perm;      // storage position -> logical axis
   DeviceBuffer psi;
@@ -235,7 +237,7 @@ struct WaveFunction {
   int cache_slot = -1;  // change_observer.rs:10 (last_norm), on the device
 
   WaveFunction(const std::vector<size_t>& shape, const std::vector<Grid>& grids, const std::vector<int>& perm,
-               bool fp64);
+               int real);
   std::vector<const double*> weight_ptrs();
   void set_weights(DevOp& op);  // op.w / op.wf: FP64 and FP32 weights per logical axis
   size_t points() const;
@@ -481,7 +483,7 @@ class Batch {
  private:
   struct Group {
     RecordedPass::Kind kind;
-    bool fp64;
+    int real;
     bool sweep = false;  // lane-sweep groups: every member's pass runs the compact sweep kernel
     int threads;
     size_t smem;

@@ -52,7 +52,7 @@ def _radial_polar_omega(lib, nr, nth, nom, mass, dt):
     return wf, tg, st
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 2e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("float_float", 1e-11), ("fp32_simt", 2e-6)])
 def test_associated_legendre_operator_propagation_matches_oracle(so, precision, tol):
     nr, nth, nom, steps = 128, 16, 3, 4
     wf, tg, st = _radial_polar_omega(so, nr, nth, nom, 50.0, 0.2)

@@ -24,13 +24,14 @@ def _two_d(precision, nr=512, nth=32, seed=7):
     return W.radial_angular_2d(nr=nr, nth=nth, step_no=1000, seed=seed, r0=25.0, precision=precision)[0]
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32_tf32x3", "fp32_bf16x6"])
+@pytest.mark.parametrize("precision", ["fp64", "float_float", "fp32_tf32x3", "fp32_bf16x6"])
 def test_resume_equals_uninterrupted_2d(so, precision):
-    """The restored propagation continues bit for bit like the one that took the checkpoint.
-    In FP64 that is also bit for bit the run that never stopped.  In FP32 a run split at a
-    step boundary closes its last pass there (the uninterrupted run fuses the end of one step
-    with the start of the next into one pass), and FP32 rounds the same operations in another
-    order, so it differs from the uninterrupted run by rounding only."""
+    """The restored propagation continues bit for bit like the one that took the checkpoint
+    (a float-float checkpoint carries the state's device words).  In FP64 that is also bit
+    for bit the run that never stopped.  In FP32 and float-float a run split at a step
+    boundary closes its last pass there (the uninterrupted run fuses the end of one step with
+    the start of the next into one pass), and those precisions round the same operations in
+    another order, so they differ from the uninterrupted run by rounding only."""
     n = 7
     whole = _two_d(precision)
     whole.steps(2 * n)
@@ -53,8 +54,9 @@ def test_resume_equals_uninterrupted_2d(so, precision):
         assert resumed.all_losses() == whole.all_losses()
         assert resumed.norm() == whole.norm()
     else:
-        assert rel_l2(resumed.get_array(), whole.get_array()) < 1e-5
-        assert abs(resumed.all_losses()[0] - whole.all_losses()[0]) < 1e-7
+        tol = 1e-12 if precision == "float_float" else 1e-5
+        assert rel_l2(resumed.get_array(), whole.get_array()) < tol
+        assert abs(resumed.all_losses()[0] - whole.all_losses()[0]) < tol / 100
 
 
 def _harmonic_imaginary(so, frames=10, steps=40):

@@ -10,6 +10,9 @@ dt = 0.5, border damping with a loss checker), 10^4 real-time steps.
   16 significand bits, so each operand carries a relative error up to 2^-17 ~ 7.6e-6);
   the accumulated error at 10^2, 10^3 and 10^4 steps is reported (written to
   precision_report.json in $SO_REPORT_DIR when set).
+* The float-float state against the FP64 GPU path: one step within 1e-11, and still within
+  the metric's 1e-6 after 10^4 steps (the FP32 modes are not), with its norm and energy
+  close to FP64's.
 """
 import json
 import os
@@ -24,8 +27,9 @@ pytestmark = pytest.mark.gpu
 
 NR, NTH = 4096, 128
 CHECKPOINTS = (100, 1000, 10000)
-FP32_MODES = ("fp32_simt", "fp32_tf32x3", "fp32_bf16x3", "fp32_bf16x6")
-ONE_STEP_TOL = {"fp32_simt": 1e-6, "fp32_tf32x3": 1e-6, "fp32_bf16x3": 2e-5, "fp32_bf16x6": 1e-6}
+FP32_MODES = ("fp32_simt", "fp32_tf32x3", "fp32_bf16x3", "fp32_bf16x6", "float_float")
+ONE_STEP_TOL = {"fp32_simt": 1e-6, "fp32_tf32x3": 1e-6, "fp32_bf16x3": 2e-5, "fp32_bf16x6": 1e-6,
+                "float_float": 1e-11}
 
 
 def _norm(psi, wr, wth):
@@ -103,3 +107,6 @@ def test_long_run_fp64_vs_cpu_restatement_and_fp32_modes(tmp_path):
     assert abs(energy["fp64"] - energy["cpu"]) <= 1e-9 * abs(energy["cpu"])
     for m in FP32_MODES:
         assert np.isfinite(last[m]["rel_l2_vs_fp64"])
+    ff = last["float_float"]
+    assert ff["rel_l2_vs_fp64"] <= 1e-6 and abs(ff["norm_drift"]) <= 1e-8 and abs(ff["loss_diff"]) <= 1e-8, ff
+    assert abs(energy["float_float"] - energy["fp64"]) <= 1e-8 * abs(energy["fp64"])

@@ -238,7 +238,7 @@ def _unitary(rng, n, count):
     return np.stack([np.linalg.qr(m)[0] for m in z])
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 2e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("float_float", 1e-11), ("fp32_simt", 2e-6)])
 @pytest.mark.parametrize("count", [40, 64])
 def test_non_diag_propagator_matches_oracle(so, precision, tol, count):
     """NonDiagPropagator (non_diagonal_propagator.rs:9-66): a matrix per lane along axis 1,
@@ -271,7 +271,7 @@ def test_non_diag_propagator_matches_oracle(so, precision, tol, count):
         assert rel_l2(prop.get_array(), oprop.wave_function.array) < tol * (k + 1)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 2e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("float_float", 1e-11), ("fp32_simt", 2e-6)])
 def test_state_matrix_transformation_matches_oracle(so, precision, tol):
     """StateMatrixTransformation (state_matrix_transformation.rs:8-73): matrix i acts along
     axis 0 on slice i of the dependent axis 1; transform in the first half-step, inverse in
@@ -306,7 +306,7 @@ def test_state_matrix_transformation_matches_oracle(so, precision, tol):
         assert rel_l2(prop.get_array(), oprop.wave_function.array) < tol * (k + 1)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 3e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("float_float", 1e-11), ("fp32_simt", 3e-6)])
 def test_three_dim_two_fft_axes_matches_oracle(so, precision, tol):
     """A 3-D state with FFTs along axes 0 and 2 (a power-of-two lane and a 24-point lane, so
     the passes run strided lanes and the direct DFT), kinetic phases along both, and a full
@@ -342,7 +342,7 @@ def test_three_dim_two_fft_axes_matches_oracle(so, precision, tol):
     assert abs(prop.norm() - oprop.wave_function.norm()) < 10 * tol * abs(oprop.wave_function.norm())
 
 
-@pytest.mark.parametrize("precision,n", [("fp32_simt", 16384), ("fp64", 16384)])
+@pytest.mark.parametrize("precision,n", [("fp32_simt", 16384), ("fp64", 16384), ("float_float", 16384)])
 def test_lanes_beyond_the_tile_limit_are_rejected(so, precision, n):
     """A lane longer than a CTA tile holds (8192 points) is refused with a status before any
     kernel runs; the context stays usable."""
@@ -365,7 +365,7 @@ def test_fp64_lanes_beyond_4096_need_the_fft_pair_form(so):
     assert "not supported" in str(e.value)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_tf32x3", 1e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("float_float", 1e-11), ("fp32_tf32x3", 1e-6)])
 def test_radial_angular_8192_lanes_match_oracle(so, precision, tol):
     """Nr = 8192 (the longest radial lanes of the batched workload): the FP64 FFT-pair kernel
     (radix-8 stages, 16 values per thread) and the FP32 tensor-core + FFT-pair step against the
@@ -383,7 +383,7 @@ def test_radial_angular_8192_lanes_match_oracle(so, precision, tol):
     assert any("fftpair" in t[0] for t in prop.kernel_times())
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_simt", 3e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("float_float", 1e-11), ("fp32_simt", 3e-6)])
 def test_two_dim_savers_match_oracle(so, precision, tol):
     """WaveFunctionSaver (|psi|^2 frames) and StateSaver (state_density along an axis) on a
     2-D propagation, saved at the first half of every step_no / frames_no-th step
