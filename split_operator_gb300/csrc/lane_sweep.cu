@@ -309,12 +309,74 @@ __device__ void dft_direct(C*& buf, C*& alt, const Geometry& g, int dir, const C
   alt = t;
 }
 
+// Float-float lane <- M lane for a real matrix with the parity structure of a Legendre
+// pair (flags bits 1-2; the matrix in op.ptr is then the half matrix H, h = n / 2):
+//   kind 1, M[a][n-1-b] = (-1)^a M[a][b] (a transform with quadrature weights):
+//     out_a = sum_{b<h} H[a][b] (x_b + (-1)^a x_{n-1-b}),   H stored HT[b n + a];
+//   kind 2, M[n-1-b][a] = (-1)^a M[b][a] (its inverse): with E_b / O_b the sums over the
+//     even / odd a of H[b][a] x_a, out_b = E_b + O_b and out_{n-1-b} = E_b - O_b,
+//     H stored HT[a h + b].
+// Half the products of the plain form.  The result ends in buf (the pointers swap for kind 2).
+template <typename C>
+__device__ void mat_apply_parity_ff(C*& buf, C*& alt, const Geometry& g, const DevOp& op, int kind) {
+  const int n = (int)g.n, L = g.lanes_per_tile, ls = g.lane_stride, h = n / 2;
+  const ff* ht = reinterpret_cast<const ff*>(op.ptr);
+  if (kind == 1) {
+    // S_b = x_b + x_{n-1-b} and D_b = x_b - x_{n-1-b} into alt (S at b, D at h + b)
+    for (int o = threadIdx.x; o < L * h; o += blockDim.x) {
+      const int l = o / h, b = o - l * h;
+      const C x0 = buf[sidx(l, b, ls)], x1 = buf[sidx(l, n - 1 - b, ls)];
+      alt[sidx(l, b, ls)] = cadd(x0, x1);
+      alt[sidx(l, h + b, ls)] = csub(x0, x1);
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < L * n; o += blockDim.x) {
+      const int l = o / n, a = o - l * n, off = (a & 1) ? h : 0;
+      FfDot sr, si;
+      for (int b = 0; b < h; ++b) {
+        const ff m = ldg_ff(ht + (int64_t)b * n + a);
+        const C x = alt[sidx(l, off + b, ls)];
+        sr.add(m, x.x);
+        si.add(m, x.y);
+      }
+      buf[sidx(l, a, ls)] = C{sr.value(), si.value()};
+    }
+  } else {
+    for (int o = threadIdx.x; o < L * h; o += blockDim.x) {
+      const int l = o / h, b = o - l * h;
+      FfDot er, ei, orr, oi;
+      for (int a = 0; a < n; a += 2) {
+        const ff me = ldg_ff(ht + (int64_t)a * h + b), mo = ldg_ff(ht + (int64_t)(a + 1) * h + b);
+        const C xe = buf[sidx(l, a, ls)], xo = buf[sidx(l, a + 1, ls)];
+        er.add(me, xe.x);
+        ei.add(me, xe.y);
+        orr.add(mo, xo.x);
+        oi.add(mo, xo.y);
+      }
+      const ff e_r = er.value(), e_i = ei.value(), o_r = orr.value(), o_i = oi.value();
+      alt[sidx(l, b, ls)] = C{e_r + o_r, e_i + o_i};
+      alt[sidx(l, n - 1 - b, ls)] = C{e_r - o_r, e_i - o_i};
+    }
+    C* t = buf;
+    buf = alt;
+    alt = t;
+  }
+  __syncthreads();
+}
+
 // lane <- M lane.  Matrices are stored transposed (MT[k*n + j] = M[j][k]) so that
 // threads with consecutive j read consecutive addresses; real matrices store one
 // real per entry.  `sel` picks the matrix of a lane (-1: leave the lane as it is).
 template <typename C>
 __device__ void mat_apply(C*& buf, C*& alt, const Geometry& g, const DevOp& op, const int* lane_sel) {
   using R = decltype(buf[0].x);
+  if constexpr (kIsFF<R>) {
+    const int par = (op.flags >> 1) & 3;
+    if (par && !lane_sel) {
+      mat_apply_parity_ff(buf, alt, g, op, par);
+      return;
+    }
+  }
   const int n = (int)g.n, L = g.lanes_per_tile, ls = g.lane_stride;
   const int total = L * n;
   const bool real = op.flags & 1;

@@ -299,11 +299,35 @@ const void* Engine::table_nd(const void* key, uint64_t version, const std::vecto
   return c.buf.ptr;
 }
 
+// Parity structure of a real n x n matrix (logical M[a][b] = m[a n + b]) within tol of its
+// largest entry: 1 when M[a][n-1-b] = (-1)^a M[a][b] (a Legendre transform with quadrature
+// weights), 2 when M[n-1-b][a] = (-1)^a M[b][a] (its inverse), else 0.
+static int lane_matrix_parity(const std::vector<cplx>& m, size_t n, double rel_tol) {
+  if (n < 16 || n % 2) return 0;
+  double amax = 0.0;
+  for (const cplx& v : m) amax = std::max(amax, std::fabs(v.real()));
+  const double tol = rel_tol * amax;
+  bool rowp = true, colp = true;
+  for (size_t a = 0; a < n && (rowp || colp); ++a) {
+    const double sg = (a & 1) ? -1.0 : 1.0;
+    for (size_t b = 0; b < n; ++b) {
+      if (rowp && std::fabs(m[a * n + (n - 1 - b)].real() - sg * m[a * n + b].real()) > tol) rowp = false;
+      if (colp && std::fabs(m[(n - 1 - b) * n + a].real() - sg * m[b * n + a].real()) > tol) colp = false;
+    }
+  }
+  return rowp ? 1 : (colp ? 2 : 0);
+}
+
 const void* Engine::matrices(const void* key, uint64_t version, const std::vector<cplx>& m, size_t n, size_t count,
-                             bool& real) {
+                             bool& real, int* parity) {
   auto& c = tables_[{key, 2}];
+  if (parity) *parity = 0;
   if (c.buf.ptr && c.version == version) {
     real = c.real;
+    if (parity && c.parity) {
+      *parity = c.parity;
+      return c.half_buf.ptr;
+    }
     return c.buf.ptr;
   }
   if (c.buf.ptr) flush();
@@ -331,6 +355,32 @@ const void* Engine::matrices(const void* key, uint64_t version, const std::vecto
   }
   c.version = version;
   c.real = real;
+  c.parity = 0;
+  if (this->real == kRealFF && real && count == 1) {
+    // float-float Legendre pairs: the half matrix of the parity form, each entry the mean of
+    // the two it stands for (the structure holds to ~1e-14 of the largest entry: the nodes'
+    // cosines are symmetric to an ulp), in the layout mat_apply_parity_ff reads
+    const int kind = lane_matrix_parity(m, n, 1e-13);
+    if (kind) {
+      const size_t h = n / 2;
+      std::vector<float> v(2 * n * h);
+      for (size_t a = 0; a < n; ++a)
+        for (size_t b = 0; b < h; ++b) {
+          const double sg = (a & 1) ? -1.0 : 1.0;
+          if (kind == 1) {  // H[a][b] at b n + a
+            ff_pair(0.5 * (m[a * n + b].real() + sg * m[a * n + (n - 1 - b)].real()), &v[2 * (b * n + a)]);
+          } else {          // H[b][a] at a h + b
+            ff_pair(0.5 * (m[b * n + a].real() + sg * m[(n - 1 - b) * n + a].real()), &v[2 * (a * h + b)]);
+          }
+        }
+      upload(c.half_buf, v, stream);
+      c.parity = kind;
+      if (parity) {
+        *parity = kind;
+        return c.half_buf.ptr;
+      }
+    }
+  }
   if (!fp64 && tc_mode() >= 0 && real && count == 1 && (n == 32 || n == 64 || n == 128 || n == 256)) {
     std::vector<double> md(n * n);
     for (size_t i = 0; i < n * n; ++i) md[i] = m[i].real();
@@ -1110,9 +1160,10 @@ static void emit_mat(WaveFunction& wf, Emitter& em, const void* key, uint64_t ve
   if (dim >= wf.shape.size() || wf.shape[dim] != n) throw Error(SO_ERR_SHAPE, "matrix size differs from the axis");
   Action a{};
   bool real = false;
+  int parity = 0;
   a.op.kind = OP_MAT;
-  a.op.ptr = wf.eng->matrices(key, version, m, n, 1, real);
-  a.op.flags = real ? 1 : 0;
+  a.op.ptr = wf.eng->matrices(key, version, m, n, 1, real, &parity);
+  a.op.flags = (real ? 1 : 0) | (parity << 1);
   a.lane_axis = (int)dim;
   em.emit(a);
 }

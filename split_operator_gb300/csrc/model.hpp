@@ -151,8 +151,10 @@ class Engine {
   // device copies of host tables (state precision), cached by key
   const void* table_1d(const void* key, uint64_t version, const std::vector<cplx>& t);
   const void* table_nd(const void* key, uint64_t version, const std::vector<cplx>& t);
+  // parity (optional): float-float single real matrices with the parity structure of a
+  // Legendre pair get 1 or 2 (the kind) and the returned pointer is then the half matrix
   const void* matrices(const void* key, uint64_t version, const std::vector<cplx>& m, size_t n, size_t count,
-                       bool& real);
+                       bool& real, int* parity = nullptr);
   const double* weights(const Grid& g);
   const void* twiddle(size_t n, int radix = 0);  // radix 0: the precision's default stage order
 
@@ -203,6 +205,8 @@ class Engine {
     uint64_t version;
     DeviceBuffer buf;
     bool real;
+    int parity = 0;     // float-float: kind of the parity structure, half matrix in half_buf
+    DeviceBuffer half_buf;
     // A-operand chunk images of the tensor-core passes, and the same for the parity-split
     // form (when the matrix has it): shared by every engine of the process whose matrix has
     // the same values (all propagations on one polar grid), so one copy stays hot in L2
