@@ -365,7 +365,8 @@ def test_fp64_lanes_beyond_4096_need_the_fft_pair_form(so):
     assert "not supported" in str(e.value)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("float_float", 1e-11), ("fp32_tf32x3", 1e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("float_float", 1e-11), ("fp32_tf32x3", 1e-6),
+                                           ("fp32_bf16x6", 1e-6)])
 def test_radial_angular_8192_lanes_match_oracle(so, precision, tol):
     """Nr = 8192 (the longest radial lanes of the batched workload): the FP64 FFT-pair kernel
     (radix-8 stages, 16 values per thread) and the FP32 tensor-core + FFT-pair step against the

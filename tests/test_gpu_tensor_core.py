@@ -136,6 +136,26 @@ def test_radial_angular_tf32x3_close_to_oracle(so, nr, nth, precision):
     assert abs(prop.norm() - oprop.wave_function.norm()) < (6e-5 if nth == 256 else 2.5e-5)
 
 
+@pytest.mark.parametrize("precision,tol", [("fp32_bf16x6", 1e-6), ("fp32_tf32x3", 1e-6), ("fp32_bf16x3", 2e-5)])
+def test_full_step_at_4096x128_matches_oracle(so, precision, tol):
+    """The whole 2-D step at 4096 x 128 (Morse + P2, Legendre pair on the tensor cores, the
+    fixed-shape radial FFT pair, border damping with a loss checker) in each tensor-core
+    mode, step by step against the FP64 oracle (propagation.rs:134-190)."""
+    from split_operator_gb300 import workloads as W
+    steps = 3
+    prop, _ = W.radial_angular_2d(nr=4096, nth=128, step_no=steps, seed=2026, precision=precision)
+    oprop, _ = S.radial_angular_2d(nr=4096, nth=128, step_no=steps, seed=2026)
+    prop.set_timing(True)
+    for k in range(steps):
+        prop.steps(1)
+        oprop.step()
+        assert rel_l2(prop.get_array(), oprop.wave_function.array) < tol * (k + 1), k
+    assert abs(prop.all_losses()[0] - oprop.all_losses()[0][1]) < tol
+    names = " ".join(t[0] for t in prop.kernel_times())
+    tag = {"fp32_bf16x6": "tcbf16x6", "fp32_tf32x3": "tc3xtf32", "fp32_bf16x3": "tcbf16x3"}[precision]
+    assert tag in names and "fftpair" in names, names
+
+
 @pytest.mark.parametrize("precision", ["fp32_tf32x3", "fp32_bf16x6"])
 def test_parity_split_legendre_pair_matches_plain_form(so, monkeypatch, precision):
     """n = 256 Legendre pair: the parity-split GEMMs (two K = 128 halves) give the same
