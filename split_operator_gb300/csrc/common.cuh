@@ -169,7 +169,7 @@ bool schedules_from_json(const std::string& text);
 // FFT pair pass (lane_sweep.cu): [FFT] [DIAG1D along / DIAGND]* [FFT] [DIAG1D along / DIAGND]*
 // over contiguous power-of-two FP32 lanes, every thread holding 16 values in registers.
 // fft_pair_plan checks the pass and sets its tiling (lanes per tile, tiles) and p.fused.
-bool fft_pair_plan(PassParams& p, bool fp64, bool resident);
+bool fft_pair_plan(PassParams& p, int real, bool resident);
 int fft_pair_threads(const Geometry& g);  // the default threads per CTA
 int fft_pair_block(const Geometry& g);    // threads per CTA of a planned pass (lanes per tile x n / 16)
 

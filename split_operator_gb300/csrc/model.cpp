@@ -705,7 +705,7 @@ void Engine::launch(const std::vector<DevOp>& ops, int axis, bool resident, int 
   if (fft) p.twiddle = twiddle((size_t)p.g.n);
   pass_choose_buffers(p, fp64);
   if (!fp64 && tc_mode() >= 0 && !resident && try_launch_tc(ops, axis, p)) return;
-  if ((fft_pair || (fp64 && p.g.n > 4096)) && fft_pair_plan(p, fp64, resident)) {
+  if ((fft_pair || (fp64 && p.g.n > 4096)) && fft_pair_plan(p, real, resident)) {
     name_tag = p.radix == 8 && !fp64 ? " fftpair r8" : " fftpair";
     if (p.radix != (fp64 ? 8 : 16)) p.twiddle = twiddle((size_t)p.g.n, p.radix);  // the table in its stage order
     p.ct = fft_pair_ct ? fft_pair_ct_lgn(p, fp64) : 0;
