@@ -384,9 +384,14 @@ def run_ours(a):
 
     # end to end through the C ABI: pinned FP64 host state in, one step, state out
     e2e_steps = 5
-    hosts = [torch.empty(int(np.prod(p.wave_function_shape())) * 2, dtype=torch.float64).pin_memory()
-             for p in props]
-    outs = [torch.empty_like(h).pin_memory() for h in hosts]
+    # every instance's state back to back in one pinned array (in and out), in member order:
+    # the library then moves each pipeline chunk with one copy per direction
+    sizes = [int(np.prod(p.wave_function_shape())) * 2 for p in props]
+    host_in = torch.empty(sum(sizes), dtype=torch.float64).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    hosts = [host_in[int(offs[k]):int(offs[k + 1])] for k in range(len(props))]
+    outs = [host_out[int(offs[k]):int(offs[k + 1])] for k in range(len(props))]
     for p, h in zip(props, hosts):
         h.numpy()[:] = p.get_array().view(np.float64).ravel()
     in_ptrs, out_ptrs = [h.data_ptr() for h in hosts], [o.data_ptr() for o in outs]
@@ -438,7 +443,8 @@ def run_ours(a):
                                                                "GPU model"},
            "note": ("every step: one so_batch_steps_host call: pinned FP64 host states of all instances in, one "
                     "step, states out to pinned host buffers, pipelined over 16 instance chunks on their own "
-                    "streams (copy engines both ways)") if not single else
+                    "streams (copy engines both ways); the instances' states lie back to back in one pinned "
+                    "array per direction, so each chunk moves with one copy per direction") if not single else
                    "every step: so_propagation_set_array from a pinned FP64 host buffer, one step, "
                    "so_propagation_get_array into a pinned host buffer"}
 

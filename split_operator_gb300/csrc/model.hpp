@@ -171,6 +171,9 @@ class Engine {
   void unstage_in();
   void stage_out();
   void unstage_out(double* host);
+  // the layout halves alone, from / to a logical complex128 array already in device memory
+  void import_device(const double* dev);
+  void export_device(double* dev);
   void export_host(double* host, bool sync = true, bool copy_engine = false);  // storage -> logical complex128
   void check_nonfinite();
 
@@ -510,6 +513,9 @@ class Batch {
     // the chunk's copies in, its SM work (layout kernels, steps) and its copies out are done
     cudaEvent_t in_done = nullptr, sm_done = nullptr, out_done = nullptr;
     std::unique_ptr<Batch> batch;
+    // the chunk's members' logical complex128 arrays back to back (used when the caller's
+    // host arrays are back to back too: one copy per direction instead of one per member)
+    DeviceBuffer stage;
   };
   std::vector<Chunk> chunks_;  // steps_host pipeline (built on first use)
   struct TraceBuf {

@@ -176,3 +176,46 @@ def test_batch_steps_host_pipeline_equals_separate_calls(so):
     bb.steps(2)
     for o, w in zip(outs, bb.get_arrays()):
         assert np.array_equal(o.numpy().view(np.complex128).reshape(w.shape), w)
+
+
+def test_batch_steps_host_back_to_back_arrays(so, monkeypatch):
+    """Host arrays back to back in one pinned buffer (in member order): each pipeline chunk
+    moves with one copy per direction through the chunk's staging buffer.  The results equal
+    set_arrays + steps + get_arrays bit for bit, in place as well, and with only the inputs
+    back to back (outputs in separate buffers: copied per member)."""
+    torch = pytest.importorskip("torch")
+    from split_operator_gb300 import workloads as W
+    monkeypatch.setenv("SO_HOST_CHUNKS", "2")  # two chunks of three members
+    shapes = [(256, 32), (512, 64), (128, 128), (256, 256), (512, 32), (256, 64)]
+    mk = lambda: [W.radial_angular_2d(nr=nr, nth=nth, step_no=10, seed=500 + k, precision="fp32_bf16x6")[0]
+                  for k, (nr, nth) in enumerate(shapes)]
+    pa, pb = mk(), mk()
+    ba, bb = so.Batch(pa), so.Batch(pb)
+    rng = np.random.default_rng(17)
+    states = [rng.normal(size=s) + 1j * rng.normal(size=s) for s in shapes]
+    sizes = [2 * nr * nth for nr, nth in shapes]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    big_in = torch.empty(int(offs[-1]), dtype=torch.float64).pin_memory()
+    big_out = torch.empty_like(big_in).pin_memory()
+    views_in = [big_in[int(offs[k]):int(offs[k + 1])] for k in range(len(shapes))]
+    views_out = [big_out[int(offs[k]):int(offs[k + 1])] for k in range(len(shapes))]
+    for v, s in zip(views_in, states):
+        v.numpy()[:] = s.view(np.float64).ravel()
+    ba.steps_host_ptr([v.data_ptr() for v in views_in], [v.data_ptr() for v in views_out], 3)
+    bb.set_arrays(states)
+    bb.steps(3)
+    for v, w in zip(views_out, bb.get_arrays()):
+        assert np.array_equal(v.numpy().view(np.complex128).reshape(w.shape), w)
+    for x, y in zip(pa, pb):
+        assert x.all_losses() == y.all_losses()
+    # in place on the back-to-back buffer
+    ba.steps_host_ptr([v.data_ptr() for v in views_out], [v.data_ptr() for v in views_out], 2)
+    bb.steps(2)
+    for v, w in zip(views_out, bb.get_arrays()):
+        assert np.array_equal(v.numpy().view(np.complex128).reshape(w.shape), w)
+    # inputs back to back, outputs separate
+    seps = [torch.empty(n, dtype=torch.float64).pin_memory() for n in sizes]
+    ba.steps_host_ptr([v.data_ptr() for v in views_out], [t.data_ptr() for t in seps], 1)
+    bb.steps(1)
+    for t, w in zip(seps, bb.get_arrays()):
+        assert np.array_equal(t.numpy().view(np.complex128).reshape(w.shape), w)
