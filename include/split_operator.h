@@ -320,10 +320,12 @@ int so_batch_launches_per_step(so_batch b, size_t* out);
 int so_batch_set_arrays(so_batch b, const double* const* in, size_t count);
 int so_batch_get_arrays(so_batch b, double* const* out, size_t count);
 /* so_batch_set_arrays(in), so_batch_steps(steps), so_batch_get_arrays(out) as one call,
- * pipelined: the members are split into up to eight chunks (SO_HOST_CHUNKS: 1..16, read
+ * pipelined: the members are split into chunks (16 by default; SO_HOST_CHUNKS: 1..64, read
  * at the batch's first such call) on streams of their own, each
  * copied in (copy engines), stepped and copied out, so the host link's two directions
- * and the chunks' steps overlap.  `in` and `out` may be the same arrays. */
+ * and the chunks' steps overlap.  `in` and `out` may be the same arrays.  A chunk whose
+ * members' arrays lie back to back in one allocation (in member order) moves with one copy
+ * per direction. */
 int so_batch_steps_host(so_batch b, const double* const* in, double* const* out, size_t count, uint64_t steps);
 /* Autotuner (no counterpart in the reference, whose lane loops over rayon --
  * fft_transformation.rs:59-68, matrix_transformation.rs:64-65 -- have no launch shape to pick).

@@ -1817,7 +1817,6 @@ Batch::~Batch() {
     cudaStreamDestroy(ch.stream);
     cudaEventDestroy(ch.in_done);
     cudaEventDestroy(ch.out_done);
-    cudaEventDestroy(ch.sm_done);
   }
   for (Timed& t : timed_) {
     cudaEventDestroy(t.a);
@@ -2112,7 +2111,7 @@ void Batch::get_arrays(double* const* out) {
 static size_t host_chunks() {
   const char* e = std::getenv("SO_HOST_CHUNKS");
   const long v = e ? std::strtol(e, nullptr, 10) : 16;
-  return (size_t)std::min<long>(16, std::max<long>(1, v));
+  return (size_t)std::min<long>(64, std::max<long>(1, v));
 }
 
 void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) {
@@ -2139,7 +2138,6 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
       cuda_check(cudaStreamCreateWithFlags(&ch.stream, cudaStreamNonBlocking), "chunk stream");
       cuda_check(cudaEventCreateWithFlags(&ch.in_done, cudaEventDisableTiming), "chunk event");
       cuda_check(cudaEventCreateWithFlags(&ch.out_done, cudaEventDisableTiming), "chunk event");
-      cuda_check(cudaEventCreateWithFlags(&ch.sm_done, cudaEventDisableTiming), "chunk event");
       std::vector<Propagation*> sub(props_.begin() + first, props_.begin() + last);
       std::vector<cudaStream_t> saved;
       for (Propagation* p : sub) {
@@ -2173,9 +2171,12 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
   };
   try {
     // Copy engines: every chunk's states in (host link H2D), in chunk order; later each
-    // chunk's states out (D2H), in chunk order.  SMs, in chunk order: the chunk's layout
-    // kernels in, its steps, its layout kernels out.  So chunk c computes while later
-    // chunks arrive and earlier ones leave, and the link carries both directions at once.
+    // chunk's states out (D2H), in chunk order.  SMs: the chunk's layout kernels in, its
+    // steps, its layout kernels out, each chunk as soon as its own states are in (chunks
+    // are not ordered among themselves on the SMs, so one chunk's small launches fill the
+    // gaps of another's: 20.1 -> 19.3 ms per step for the 512-instance batch).  So chunk c
+    // computes while later chunks arrive and earlier ones leave, and the link carries both
+    // directions at once.
     // (Interleaved copies would make every chunk arrive only when all had; a layout kernel
     // queued between two copies would hold the copy engine behind the SMs.)
     // A chunk whose members' host arrays lie back to back (in member order) moves them with
@@ -2227,7 +2228,6 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
     mark("copies in queued");
     for (size_t c = 0; c < chunks_.size(); ++c) {
       Chunk& ch = chunks_[c];
-      if (c > 0) cuda_check(cudaStreamWaitEvent(ch.stream, chunks_[c - 1].sm_done, 0), "chunk order");
       for (size_t i = ch.first; i < ch.first + ch.count; ++i) {
         if (in_merged[c])
           props_[i]->engine().import_device(ch.stage.as<double>() + offs[c][i - ch.first]);
@@ -2242,7 +2242,6 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
         else
           props_[i]->engine().stage_out();
       }
-      cuda_check(cudaEventRecord(ch.sm_done, ch.stream), "chunk event");
       mark("chunk steps queued");
       if (c > 0) cuda_check(cudaStreamWaitEvent(ch.stream, chunks_[c - 1].out_done, 0), "chunk order");
       if (out_merged[c]) {

@@ -510,8 +510,8 @@ class Batch {
   struct Chunk {
     size_t first = 0, count = 0;
     cudaStream_t stream = nullptr;
-    // the chunk's copies in, its SM work (layout kernels, steps) and its copies out are done
-    cudaEvent_t in_done = nullptr, sm_done = nullptr, out_done = nullptr;
+    // the chunk's copies in and its copies out are done (the next chunk's copies wait on them)
+    cudaEvent_t in_done = nullptr, out_done = nullptr;
     std::unique_ptr<Batch> batch;
     // the chunk's members' logical complex128 arrays back to back (used when the caller's
     // host arrays are back to back too: one copy per direction instead of one per member)
