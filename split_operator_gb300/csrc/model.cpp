@@ -2125,11 +2125,17 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
     double total = 0.0;
     for (Propagation* p : props_) total += (double)p->engine().points();
     const size_t k = std::min<size_t>(kHostChunks, m);
+    // the first and the last chunk get half the points of the others: the link carries one
+    // direction alone while the first chunk comes in and the last goes out (512-instance
+    // batch, 16 chunks: 19.2 -> 19.0 ms per step; a third of the others: 19.1 ms)
+    const double taper = 0.5;
+    std::vector<double> wsum(k + 1, 0.0);
+    for (size_t c = 0; c < k; ++c) wsum[c + 1] = wsum[c] + ((k > 2 && (c == 0 || c + 1 == k)) ? taper : 1.0);
     size_t first = 0;
     double acc = 0.0;
     for (size_t c = 0; c < k; ++c) {
       size_t last = first;
-      const double goal = total * (double)(c + 1) / (double)k;
+      const double goal = total * wsum[c + 1] / wsum[k];
       while (last < m && (c + 1 == k || acc < goal || last == first)) acc += (double)props_[last++]->engine().points();
       if (last == first) break;
       Chunk ch;
