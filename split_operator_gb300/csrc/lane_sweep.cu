@@ -1015,7 +1015,7 @@ __global__ void __launch_bounds__(512, 1) fft_pair_kernel_f64(const __grid_const
   fft_pair_tile<double, 8>(p, blockIdx.x);
 }
 
-// float-float lanes of 8192 points (as FP64)
+// float-float lanes of 512-8192 points (radix-8 stages, the FP64 table order)
 __global__ void __launch_bounds__(512, 1) fft_pair_kernel_ff(const __grid_constant__ PassParams p) {
   fft_pair_tile<ff, 8>(p, blockIdx.x);
 }
