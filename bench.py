@@ -145,7 +145,8 @@ def kernel_of(group_name):
     if "tc3xtf32" in group_name or "tcbf16x3" in group_name or "tcbf16x6" in group_name:
         return "angular_tc_kernel_batched"
     if "fftpair" in group_name:
-        return "fft_pair_kernel_batched"
+        # float-float pairs run their own instantiation
+        return "fft_pair_kernel_batched_ff" if " ff " in f" {group_name} " else "fft_pair_kernel_batched"
     if "scalar" in group_name:
         return "scalar_program_kernel"
     return "pass_kernel_batched"

@@ -18,6 +18,8 @@ def test_kernel_names_of_batched_groups():
     assert bench.kernel_of("batched 5x f32 tcbf16x3 parity axis1: mat") == "angular_tc_kernel_batched"
     assert bench.kernel_of("batched 9x f32 sweep fftpair axis0: fft diag1d fft diagnd") == "fft_pair_kernel_batched"
     assert bench.kernel_of("batched 9x f64 sweep axis0: fft diag1d fft diagnd") == "pass_kernel_batched"
+    assert bench.kernel_of("batched 9x ff sweep fftpair axis0: fft diag1d fft diagnd") == "fft_pair_kernel_batched_ff"
+    assert bench.kernel_of("batched 9x ff sweep axis1: mat diagnd norm") == "pass_kernel_batched"
 
 
 def test_roofline_aggregates_all_launches_of_the_dominant_kernel():
