@@ -2201,8 +2201,10 @@ void Batch::steps_host(const double* const* in, double* const* out, uint64_t n) 
         const size_t pts = props_[i]->engine().points();
         if (i > ch.first) {
           const size_t prev = props_[i - 1]->engine().points();
-          ic = ic && in[i] == in[i - 1] + 2 * prev;
-          oc = oc && out[i] == out[i - 1] + 2 * prev;
+          // addresses compared as integers (the arrays are separate objects to the language)
+          const uintptr_t step = 2 * prev * sizeof(double);
+          ic = ic && reinterpret_cast<uintptr_t>(in[i]) == reinterpret_cast<uintptr_t>(in[i - 1]) + step;
+          oc = oc && reinterpret_cast<uintptr_t>(out[i]) == reinterpret_cast<uintptr_t>(out[i - 1]) + step;
         }
         total += 2 * pts;
       }
